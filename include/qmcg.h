@@ -1,0 +1,184 @@
+/* qmcg — GB300-native batched particle-by-particle Slater-Jastrow move loop.
+ *
+ * C ABI over opaque handles.  Plain pointers and sizes only; every function
+ * returns QMCG_OK (0) or a negative error code and never throws.  One crowd
+ * handle belongs to one host thread (like one QMCPACK crowd); all work of a
+ * crowd runs on that crowd's own CUDA stream.
+ *
+ * The entry points mirror the static batched ("mw_") calls the reference's
+ * batched VMC/DMC drivers make for one crowd (QMCPACK 4.3.0):
+ *   TrialWaveFunction::mw_*  src/QMCWaveFunctions/TrialWaveFunction.cpp
+ *   ParticleSet::mw_*        src/Particle/ParticleSet.cpp
+ * Positions, gradients and ratios cross the ABI as FP64 host arrays, as the
+ * reference's TWFGrads<POS> / std::vector<PsiValue> do.
+ */
+#ifndef QMCG_H
+#define QMCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- errors */
+#define QMCG_OK 0
+#define QMCG_ERR_ARG (-1)        /* invalid argument or size                       */
+#define QMCG_ERR_CUDA (-2)       /* a CUDA call failed (see qmcg_last_error)       */
+#define QMCG_ERR_SINGULAR (-3)   /* zero pivot in the FP64 inverse                 */
+#define QMCG_ERR_NONFINITE (-4)  /* NaN/Inf ratio or gradient (NaNguard)           */
+#define QMCG_ERR_ZERO_RATIO (-5) /* accepted move with a zero determinant ratio    */
+#define QMCG_ERR_STATE (-6)      /* call out of sequence                           */
+#define QMCG_ERR_NO_DEVICE (-7)  /* no usable CUDA device                          */
+
+typedef struct qmcg_system_s* qmcg_system;
+typedef struct qmcg_crowd_s* qmcg_crowd;
+
+/* A Slater-Jastrow system: what QMCPACK reads from its XML input for this path.
+ *   cell       orthorhombic, periodic in x, y, z (DTD_BConds<T,3,PPPO>,
+ *              src/Particle/Lattice/ParticleBConds3DSoa.h:94-185)
+ *   orbitals   real Gamma-point orbitals as one periodic tricubic multi-B-spline
+ *              (SplineR2R, src/QMCWaveFunctions/BsplineFactory/SplineR2R.h), coefficient
+ *              table [gx+3][gy+3][gz+3][num_orbitals_padded] in the einspline ghost
+ *              layout (src/spline2/MultiBsplineBase.hpp:75-130), orbital index fastest
+ *   J1, J2     cusp-corrected B-spline radial functors (BsplineFunctor::reset,
+ *              src/QMCWaveFunctions/Jastrow/BsplineFunctor.h:117-133); J2 functor 0 acts
+ *              between equal spins, functor 1 between opposite spins.
+ * Both spin determinants use the same orbital set, so n_up == n_dn == num_orbitals. */
+typedef struct
+{
+  int precision;           /* 8: FP64 move loop; 4: FP32 move loop with FP64 recompute */
+  int n_up, n_dn;
+  int num_orbitals;
+  int num_orbitals_padded; /* multiple of 16 */
+  double lattice[3];       /* cell lengths, bohr */
+  int num_ions;
+  const double* ion_pos;   /* [num_ions][3] */
+  const int* ion_species;  /* [num_ions], 0 <= species < num_ion_species */
+  int num_ion_species;
+  int grid[3];             /* unique periodic grid points per axis */
+  const void* spline_coefs;/* float (precision 4) or double (precision 8) */
+  int j1_num_params;       /* 0 disables J1 */
+  double j1_rcut;
+  const double* j1_params; /* [num_ion_species][j1_num_params] */
+  const double* j1_cusp;   /* [num_ion_species] */
+  int j2_num_params;       /* 0 disables J2 */
+  double j2_rcut;
+  const double* j2_params; /* [2][j2_num_params] */
+  const double* j2_cusp;   /* [2] */
+} qmcg_system_desc;
+
+/* Driver parameters of one VMC sweep loop (VMCBatched::advanceWalkers,
+ * src/QMCDrivers/VMC/VMCBatched.cpp:57-228).
+ * rng_mode 0: the bit-compatible stream of the reference — std::mt19937 seeded
+ *             with `seed`, Box-Muller Gaussians [iat][iw][xyz] per sweep and one
+ *             uniform per walker and electron consumed only when the move is valid
+ *             and |ratio|^2 >= epsilon (StdRandom.h:34-59, RandomSeqGenerator.h:33-51,
+ *             VMCBatched.cpp:109,156-158); the host generates it between sweeps.
+ * rng_mode 1: counter-based Philox4x32-10 on the device, no host round trip. */
+typedef struct
+{
+  double tau;
+  int use_drift;
+  int rng_mode;
+  uint64_t seed;
+  int recompute_every; /* FP64 recompute after every this many sweeps; 0 = never */
+} qmcg_sweep_params;
+
+typedef struct
+{
+  uint64_t accepted;
+  uint64_t rejected;
+  int status;          /* OR of walker status bits since the last call */
+} qmcg_sweep_stats;
+
+/* ---------------------------------------------------------------- library */
+const char* qmcg_last_error(void);   /* message of the last failed call on this thread */
+int qmcg_device_count(int* count);
+
+/* ---------------------------------------------------------------- system */
+/* Builds the device-resident system (spline table, ions, Jastrow functors).
+ * Replaces the construction done by EinsplineSetBuilder / RadialJastrowBuilder
+ * for the SPOSet and Jastrow objects of one TrialWaveFunction. */
+int qmcg_system_create(const qmcg_system_desc* desc, qmcg_system* out);
+int qmcg_system_destroy(qmcg_system sys);
+
+/* ---------------------------------------------------------------- crowd */
+/* nw walkers with delay rank k (k = 1: Sherman-Morrison rank-1).  Replaces the
+ * per-crowd resources acquired by TrialWaveFunction::acquireResource /
+ * ParticleSet::acquireResource (src/QMCWaveFunctions/WaveFunctionComponent.h:424-436). */
+int qmcg_crowd_create(qmcg_system sys, int num_walkers, int delay_rank, qmcg_crowd* out);
+int qmcg_crowd_destroy(qmcg_crowd crowd);
+/* the crowd's cudaStream_t, for callers that time or order work around it */
+int qmcg_crowd_stream(qmcg_crowd crowd, void** stream);
+
+/* R: [nw][n_elec][3] FP64.  Replaces copying walker positions into the ParticleSets
+ * (ParticleSet::loadWalker, src/Particle/ParticleSet.cpp). */
+int qmcg_load_walkers(qmcg_crowd crowd, const double* R);
+int qmcg_get_positions(qmcg_crowd crowd, double* R);
+
+/* Full recompute of every walker: all-electron orbitals, FP64 inverse and log
+ * det, J1/J2 state.  TrialWaveFunction::mw_evaluateLog / mw_recompute
+ * (src/QMCWaveFunctions/TrialWaveFunction.cpp:161-260).  log_psi, signs may be NULL. */
+int qmcg_mw_evaluate_log(qmcg_crowd crowd, double* log_psi, int* signs);
+
+/* TrialWaveFunction::mw_prepareGroup (TrialWaveFunction.cpp:523): no-op kept for the call sequence. */
+int qmcg_mw_prepare_group(qmcg_crowd crowd, int group);
+
+/* grads [nw][3]: gradient of log psi w.r.t. electron iat at the current positions.
+ * TrialWaveFunction::mw_evalGrad (TrialWaveFunction.cpp:568-595). */
+int qmcg_mw_eval_grad(qmcg_crowd crowd, int iat, double* grads);
+
+/* Propose r_iat + displ[iw] for every walker and build the distance rows.
+ * ParticleSet::mw_makeMove (src/Particle/ParticleSet.cpp:397-427).  valid[nw] may be
+ * NULL; a fully periodic cell makes every move valid. */
+int qmcg_mw_make_move(qmcg_crowd crowd, int iat, const double* displ, int* valid);
+
+/* ratios [nw] psi(new)/psi(old), grads [nw][3] gradient of log psi at the proposed
+ * position.  TrialWaveFunction::mw_calcRatioGrad (TrialWaveFunction.cpp:685-772). */
+int qmcg_mw_calc_ratio_grad(qmcg_crowd crowd, int iat, double* ratios, double* grads);
+
+/* accepted [nw] (0/1).  TrialWaveFunction::mw_accept_rejectMove (TrialWaveFunction.cpp:790-821)
+ * together with ParticleSet::mw_accept_rejectMove (ParticleSet.cpp:717-758). */
+int qmcg_mw_accept_reject_move(qmcg_crowd crowd, int iat, const int* accepted);
+
+/* Flush pending delayed updates.  TrialWaveFunction::mw_completeUpdates (TrialWaveFunction.cpp:833). */
+int qmcg_mw_complete_updates(qmcg_crowd crowd);
+
+/* Tracked log|psi| per walker (determinant logs accumulated from accepted ratios plus
+ * the Jastrow state), signs (+1/-1), parts [nw][4] = log|det_up|, log|det_dn|, log J1,
+ * log J2.  Any pointer may be NULL. */
+int qmcg_get_log(qmcg_crowd crowd, double* log_psi, int* signs, double* parts);
+
+/* Ainv = (M^-1)^T of spin s, [nw][N][N] as FP64 (DiracDeterminantBatched::get_psiMinv). */
+int qmcg_get_inverse(qmcg_crowd crowd, int spin, double* ainv);
+
+/* J2 [nw][5][n_elec] = Uat, dUat xyz, d2Uat; J1 [nw][5][n_elec] = Vat, Grad xyz, Lap.  Either may be NULL. */
+int qmcg_get_jastrow_state(qmcg_crowd crowd, double* j2, double* j1);
+
+/* Orbital value, gradient xyz and Laplacian at the proposed position, [nw][5][N]
+ * (the phi_vgl_v array of SplineR2R::mw_evaluateVGLandDetRatioGrads). */
+int qmcg_get_phi_vgl(qmcg_crowd crowd, double* phi);
+
+/* Device-resident VMC sweeps: num_sweeps x (every electron proposed, tested and
+ * accepted or rejected for every walker), then mw_completeUpdates, with the FP64
+ * recompute every params->recompute_every sweeps.  Replaces the body of
+ * VMCBatched::advanceWalkers (VMCBatched.cpp:106-177); runs as one captured CUDA
+ * graph per sweep.  accept_log [num_sweeps][n_elec][nw] (0/1) may be NULL. */
+int qmcg_vmc_sweeps(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, qmcg_sweep_stats* stats,
+                    int* accept_log);
+
+/* Replays the captured sweep graph num_sweeps times with counter-based random
+ * numbers and returns without synchronizing (timing helper for benchmarks; the
+ * graph must have been built by a previous qmcg_vmc_sweeps with rng_mode 1). */
+int qmcg_vmc_sweeps_async(qmcg_crowd crowd, int num_sweeps);
+
+/* Waits for the crowd's stream, then reports and clears the walker status bits. */
+int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMCG_H */

@@ -1,0 +1,98 @@
+"""ctypes binding of libqmcg.so (the C ABI declared in include/qmcg.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqmcg.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+# every symbol the header declares, in declaration order
+EXPORTS = [
+    "qmcg_last_error", "qmcg_device_count", "qmcg_system_create", "qmcg_system_destroy",
+    "qmcg_crowd_create", "qmcg_crowd_destroy", "qmcg_crowd_stream", "qmcg_load_walkers",
+    "qmcg_get_positions", "qmcg_mw_evaluate_log", "qmcg_mw_prepare_group", "qmcg_mw_eval_grad",
+    "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
+    "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
+    "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
+]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int), ("n_up", C.c_int), ("n_dn", C.c_int), ("num_orbitals", C.c_int),
+        ("num_orbitals_padded", C.c_int), ("lattice", C.c_double * 3), ("num_ions", C.c_int),
+        ("ion_pos", _dp), ("ion_species", _ip), ("num_ion_species", C.c_int), ("grid", C.c_int * 3),
+        ("spline_coefs", C.c_void_p), ("j1_num_params", C.c_int), ("j1_rcut", C.c_double),
+        ("j1_params", _dp), ("j1_cusp", _dp), ("j2_num_params", C.c_int), ("j2_rcut", C.c_double),
+        ("j2_params", _dp), ("j2_cusp", _dp),
+    ]
+
+
+class SweepParams(C.Structure):
+    _fields_ = [("tau", C.c_double), ("use_drift", C.c_int), ("rng_mode", C.c_int), ("seed", C.c_uint64),
+                ("recompute_every", C.c_int)]
+
+
+class SweepStats(C.Structure):
+    _fields_ = [("accepted", C.c_uint64), ("rejected", C.c_uint64), ("status", C.c_int)]
+
+
+_LIB = None
+
+
+class QmcgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"qmcg error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built (no CPU fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with python -m qmcpack_gb300.build "
+                          "(the move loop has no CPU fallback)")
+    L = C.CDLL(path)
+    L.qmcg_last_error.restype = C.c_char_p
+    vp = C.c_void_p
+    sig = {
+        "qmcg_device_count": [_ip],
+        "qmcg_system_create": [C.POINTER(SystemDesc), C.POINTER(vp)],
+        "qmcg_system_destroy": [vp],
+        "qmcg_crowd_create": [vp, C.c_int, C.c_int, C.POINTER(vp)],
+        "qmcg_crowd_destroy": [vp],
+        "qmcg_crowd_stream": [vp, C.POINTER(vp)],
+        "qmcg_load_walkers": [vp, _dp],
+        "qmcg_get_positions": [vp, _dp],
+        "qmcg_mw_evaluate_log": [vp, _dp, _ip],
+        "qmcg_mw_prepare_group": [vp, C.c_int],
+        "qmcg_mw_eval_grad": [vp, C.c_int, _dp],
+        "qmcg_mw_make_move": [vp, C.c_int, _dp, _ip],
+        "qmcg_mw_calc_ratio_grad": [vp, C.c_int, _dp, _dp],
+        "qmcg_mw_accept_reject_move": [vp, C.c_int, _ip],
+        "qmcg_mw_complete_updates": [vp],
+        "qmcg_get_log": [vp, _dp, _ip, _dp],
+        "qmcg_get_inverse": [vp, C.c_int, _dp],
+        "qmcg_get_jastrow_state": [vp, _dp, _dp],
+        "qmcg_get_phi_vgl": [vp, _dp],
+        "qmcg_vmc_sweeps": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats), _ip],
+        "qmcg_vmc_sweeps_async": [vp, C.c_int],
+        "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    _LIB = L
+    return L
+
+
+def check(rc: int):
+    if rc != 0:
+        raise QmcgError(rc, load().qmcg_last_error().decode())

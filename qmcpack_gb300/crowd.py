@@ -1,0 +1,184 @@
+"""Host-side mirror of the reference's batched (mw_) interface for one crowd.
+
+The method names and argument meanings follow QMCPACK's static batched calls
+(TrialWaveFunction::mw_* in src/QMCWaveFunctions/TrialWaveFunction.cpp and
+ParticleSet::mw_* in src/Particle/ParticleSet.cpp); every call goes through the
+C ABI of libqmcg.so to the sm_103a kernels.  Errors raise QmcgError (the
+reference throws std::runtime_error for the same conditions).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import QmcgError, SweepParams, SweepStats, SystemDesc, check
+from .system import System
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class DeviceSystem:
+    """Device-resident system: spline table, ions and Jastrow functors."""
+
+    def __init__(self, system: System):
+        L = _lib.load()
+        s = system
+        self.system = s
+        prec = s.spec.precision
+        coef_dtype = np.float64 if prec == 8 else np.float32
+        self._coefs = np.ascontiguousarray(s.coefs, dtype=coef_dtype)
+        self._ions = _d(s.ion_pos)
+        self._spec = np.ascontiguousarray(s.ion_species, np.int32)
+        self._j1p, self._j1c = _d(s.j1_params), _d(s.j1_cusp)
+        self._j2p, self._j2c = _d(s.j2_params), _d(s.j2_cusp)
+        d = SystemDesc()
+        d.precision = prec
+        d.n_up, d.n_dn = s.spec.n_up, s.spec.n_dn
+        d.num_orbitals, d.num_orbitals_padded = s.norb, s.npad
+        d.lattice = (C.c_double * 3)(*[float(x) for x in s.lattice])
+        d.num_ions = len(self._ions)
+        d.ion_pos = _p(self._ions)
+        d.ion_species = _p(self._spec, _ip)
+        d.num_ion_species = s.n_ion_species
+        d.grid = (C.c_int * 3)(*[int(x) for x in s.grid])
+        d.spline_coefs = self._coefs.ctypes.data
+        d.j1_num_params, d.j1_rcut = self._j1p.shape[1], s.spec.j1_rcut
+        d.j1_params, d.j1_cusp = _p(self._j1p), _p(self._j1c)
+        d.j2_num_params, d.j2_rcut = self._j2p.shape[1], s.spec.j2_rcut
+        d.j2_params, d.j2_cusp = _p(self._j2p), _p(self._j2c)
+        self.handle = C.c_void_p()
+        check(L.qmcg_system_create(C.byref(d), C.byref(self.handle)))
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            _lib.load().qmcg_system_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+
+class Crowd:
+    """nw walkers of one system; one CUDA stream; the mw_ call sequence."""
+
+    def __init__(self, dsys: DeviceSystem, nw: int, delay_rank: int):
+        self.L = _lib.load()
+        self.dsys = dsys
+        self.nw, self.k = nw, delay_rank
+        s = dsys.system
+        self.ne, self.norb, self.nup = s.n_elec, s.norb, s.spec.n_up
+        self.handle = C.c_void_p()
+        check(self.L.qmcg_crowd_create(dsys.handle, nw, delay_rank, C.byref(self.handle)))
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            self.L.qmcg_crowd_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    # ---- ParticleSet side
+    def load_walkers(self, R):
+        R = _d(R)
+        assert R.shape == (self.nw, self.ne, 3)
+        check(self.L.qmcg_load_walkers(self.handle, _p(R)))
+
+    def positions(self):
+        R = np.zeros((self.nw, self.ne, 3))
+        check(self.L.qmcg_get_positions(self.handle, _p(R)))
+        return R
+
+    def mw_makeMove(self, iat: int, displ):
+        d = _d(displ)
+        valid = np.zeros(self.nw, np.int32)
+        check(self.L.qmcg_mw_make_move(self.handle, iat, _p(d), _p(valid, _ip)))
+        return valid.astype(bool)
+
+    # ---- TrialWaveFunction side
+    def mw_evaluateLog(self):
+        lp = np.zeros(self.nw)
+        sg = np.zeros(self.nw, np.int32)
+        check(self.L.qmcg_mw_evaluate_log(self.handle, _p(lp), _p(sg, _ip)))
+        return lp, sg
+
+    def mw_prepareGroup(self, group: int):
+        check(self.L.qmcg_mw_prepare_group(self.handle, group))
+
+    def mw_evalGrad(self, iat: int):
+        g = np.zeros((self.nw, 3))
+        check(self.L.qmcg_mw_eval_grad(self.handle, iat, _p(g)))
+        return g
+
+    def mw_calcRatioGrad(self, iat: int):
+        r = np.zeros(self.nw)
+        g = np.zeros((self.nw, 3))
+        check(self.L.qmcg_mw_calc_ratio_grad(self.handle, iat, _p(r), _p(g)))
+        return r, g
+
+    def mw_accept_rejectMove(self, iat: int, accepted):
+        a = np.ascontiguousarray(np.asarray(accepted).astype(np.int32))
+        check(self.L.qmcg_mw_accept_reject_move(self.handle, iat, _p(a, _ip)))
+
+    def mw_completeUpdates(self):
+        check(self.L.qmcg_mw_complete_updates(self.handle))
+
+    # ---- state readback
+    def get_log(self):
+        lp = np.zeros(self.nw)
+        sg = np.zeros(self.nw, np.int32)
+        parts = np.zeros((self.nw, 4))
+        check(self.L.qmcg_get_log(self.handle, _p(lp), _p(sg, _ip), _p(parts)))
+        return lp, sg, parts
+
+    def inverse(self, spin: int):
+        a = np.zeros((self.nw, self.norb, self.norb))
+        check(self.L.qmcg_get_inverse(self.handle, spin, _p(a)))
+        return a
+
+    def jastrow_state(self):
+        j2 = np.zeros((self.nw, 5, self.ne))
+        j1 = np.zeros((self.nw, 5, self.ne))
+        check(self.L.qmcg_get_jastrow_state(self.handle, _p(j2), _p(j1)))
+        return j2, j1
+
+    def phi_vgl(self):
+        out = np.zeros((self.nw, 5, self.norb))
+        check(self.L.qmcg_get_phi_vgl(self.handle, _p(out)))
+        return out
+
+    # ---- device-resident sweeps
+    def vmc_sweeps(self, nsweeps: int, tau: float, seed: int, rng_mode: int = 1, use_drift: bool = True,
+                   recompute_every: int = 0, log_accepts: bool = False):
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=rng_mode, seed=seed,
+                        recompute_every=recompute_every)
+        st = SweepStats()
+        acc = np.zeros((nsweeps, self.ne, self.nw), np.int32) if log_accepts else None
+        check(self.L.qmcg_vmc_sweeps(self.handle, C.byref(p), nsweeps, C.byref(st),
+                                     _p(acc, _ip) if acc is not None else None))
+        return st.accepted, st.rejected, acc
+
+    def vmc_sweeps_async(self, nsweeps: int):
+        check(self.L.qmcg_vmc_sweeps_async(self.handle, nsweeps))
+
+    def sync(self):
+        st = SweepStats()
+        check(self.L.qmcg_crowd_sync(self.handle, C.byref(st)))
+        return st.accepted, st.rejected
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        check(self.L.qmcg_crowd_stream(self.handle, C.byref(p)))
+        return p.value or 0

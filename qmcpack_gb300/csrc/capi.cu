@@ -1,0 +1,998 @@
+// C ABI of the library (include/qmcg.h): system and crowd handles, device
+// memory, the mw_ call sequence and the captured sweep graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/qmcg.h"
+#include "common.cuh"
+#include "launch.h"
+
+using namespace qmcg;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg)
+{
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                                                 \
+  do                                                                                                                   \
+  {                                                                                                                    \
+    cudaError_t e_ = (expr);                                                                                           \
+    if (e_ != cudaSuccess)                                                                                             \
+      return fail(QMCG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));                                \
+  } while (0)
+
+extern "C" const char* qmcg_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int qmcg_device_count(int* count)
+{
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess)
+    n = 0;
+  if (count)
+    *count = n;
+  return n > 0 ? QMCG_OK : fail(QMCG_ERR_NO_DEVICE, "no CUDA device");
+}
+
+// ---------------------------------------------------------------------------
+// device memory owned by a handle
+// ---------------------------------------------------------------------------
+struct DeviceArena
+{
+  std::vector<void*> ptrs;
+  ~DeviceArena()
+  {
+    for (void* p : ptrs)
+      cudaFree(p);
+  }
+  template<typename X>
+  cudaError_t alloc(X** p, size_t count)
+  {
+    void* q       = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(X));
+    if (e != cudaSuccess)
+      return e;
+    ptrs.push_back(q);
+    e = cudaMemset(q, 0, std::max<size_t>(count, 1) * sizeof(X));
+    *p = static_cast<X*>(q);
+    return e;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// system
+// ---------------------------------------------------------------------------
+struct qmcg_system_s
+{
+  int prec;
+  int nup, ndn, ne, norb, lda, nions, nions_pad, nion_species;
+  int grid[3];
+  double L[3];
+  DeviceArena mem;
+  void* coefs = nullptr;
+  void* ions  = nullptr;
+  int* ion_species = nullptr;
+  void* j1c = nullptr;
+  void* j2c = nullptr;
+  int j1_ncoef = 0, j2_ncoef = 0;
+  double j1_rcut = 0, j2_rcut = 0;
+  double j1_dri = 0, j2_dri = 0;
+  int has_j1 = 0, has_j2 = 0;
+};
+
+// BsplineFunctor::reset (BsplineFunctor.h:117-133) in the functor precision T
+template<typename T>
+static void functor_coefs(int nparams, double cutoff, const double* params, double cusp, std::vector<T>& out,
+                          double& dri)
+{
+  const int numCoefs = nparams + 4;
+  const int numKnots = numCoefs - 2;
+  const T DeltaR     = static_cast<T>(cutoff) / static_cast<T>(numKnots - 1);
+  const T DeltaRInv  = T(1.0) / DeltaR;
+  std::vector<T> c(numCoefs, T(0));
+  c[1] = static_cast<T>(params[0]);
+  c[2] = static_cast<T>(params[1]);
+  c[0] = static_cast<T>(params[1]) - T(2.0) * DeltaR * static_cast<T>(cusp);
+  for (int i = 2; i < nparams; i++)
+    c[i + 1] = static_cast<T>(params[i]);
+  out.insert(out.end(), c.begin(), c.end());
+  dri = static_cast<double>(DeltaRInv);
+}
+
+template<typename T>
+static int build_system(const qmcg_system_desc* d, qmcg_system_s* s)
+{
+  const size_t ncoef = (size_t)(d->grid[0] + 3) * (d->grid[1] + 3) * (d->grid[2] + 3) * d->num_orbitals_padded;
+  T* coefs;
+  CUDA_TRY(s->mem.alloc(&coefs, ncoef));
+  CUDA_TRY(cudaMemcpy(coefs, d->spline_coefs, ncoef * sizeof(T), cudaMemcpyHostToDevice));
+  s->coefs = coefs;
+  std::vector<T> ions((size_t)3 * s->nions_pad, T(0));
+  for (int i = 0; i < d->num_ions; i++)
+    for (int k = 0; k < 3; k++)
+      ions[(size_t)k * s->nions_pad + i] = static_cast<T>(d->ion_pos[i * 3 + k]);
+  T* dions;
+  CUDA_TRY(s->mem.alloc(&dions, ions.size()));
+  CUDA_TRY(cudaMemcpy(dions, ions.data(), ions.size() * sizeof(T), cudaMemcpyHostToDevice));
+  s->ions = dions;
+  std::vector<int> spc(std::max(d->num_ions, 1), 0);
+  for (int i = 0; i < d->num_ions; i++)
+    spc[i] = d->ion_species ? d->ion_species[i] : 0;
+  CUDA_TRY(s->mem.alloc(&s->ion_species, spc.size()));
+  CUDA_TRY(cudaMemcpy(s->ion_species, spc.data(), spc.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (s->has_j1)
+  {
+    std::vector<T> c;
+    for (int sp = 0; sp < d->num_ion_species; sp++)
+      functor_coefs<T>(d->j1_num_params, d->j1_rcut, d->j1_params + (size_t)sp * d->j1_num_params,
+                       d->j1_cusp ? d->j1_cusp[sp] : 0.0, c, s->j1_dri);
+    T* dc;
+    CUDA_TRY(s->mem.alloc(&dc, c.size()));
+    CUDA_TRY(cudaMemcpy(dc, c.data(), c.size() * sizeof(T), cudaMemcpyHostToDevice));
+    s->j1c      = dc;
+    s->j1_ncoef = d->j1_num_params + 4;
+  }
+  if (s->has_j2)
+  {
+    std::vector<T> c;
+    for (int p = 0; p < 2; p++)
+      functor_coefs<T>(d->j2_num_params, d->j2_rcut, d->j2_params + (size_t)p * d->j2_num_params,
+                       d->j2_cusp ? d->j2_cusp[p] : 0.0, c, s->j2_dri);
+    T* dc;
+    CUDA_TRY(s->mem.alloc(&dc, c.size()));
+    CUDA_TRY(cudaMemcpy(dc, c.data(), c.size() * sizeof(T), cudaMemcpyHostToDevice));
+    s->j2c      = dc;
+    s->j2_ncoef = d->j2_num_params + 4;
+  }
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_system_create(const qmcg_system_desc* d, qmcg_system* out)
+{
+  if (!d || !out)
+    return fail(QMCG_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (d->precision != 4 && d->precision != 8)
+    return fail(QMCG_ERR_ARG, "precision must be 4 or 8");
+  if (d->n_up <= 0 || d->n_up != d->n_dn || d->num_orbitals != d->n_up)
+    return fail(QMCG_ERR_ARG, "need n_up == n_dn == num_orbitals > 0");
+  if (d->num_orbitals_padded < d->num_orbitals || d->num_orbitals_padded % 16 != 0)
+    return fail(QMCG_ERR_ARG, "num_orbitals_padded must be a multiple of 16 and >= num_orbitals");
+  for (int k = 0; k < 3; k++)
+  {
+    if (!(d->lattice[k] > 0))
+      return fail(QMCG_ERR_ARG, "lattice lengths must be positive (periodic orthorhombic cell)");
+    if (d->grid[k] < 1)
+      return fail(QMCG_ERR_ARG, "grid must be >= 1");
+  }
+  if (!d->spline_coefs || (d->num_ions > 0 && !d->ion_pos))
+    return fail(QMCG_ERR_ARG, "missing spline coefficients or ion positions");
+  if (d->num_ions < 0 || (d->num_ions > 0 && d->num_ion_species < 1))
+    return fail(QMCG_ERR_ARG, "bad ion count or species count");
+  if (d->ion_species)
+    for (int i = 0; i < d->num_ions; i++)
+      if (d->ion_species[i] < 0 || d->ion_species[i] >= d->num_ion_species)
+        return fail(QMCG_ERR_ARG, "ion species index out of range");
+  if ((d->j1_num_params > 0 && (!d->j1_params || !(d->j1_rcut > 0))) ||
+      (d->j2_num_params > 0 && (!d->j2_params || !(d->j2_rcut > 0))))
+    return fail(QMCG_ERR_ARG, "Jastrow parameters or cutoff missing");
+  if (d->j1_num_params < 0 || d->j2_num_params < 0 || (d->j1_num_params > 0 && d->j1_num_params < 2) ||
+      (d->j2_num_params > 0 && d->j2_num_params < 2))
+    return fail(QMCG_ERR_ARG, "Jastrow functors need at least 2 parameters");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(QMCG_ERR_NO_DEVICE, "no CUDA device");
+  auto s          = std::make_unique<qmcg_system_s>();
+  s->prec         = d->precision;
+  s->nup          = d->n_up;
+  s->ndn          = d->n_dn;
+  s->ne           = d->n_up + d->n_dn;
+  s->norb         = d->num_orbitals;
+  s->lda          = d->num_orbitals_padded;
+  s->nions        = d->num_ions;
+  s->nions_pad    = std::max(32, ((d->num_ions + 31) / 32) * 32);
+  s->nion_species = std::max(1, d->num_ion_species);
+  for (int k = 0; k < 3; k++)
+  {
+    s->grid[k] = d->grid[k];
+    s->L[k]    = d->lattice[k];
+  }
+  s->has_j1  = (d->j1_num_params > 0 && d->num_ions > 0) ? 1 : 0;
+  s->has_j2  = d->j2_num_params > 0 ? 1 : 0;
+  s->j1_rcut = d->j1_rcut;
+  s->j2_rcut = d->j2_rcut;
+  int rc = d->precision == 8 ? build_system<double>(d, s.get()) : build_system<float>(d, s.get());
+  if (rc != QMCG_OK)
+    return rc;
+  *out = s.release();
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_system_destroy(qmcg_system sys)
+{
+  delete sys;
+  return QMCG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host side of the bit-compatible random stream (StdRandom<double> + Box-Muller)
+// ---------------------------------------------------------------------------
+struct HostStream
+{
+  std::mt19937 eng;
+  std::deque<uint32_t> ahead;
+  void seed(uint64_t s)
+  {
+    eng.seed(static_cast<std::mt19937::result_type>(s));
+    ahead.clear();
+  }
+  uint32_t next()
+  {
+    if (!ahead.empty())
+    {
+      const uint32_t x = ahead.front();
+      ahead.pop_front();
+      return x;
+    }
+    return eng();
+  }
+  static double to_uniform(uint32_t x)
+  {
+    return static_cast<double>(x - std::mt19937::min()) /
+        (static_cast<double>(std::mt19937::max() - std::mt19937::min()) + 1.0);
+  }
+  double uniform() { return to_uniform(next()); }
+  void peek_uniforms(double* out, size_t n)
+  {
+    while (ahead.size() < n)
+      ahead.push_back(eng());
+    for (size_t i = 0; i < n; i++)
+      out[i] = to_uniform(ahead[i]);
+  }
+  void consume(size_t n)
+  {
+    for (size_t i = 0; i < n; i++)
+      next();
+  }
+  void gauss(double* a, size_t n)
+  {
+    const double slightly_less_than_one = 1.0 - std::numeric_limits<double>::epsilon();
+    const long nm1 = static_cast<long>(n) - 1;
+    for (long i = 0; i < nm1; i += 2)
+    {
+      const double t1 = std::sqrt(-2.0 * std::log(1.0 - slightly_less_than_one * uniform()));
+      const double t2 = 2.0 * M_PI * uniform();
+      a[i]            = t1 * std::cos(t2);
+      a[i + 1]        = t1 * std::sin(t2);
+    }
+    if (n % 2 == 1)
+    {
+      const double t1 = std::sqrt(-2.0 * std::log(1.0 - slightly_less_than_one * uniform()));
+      const double t2 = 2.0 * M_PI * uniform();
+      a[nm1]          = t1 * std::cos(t2);
+    }
+  }
+};
+
+__global__ void bump_counter_kernel(unsigned long long* c) { c[0] += 1ull; }
+__global__ void reset_cursor_kernel(int* c) { c[0] = 0; c[1] = 0; }
+
+// ---------------------------------------------------------------------------
+// crowd
+// ---------------------------------------------------------------------------
+struct qmcg_crowd_s
+{
+  virtual ~qmcg_crowd_s() = default;
+  qmcg_system sys        = nullptr;
+  cudaStream_t stream    = nullptr;
+  int nw = 0, k = 1;
+  int dc[2]              = {0, 0};
+  int invrow_iat         = -1;
+  virtual int load(const double* R)                      = 0;
+  virtual int positions(double* R)                       = 0;
+  virtual int evaluate_log(double* lp, int* sg)          = 0;
+  virtual int eval_grad(int iat, double* g)              = 0;
+  virtual int make_move(int iat, const double* d)        = 0;
+  virtual int ratio_grad(int iat, double* r, double* g)  = 0;
+  virtual int accept_reject(int iat, const int* acc)     = 0;
+  virtual int complete()                                 = 0;
+  virtual int get_log(double* lp, int* sg, double* parts) = 0;
+  virtual int get_inverse(int spin, double* a)           = 0;
+  virtual int get_jastrow(double* j2, double* j1)        = 0;
+  virtual int get_phi(double* phi)                       = 0;
+  virtual int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) = 0;
+  virtual int sweeps_async(int n)                        = 0;
+  virtual int sync(qmcg_sweep_stats* st)                 = 0;
+};
+
+template<typename T>
+struct Crowd final : qmcg_crowd_s
+{
+  DevState<T> s{};
+  DeviceArena mem;
+  double* Mt = nullptr; // FP64 Slater matrices for the recompute, [2][nw][N][N]
+  T* W       = nullptr; // flush scratch, [nw][k][lda]
+  double* gauss_d = nullptr;
+  double* unif_d  = nullptr;
+  double* gauss_h = nullptr; // pinned
+  double* unif_h  = nullptr; // pinned
+  HostStream hs;
+  bool stream_seeded = false;
+  uint64_t hs_seed    = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_rng_mode = -1, graph_use_drift = -1;
+  double graph_tau = 0;
+  uint64_t graph_seed = 0;
+  int sweeps_since_recompute = 0;
+
+  ~Crowd() override
+  {
+    if (graph)
+      cudaGraphExecDestroy(graph);
+    if (gauss_h)
+      cudaFreeHost(gauss_h);
+    if (unif_h)
+      cudaFreeHost(unif_h);
+    if (stream)
+      cudaStreamDestroy(stream);
+  }
+
+  int init(qmcg_system sys_, int nw_, int k_)
+  {
+    sys = sys_;
+    nw  = nw_;
+    k   = k_;
+    CUDA_TRY(setup_move_kernels<T>());
+    CUDA_TRY(setup_recompute_kernels<T>());
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    DevState<T>& d = s;
+    d.nw        = nw;
+    d.ne        = sys->ne;
+    d.ne_pad    = ((sys->ne + 31) / 32) * 32;
+    d.nup       = sys->nup;
+    d.norb      = sys->norb;
+    d.lda       = sys->lda;
+    d.nions     = sys->nions;
+    d.nions_pad = sys->nions_pad;
+    d.k         = k;
+    d.coefs     = static_cast<const T*>(sys->coefs);
+    d.gx        = sys->grid[0];
+    d.gy        = sys->grid[1];
+    d.gz        = sys->grid[2];
+    d.zs        = sys->lda;
+    d.ys        = (long long)(sys->grid[2] + 3) * d.zs;
+    d.xs        = (long long)(sys->grid[1] + 3) * d.ys;
+    for (int q = 0; q < 3; q++)
+      d.L[q] = sys->L[q];
+    d.ions        = static_cast<const T*>(sys->ions);
+    d.ion_species = sys->ion_species;
+    d.j1c         = static_cast<const T*>(sys->j1c);
+    d.j1_ncoef    = sys->j1_ncoef;
+    d.j1_maxidx   = sys->j1_ncoef - 4;
+    d.j1_dri      = static_cast<T>(sys->j1_dri);
+    d.j1_rcut     = static_cast<T>(sys->j1_rcut);
+    d.j2c         = static_cast<const T*>(sys->j2c);
+    d.j2_ncoef    = sys->j2_ncoef;
+    d.j2_maxidx   = sys->j2_ncoef - 4;
+    d.j2_dri      = static_cast<T>(sys->j2_dri);
+    d.j2_rcut     = static_cast<T>(sys->j2_rcut);
+    d.has_j1      = sys->has_j1;
+    d.has_j2      = sys->has_j2;
+    const size_t N = sys->norb, lda = sys->lda, ne_pad = d.ne_pad;
+    CUDA_TRY(mem.alloc(&d.R, (size_t)nw * 3 * ne_pad));
+    CUDA_TRY(mem.alloc(&d.Rt, (size_t)nw * 3 * ne_pad));
+    CUDA_TRY(mem.alloc(&d.Ainv, 2 * (size_t)nw * N * lda));
+    CUDA_TRY(mem.alloc(&d.dgrad, 2 * (size_t)nw * N * 3 * lda));
+    CUDA_TRY(mem.alloc(&d.dlap, 2 * (size_t)nw * N * lda));
+    CUDA_TRY(mem.alloc(&d.U, 2 * (size_t)nw * k * lda));
+    CUDA_TRY(mem.alloc(&d.V, 2 * (size_t)nw * k * lda));
+    CUDA_TRY(mem.alloc(&d.Binv, 2 * (size_t)nw * k * k));
+    CUDA_TRY(mem.alloc(&d.delay_list, 2 * (size_t)nw * k));
+    CUDA_TRY(mem.alloc(&d.J2, (size_t)nw * 5 * ne_pad));
+    CUDA_TRY(mem.alloc(&d.J1, (size_t)nw * 5 * ne_pad));
+    CUDA_TRY(mem.alloc(&d.log_abs, 2 * (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.sign, 2 * (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.active_pos, (size_t)nw * 3));
+    CUDA_TRY(mem.alloc(&d.disp, (size_t)nw * 3));
+    CUDA_TRY(mem.alloc(&d.invRow, (size_t)nw * lda));
+    CUDA_TRY(mem.alloc(&d.rcopy, (size_t)nw * lda));
+    CUDA_TRY(mem.alloc(&d.phi, (size_t)nw * 5 * lda));
+    CUDA_TRY(mem.alloc(&d.cur_det, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.cur_j, (size_t)nw * 10));
+    CUDA_TRY(mem.alloc(&d.grads_now, (size_t)nw * 3));
+    CUDA_TRY(mem.alloc(&d.grads_new, (size_t)nw * 3));
+    CUDA_TRY(mem.alloc(&d.ratios, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.log_gf, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.prob, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.flag, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.accepted, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.status, (size_t)nw));
+    CUDA_TRY(mem.alloc(&d.counters, 2));
+    CUDA_TRY(mem.alloc(&d.ucursor, 2));
+    CUDA_TRY(mem.alloc(&d.sweep_counter, 1));
+    CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
+    CUDA_TRY(mem.alloc(&W, (size_t)nw * k * lda));
+    const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
+    CUDA_TRY(mem.alloc(&gauss_d, ng));
+    CUDA_TRY(mem.alloc(&unif_d, nu));
+    CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
+    CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
+    d.gauss     = gauss_d;
+    d.uniform   = unif_d;
+    d.rng_mode  = 1;
+    d.tau       = 0.3;
+    d.use_drift = 1;
+    CUDA_TRY(cudaDeviceSynchronize());
+    return QMCG_OK;
+  }
+
+  int check_iat(int iat) const { return (iat >= 0 && iat < sys->ne) ? QMCG_OK : fail(QMCG_ERR_ARG, "iat out of range"); }
+  int spin_of(int iat) const { return iat >= sys->nup ? 1 : 0; }
+
+  int load(const double* R) override
+  {
+    if (!R)
+      return fail(QMCG_ERR_ARG, "null positions");
+    const int ne = sys->ne, ne_pad = s.ne_pad;
+    std::vector<double> h((size_t)nw * 3 * ne_pad, 0.0);
+    std::vector<T> ht((size_t)nw * 3 * ne_pad, T(0));
+    for (int iw = 0; iw < nw; iw++)
+      for (int e = 0; e < ne; e++)
+        for (int q = 0; q < 3; q++)
+        {
+          const double x                                  = R[((size_t)iw * ne + e) * 3 + q];
+          h[((size_t)iw * 3 + q) * ne_pad + e]            = x;
+          ht[((size_t)iw * 3 + q) * ne_pad + e]           = static_cast<T>(x);
+        }
+    CUDA_TRY(cudaMemcpyAsync(s.R, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(s.Rt, ht.data(), ht.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  int positions(double* R) override
+  {
+    const int ne = sys->ne, ne_pad = s.ne_pad;
+    std::vector<double> h((size_t)nw * 3 * ne_pad);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), s.R, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int iw = 0; iw < nw; iw++)
+      for (int e = 0; e < ne; e++)
+        for (int q = 0; q < 3; q++)
+          R[((size_t)iw * ne + e) * 3 + q] = h[((size_t)iw * 3 + q) * ne_pad + e];
+    return QMCG_OK;
+  }
+
+  int status_check()
+  {
+    std::vector<int> st(nw);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    int any = 0;
+    for (int v : st)
+      any |= v;
+    if (any)
+    {
+      CUDA_TRY(cudaMemsetAsync(s.status, 0, nw * sizeof(int), stream));
+      if (any & ST_SINGULAR)
+        return fail(QMCG_ERR_SINGULAR, "singular Slater matrix");
+      if (any & ST_NONFINITE)
+        return fail(QMCG_ERR_NONFINITE, "non-finite ratio or gradient");
+      if (any & ST_ZERO_RATIO)
+        return fail(QMCG_ERR_ZERO_RATIO, "accepted move with zero determinant ratio");
+    }
+    return QMCG_OK;
+  }
+
+  int recompute_device()
+  {
+    CUDA_TRY(launch_recompute<T>(s, Mt, stream));
+    dc[0] = dc[1] = 0;
+    invrow_iat    = -1;
+    return QMCG_OK;
+  }
+
+  int evaluate_log(double* lp, int* sg) override
+  {
+    int rc = recompute_device();
+    if (rc != QMCG_OK)
+      return rc;
+    rc = status_check();
+    if (rc != QMCG_OK)
+      return rc;
+    return get_log(lp, sg, nullptr);
+  }
+
+  int eval_grad(int iat, double* g) override
+  {
+    int rc = check_iat(iat);
+    if (rc)
+      return rc;
+    CUDA_TRY(launch_propose<T>(s, iat, dc[spin_of(iat)], 0, stream));
+    invrow_iat = iat;
+    if (g)
+      CUDA_TRY(cudaMemcpyAsync(g, s.grads_now, nw * 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  int make_move(int iat, const double* d) override
+  {
+    int rc = check_iat(iat);
+    if (rc)
+      return rc;
+    if (!d)
+      return fail(QMCG_ERR_ARG, "null displacement");
+    CUDA_TRY(cudaMemcpyAsync(s.disp, d, nw * 3 * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(launch_make_move<T>(s, iat, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  int ratio_grad(int iat, double* r, double* g) override
+  {
+    int rc = check_iat(iat);
+    if (rc)
+      return rc;
+    if (invrow_iat != iat)
+    {
+      // the up-to-date inverse row of iat is prepared on demand (DelayedUpdateBatched::mw_getInvRow)
+      CUDA_TRY(launch_propose<T>(s, iat, dc[spin_of(iat)], 0, stream));
+      invrow_iat = iat;
+    }
+    CUDA_TRY(launch_ratio<T>(s, iat, 0, stream));
+    if (r)
+      CUDA_TRY(cudaMemcpyAsync(r, s.ratios, nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (g)
+      CUDA_TRY(cudaMemcpyAsync(g, s.grads_new, nw * 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return status_check();
+  }
+
+  int flush_spin(int sp)
+  {
+    if (k > 1 && dc[sp] > 0)
+    {
+      CUDA_TRY(launch_flush_simt<T>(s, sp, dc[sp], W, stream));
+      dc[sp] = 0;
+    }
+    return QMCG_OK;
+  }
+
+  int accept_reject(int iat, const int* acc) override
+  {
+    int rc = check_iat(iat);
+    if (rc)
+      return rc;
+    if (!acc)
+      return fail(QMCG_ERR_ARG, "null accept list");
+    if (invrow_iat != iat)
+      return fail(QMCG_ERR_STATE, "accept_reject without ratio_grad for this electron");
+    std::vector<int> a(nw);
+    for (int i = 0; i < nw; i++)
+      a[i] = acc[i] ? 1 : 0;
+    CUDA_TRY(cudaMemcpyAsync(s.accepted, a.data(), nw * sizeof(int), cudaMemcpyHostToDevice, stream));
+    const int sp = spin_of(iat);
+    CUDA_TRY(launch_accept<T>(s, iat, dc[sp], 0, stream));
+    invrow_iat = -1;
+    if (k > 1)
+    {
+      dc[sp]++;
+      if (dc[sp] == k)
+      {
+        rc = flush_spin(sp);
+        if (rc)
+          return rc;
+      }
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return status_check();
+  }
+
+  int complete() override
+  {
+    int rc = flush_spin(0);
+    if (rc)
+      return rc;
+    rc = flush_spin(1);
+    if (rc)
+      return rc;
+    invrow_iat = -1;
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  template<typename X>
+  int d2h(std::vector<X>& h, const X* d, size_t n)
+  {
+    h.resize(n);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), d, n * sizeof(X), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  int get_log(double* lp, int* sg, double* parts) override
+  {
+    std::vector<double> la;
+    std::vector<int> sgn;
+    std::vector<T> j1, j2;
+    int rc = d2h(la, s.log_abs, 2 * (size_t)nw);
+    if (!rc)
+      rc = d2h(sgn, s.sign, 2 * (size_t)nw);
+    if (!rc)
+      rc = d2h(j2, s.J2, (size_t)nw * 5 * s.ne_pad);
+    if (!rc)
+      rc = d2h(j1, s.J1, (size_t)nw * 5 * s.ne_pad);
+    if (rc)
+      return rc;
+    for (int iw = 0; iw < nw; iw++)
+    {
+      double u2 = 0, u1 = 0;
+      for (int e = 0; e < sys->ne; e++)
+      {
+        u2 += static_cast<double>(j2[(size_t)iw * 5 * s.ne_pad + e]);
+        u1 += static_cast<double>(j1[(size_t)iw * 5 * s.ne_pad + e]);
+      }
+      const double lj2 = s.has_j2 ? -0.5 * u2 : 0.0, lj1 = s.has_j1 ? -u1 : 0.0;
+      if (lp)
+        lp[iw] = la[iw] + la[nw + iw] + lj1 + lj2;
+      if (sg)
+        sg[iw] = sgn[iw] * sgn[nw + iw];
+      if (parts)
+      {
+        parts[iw * 4 + 0] = la[iw];
+        parts[iw * 4 + 1] = la[nw + iw];
+        parts[iw * 4 + 2] = lj1;
+        parts[iw * 4 + 3] = lj2;
+      }
+    }
+    return QMCG_OK;
+  }
+
+  int get_inverse(int spin, double* a) override
+  {
+    if (spin < 0 || spin > 1 || !a)
+      return fail(QMCG_ERR_ARG, "bad spin or null output");
+    const size_t N = sys->norb, lda = sys->lda;
+    std::vector<T> h;
+    int rc = d2h(h, s.Ainv + (size_t)spin * nw * N * lda, (size_t)nw * N * lda);
+    if (rc)
+      return rc;
+    for (int iw = 0; iw < nw; iw++)
+      for (size_t i = 0; i < N; i++)
+        for (size_t j = 0; j < N; j++)
+          a[((size_t)iw * N + i) * N + j] = static_cast<double>(h[((size_t)iw * N + i) * lda + j]);
+    return QMCG_OK;
+  }
+
+  int get_jastrow(double* j2o, double* j1o) override
+  {
+    std::vector<T> j1, j2;
+    int rc = d2h(j2, s.J2, (size_t)nw * 5 * s.ne_pad);
+    if (!rc)
+      rc = d2h(j1, s.J1, (size_t)nw * 5 * s.ne_pad);
+    if (rc)
+      return rc;
+    const int ne = sys->ne;
+    for (int iw = 0; iw < nw; iw++)
+      for (int q = 0; q < 5; q++)
+        for (int e = 0; e < ne; e++)
+        {
+          if (j2o)
+            j2o[((size_t)iw * 5 + q) * ne + e] = static_cast<double>(j2[((size_t)iw * 5 + q) * s.ne_pad + e]);
+          if (j1o)
+            j1o[((size_t)iw * 5 + q) * ne + e] = static_cast<double>(j1[((size_t)iw * 5 + q) * s.ne_pad + e]);
+        }
+    return QMCG_OK;
+  }
+
+  int get_phi(double* phi) override
+  {
+    std::vector<T> h;
+    int rc = d2h(h, s.phi, (size_t)nw * 5 * s.lda);
+    if (rc)
+      return rc;
+    const int N = sys->norb;
+    for (int iw = 0; iw < nw; iw++)
+      for (int q = 0; q < 5; q++)
+        for (int o = 0; o < N; o++)
+          phi[((size_t)iw * 5 + q) * N + o] = static_cast<double>(h[((size_t)iw * 5 + q) * s.lda + o]);
+    return QMCG_OK;
+  }
+
+  // ---- the sweep as one graph: per electron propose -> ratio -> accept, flush every k
+  int enqueue_sweep()
+  {
+    int d[2] = {0, 0};
+    if (s.rng_mode == 0)
+      reset_cursor_kernel<<<1, 1, 0, stream>>>(s.ucursor);
+    for (int iat = 0; iat < sys->ne; iat++)
+    {
+      const int sp = spin_of(iat);
+      CUDA_TRY(launch_propose<T>(s, iat, d[sp], 1, stream));
+      CUDA_TRY(launch_ratio<T>(s, iat, 1, stream));
+      CUDA_TRY(launch_accept<T>(s, iat, d[sp], 1, stream));
+      if (k > 1)
+      {
+        d[sp]++;
+        if (d[sp] == k)
+        {
+          CUDA_TRY(launch_flush_simt<T>(s, sp, k, W, stream));
+          d[sp] = 0;
+        }
+      }
+    }
+    for (int sp = 0; sp < 2; sp++)
+      if (k > 1 && d[sp] > 0)
+        CUDA_TRY(launch_flush_simt<T>(s, sp, d[sp], W, stream));
+    bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
+    CUDA_TRY(cudaGetLastError());
+    return QMCG_OK;
+  }
+
+  int build_graph(const qmcg_sweep_params* p)
+  {
+    if (graph && graph_rng_mode == p->rng_mode && graph_use_drift == p->use_drift && graph_tau == p->tau &&
+        graph_seed == p->seed)
+      return QMCG_OK;
+    if (graph)
+    {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    s.rng_mode  = p->rng_mode;
+    s.use_drift = p->use_drift;
+    s.tau       = p->tau;
+    s.seed      = p->seed;
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_sweep();
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (rc)
+      return rc;
+    if (e != cudaSuccess)
+      return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    graph_rng_mode  = p->rng_mode;
+    graph_use_drift = p->use_drift;
+    graph_tau       = p->tau;
+    graph_seed      = p->seed;
+    return QMCG_OK;
+  }
+
+  int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) override
+  {
+    if (!p || n < 0 || !(p->tau > 0) || (p->rng_mode != 0 && p->rng_mode != 1))
+      return fail(QMCG_ERR_ARG, "bad sweep parameters");
+    if (dc[0] || dc[1])
+    {
+      int rc = complete();
+      if (rc)
+        return rc;
+    }
+    if (p->rng_mode == 0 && (!stream_seeded || hs_seed != p->seed))
+    {
+      hs.seed(p->seed);
+      hs_seed       = p->seed;
+      stream_seeded = true;
+    }
+    int rc = build_graph(p);
+    if (rc)
+      return rc;
+    CUDA_TRY(cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned long long), stream));
+    const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
+    std::vector<int> accbuf;
+    for (int it = 0; it < n; it++)
+    {
+      if (p->rng_mode == 0)
+      {
+        hs.gauss(gauss_h, ng);
+        hs.peek_uniforms(unif_h, nu);
+        CUDA_TRY(cudaMemcpyAsync(gauss_d, gauss_h, ng * sizeof(double), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(unif_d, unif_h, nu * sizeof(double), cudaMemcpyHostToDevice, stream));
+      }
+      if (acc_log)
+      {
+        // electron-by-electron launches so the decisions can be logged
+        rc = sweep_logged(acc_log + (size_t)it * sys->ne * nw);
+        if (rc)
+          return rc;
+      }
+      else
+        CUDA_TRY(cudaGraphLaunch(graph, stream));
+      if (p->rng_mode == 0)
+      {
+        int used[2];
+        CUDA_TRY(cudaMemcpyAsync(used, s.ucursor, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        hs.consume(static_cast<size_t>(used[sys->ne & 1]));
+      }
+      sweeps_since_recompute++;
+      if (p->recompute_every > 0 && sweeps_since_recompute >= p->recompute_every)
+      {
+        rc = recompute_device();
+        if (rc)
+          return rc;
+        sweeps_since_recompute = 0;
+      }
+    }
+    return sync(st);
+  }
+
+  int sweep_logged(int* acc_log)
+  {
+    int d[2] = {0, 0};
+    if (s.rng_mode == 0)
+      reset_cursor_kernel<<<1, 1, 0, stream>>>(s.ucursor);
+    for (int iat = 0; iat < sys->ne; iat++)
+    {
+      const int sp = spin_of(iat);
+      CUDA_TRY(launch_propose<T>(s, iat, d[sp], 1, stream));
+      CUDA_TRY(launch_ratio<T>(s, iat, 1, stream));
+      CUDA_TRY(launch_accept<T>(s, iat, d[sp], 1, stream));
+      CUDA_TRY(cudaMemcpyAsync(acc_log + (size_t)iat * nw, s.accepted, nw * sizeof(int), cudaMemcpyDeviceToHost,
+                               stream));
+      if (k > 1)
+      {
+        d[sp]++;
+        if (d[sp] == k)
+        {
+          CUDA_TRY(launch_flush_simt<T>(s, sp, k, W, stream));
+          d[sp] = 0;
+        }
+      }
+    }
+    for (int sp = 0; sp < 2; sp++)
+      if (k > 1 && d[sp] > 0)
+        CUDA_TRY(launch_flush_simt<T>(s, sp, d[sp], W, stream));
+    bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  int sweeps_async(int n) override
+  {
+    if (!graph || graph_rng_mode != 1)
+      return fail(QMCG_ERR_STATE, "no device-RNG sweep graph built yet");
+    for (int it = 0; it < n; it++)
+      CUDA_TRY(cudaGraphLaunch(graph, stream));
+    return QMCG_OK;
+  }
+
+  int sync(qmcg_sweep_stats* st) override
+  {
+    unsigned long long c[2];
+    std::vector<int> stv(nw);
+    CUDA_TRY(cudaMemcpyAsync(c, s.counters, sizeof(c), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(stv.data(), s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    int any = 0;
+    for (int v : stv)
+      any |= v;
+    CUDA_TRY(cudaMemsetAsync(s.status, 0, nw * sizeof(int), stream));
+    if (st)
+    {
+      st->accepted = c[0];
+      st->rejected = c[1];
+      st->status   = any;
+    }
+    if (any & ST_SINGULAR)
+      return fail(QMCG_ERR_SINGULAR, "singular Slater matrix");
+    if (any & ST_NONFINITE)
+      return fail(QMCG_ERR_NONFINITE, "non-finite ratio or gradient");
+    if (any & ST_ZERO_RATIO)
+      return fail(QMCG_ERR_ZERO_RATIO, "accepted move with zero determinant ratio");
+    return QMCG_OK;
+  }
+};
+
+extern "C" int qmcg_crowd_create(qmcg_system sys, int nw, int k, qmcg_crowd* out)
+{
+  if (!sys || !out || nw <= 0 || k <= 0 || k > sys->norb)
+    return fail(QMCG_ERR_ARG, "bad crowd arguments (need 1 <= delay_rank <= num_orbitals)");
+  *out = nullptr;
+  std::unique_ptr<qmcg_crowd_s> c;
+  int rc;
+  if (sys->prec == 8)
+  {
+    auto* p = new Crowd<double>();
+    c.reset(p);
+    rc = p->init(sys, nw, k);
+  }
+  else
+  {
+    auto* p = new Crowd<float>();
+    c.reset(p);
+    rc = p->init(sys, nw, k);
+  }
+  if (rc != QMCG_OK)
+    return rc;
+  *out = c.release();
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_crowd_destroy(qmcg_crowd c)
+{
+  delete c;
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_crowd_stream(qmcg_crowd c, void** stream)
+{
+  if (!c || !stream)
+    return fail(QMCG_ERR_ARG, "null argument");
+  *stream = c->stream;
+  return QMCG_OK;
+}
+
+#define CROWD_CALL(c, call)                                                                                            \
+  do                                                                                                                   \
+  {                                                                                                                    \
+    if (!(c))                                                                                                          \
+      return fail(QMCG_ERR_ARG, "null crowd");                                                                         \
+    return (c)->call;                                                                                                  \
+  } while (0)
+
+extern "C" int qmcg_load_walkers(qmcg_crowd c, const double* R) { CROWD_CALL(c, load(R)); }
+extern "C" int qmcg_get_positions(qmcg_crowd c, double* R) { CROWD_CALL(c, positions(R)); }
+extern "C" int qmcg_mw_evaluate_log(qmcg_crowd c, double* lp, int* sg) { CROWD_CALL(c, evaluate_log(lp, sg)); }
+extern "C" int qmcg_mw_prepare_group(qmcg_crowd c, int group)
+{
+  if (!c || group < 0 || group > 1)
+    return fail(QMCG_ERR_ARG, "bad group");
+  return QMCG_OK;
+}
+extern "C" int qmcg_mw_eval_grad(qmcg_crowd c, int iat, double* g) { CROWD_CALL(c, eval_grad(iat, g)); }
+extern "C" int qmcg_mw_make_move(qmcg_crowd c, int iat, const double* d, int* valid)
+{
+  if (!c)
+    return fail(QMCG_ERR_ARG, "null crowd");
+  if (valid)
+    for (int i = 0; i < c->nw; i++)
+      valid[i] = 1;
+  return c->make_move(iat, d);
+}
+extern "C" int qmcg_mw_calc_ratio_grad(qmcg_crowd c, int iat, double* r, double* g)
+{
+  CROWD_CALL(c, ratio_grad(iat, r, g));
+}
+extern "C" int qmcg_mw_accept_reject_move(qmcg_crowd c, int iat, const int* acc)
+{
+  CROWD_CALL(c, accept_reject(iat, acc));
+}
+extern "C" int qmcg_mw_complete_updates(qmcg_crowd c) { CROWD_CALL(c, complete()); }
+extern "C" int qmcg_get_log(qmcg_crowd c, double* lp, int* sg, double* parts) { CROWD_CALL(c, get_log(lp, sg, parts)); }
+extern "C" int qmcg_get_inverse(qmcg_crowd c, int spin, double* a) { CROWD_CALL(c, get_inverse(spin, a)); }
+extern "C" int qmcg_get_jastrow_state(qmcg_crowd c, double* j2, double* j1) { CROWD_CALL(c, get_jastrow(j2, j1)); }
+extern "C" int qmcg_get_phi_vgl(qmcg_crowd c, double* phi)
+{
+  if (!phi)
+    return fail(QMCG_ERR_ARG, "null output");
+  CROWD_CALL(c, get_phi(phi));
+}
+extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc)
+{
+  CROWD_CALL(c, sweeps(p, n, st, acc));
+}
+extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
+extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }

@@ -1,0 +1,248 @@
+// Device-side state and helpers shared by the move-loop kernels.
+//
+// One crowd = nw walkers of one system, resident in HBM for a whole run:
+//   positions      R    double [nw][3][ne_pad]   (SoA, FP64 always)
+//                  Rt   T      [nw][3][ne_pad]   (copy in the move-loop precision)
+//   determinants   Ainv T      [2][nw][N][lda]   (Ainv = (M^-1)^T, row e = electron)
+//                  dgrad T     [2][nw][N][3][lda], dlap T [2][nw][N][lda]
+//   delayed update U, V T [2][nw][k][lda], Binv T [2][nw][k][k], delay_list int [2][nw][k]
+//   Jastrow state  J2 T [nw][5][ne_pad] (Uat, dUat xyz, d2Uat), J1 likewise (Vat, Grad xyz, Lap)
+// lda = orbitals padded to 16 elements, so every row starts on a 64-byte boundary.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qmcg
+{
+
+enum : int
+{
+  ST_OK          = 0,
+  ST_ZERO_RATIO  = 1,  // accepted move with a zero determinant ratio
+  ST_NONFINITE   = 2,  // NaN/Inf ratio or gradient
+  ST_SINGULAR    = 4,  // exact zero pivot in the FP64 inverse
+};
+
+template<typename T>
+struct DevState
+{
+  // ---------------- sizes
+  int nw, ne, ne_pad, nup, norb, lda, nions, nions_pad, k;
+  // ---------------- system (read-only)
+  const T* coefs;
+  int gx, gy, gz;
+  long long xs, ys, zs; // element strides of the coefficient table
+  double L[3];          // orthorhombic cell lengths
+  const T* ions;        // [3][nions_pad]
+  const int* ion_species;
+  const T* j1c;         // [n_ion_species][j1_ncoef]
+  int j1_ncoef, j1_maxidx;
+  T j1_dri, j1_rcut;
+  const T* j2c;         // [2][j2_ncoef]: same spin, opposite spin
+  int j2_ncoef, j2_maxidx;
+  T j2_dri, j2_rcut;
+  int has_j1, has_j2;
+  // ---------------- walker state
+  double* R;
+  T* Rt;
+  T* Ainv;
+  T* dgrad;
+  T* dlap;
+  T* U;
+  T* V;
+  T* Binv;
+  int* delay_list;
+  T* J2;
+  T* J1;
+  double* log_abs; // [2][nw]
+  int* sign;       // [2][nw]
+  // ---------------- move scratch
+  double* active_pos; // [nw][3]
+  double* disp;       // [nw][3]  proposed displacement (drift + diffusion)
+  T* invRow;          // [nw][lda]
+  T* rcopy;           // [nw][lda]   (SM-1 row copy)
+  T* phi;             // [nw][5][lda]  proposed orbital VGL (v, gx, gy, gz, lap)
+  T* cur_det;         // [nw]          determinant ratio of the proposed move
+  T* cur_j;           // [nw][10]      J1 (U,gx,gy,gz,lap), J2 (U,gx,gy,gz,lap) at the proposed position
+  double* grads_now;  // [nw][3]
+  double* grads_new;  // [nw][3]
+  double* ratios;     // [nw]
+  double* log_gf;     // [nw]
+  double* prob;       // [nw]  acceptance probability argument p*exp(log_gb-log_gf)
+  int* flag;          // [nw]  valid && p >= eps (a uniform is consumed)
+  int* accepted;      // [nw]
+  int* status;        // [nw]
+  unsigned long long* counters; // [0] accepted, [1] rejected
+  // ---------------- random numbers
+  const double* gauss;   // stream mode: [ne][nw][3] unit Gaussians of the current sweep
+  const double* uniform; // stream mode: uniforms, consumed in walker order
+  int* ucursor;          // [2] ping-pong consumption cursor
+  unsigned long long seed;
+  unsigned long long* sweep_counter; // device RNG: sweeps done
+  int rng_mode;          // 0: stream from the host, 1: counter-based on the device
+  double tau;
+  int use_drift;
+};
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
+// ---------------------------------------------------------------------------
+struct u4
+{
+  uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ u4 philox4x32_10(u4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+  for (int r = 0; r < 10; r++)
+  {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c  = u4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// 53-bit uniform in [0,1) from two 32-bit words
+__device__ __forceinline__ double u01(uint32_t a, uint32_t b)
+{
+  const uint64_t v = (static_cast<uint64_t>(a) << 21) ^ static_cast<uint64_t>(b >> 11);
+  return static_cast<double>(v & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------
+// cubic B-spline weights of one axis: value, first and second derivative
+// (MultiBsplineData::compute_prefactors).
+// ---------------------------------------------------------------------------
+template<typename T>
+__device__ __forceinline__ void bspline_weights(T t, T a[4], T da[4], T d2a[4])
+{
+  a[0]   = ((T(-1.0 / 6.0) * t + T(3.0 / 6.0)) * t + T(-3.0 / 6.0)) * t + T(1.0 / 6.0);
+  a[1]   = ((T(3.0 / 6.0) * t + T(-1.0)) * t + T(0.0)) * t + T(4.0 / 6.0);
+  a[2]   = ((T(-3.0 / 6.0) * t + T(3.0 / 6.0)) * t + T(3.0 / 6.0)) * t + T(1.0 / 6.0);
+  a[3]   = ((T(1.0 / 6.0) * t + T(0.0)) * t + T(0.0)) * t + T(0.0);
+  da[0]  = (T(-0.5) * t + T(1.0)) * t + T(-0.5);
+  da[1]  = (T(1.5) * t + T(-2.0)) * t + T(0.0);
+  da[2]  = (T(-1.5) * t + T(1.0)) * t + T(0.5);
+  da[3]  = (T(0.5) * t + T(0.0)) * t + T(0.0);
+  d2a[0] = T(-1.0) * t + T(1.0);
+  d2a[1] = T(3.0) * t + T(-2.0);
+  d2a[2] = T(-3.0) * t + T(1.0);
+  d2a[3] = T(1.0) * t + T(0.0);
+}
+
+template<typename T>
+struct Eps;
+template<>
+struct Eps<float>
+{
+  static constexpr float v = 1.19209290e-07f;
+};
+template<>
+struct Eps<double>
+{
+  static constexpr double v = 2.2204460492503131e-16;
+};
+
+// getSplineBound: integer cell and fraction, clamped to [0, nmax] (SplineBound.hpp:36-61);
+// a NaN argument takes the x < 0 branch so no index can leave the table
+template<typename T>
+__device__ __forceinline__ void spline_bound(T x, int nmax, int& ind, T& dx)
+{
+  if (!(x >= T(0)))
+  {
+    ind = 0;
+    dx  = T(0);
+  }
+  else
+  {
+    const T ip = floor(x);
+    dx         = x - ip;
+    ind        = static_cast<int>(ip);
+    if (ind > nmax)
+    {
+      ind = nmax;
+      dx  = T(1) - Eps<T>::v;
+    }
+  }
+}
+
+// radial B-spline functor: u, du/dr, d2u/dr2 (BsplineFunctor::evaluate_impl)
+template<typename T>
+__device__ __forceinline__ T functor_eval(const T* __restrict__ c, T dri, int maxidx, T r, T& du, T& d2u)
+{
+  r *= dri;
+  int i;
+  T t;
+  spline_bound(r, maxidx, i, t);
+  const T c0 = c[i], c1 = c[i + 1], c2 = c[i + 2], c3 = c[i + 3];
+  d2u = dri * dri *
+      (c0 * (T(-1.0) * t + T(1.0)) + c1 * (T(3.0) * t + T(-2.0)) + c2 * (T(-3.0) * t + T(1.0)) +
+       c3 * (T(1.0) * t + T(0.0)));
+  du = dri *
+      (c0 * ((T(-0.5) * t + T(1.0)) * t + T(-0.5)) + c1 * ((T(1.5) * t + T(-2.0)) * t + T(0.0)) +
+       c2 * ((T(-1.5) * t + T(1.0)) * t + T(0.5)) + c3 * ((T(0.5) * t + T(0.0)) * t + T(0.0)));
+  return c0 * (((T(-1.0 / 6.0) * t + T(3.0 / 6.0)) * t + T(-3.0 / 6.0)) * t + T(1.0 / 6.0)) +
+      c1 * (((T(3.0 / 6.0) * t + T(-1.0)) * t + T(0.0)) * t + T(4.0 / 6.0)) +
+      c2 * (((T(-3.0 / 6.0) * t + T(3.0 / 6.0)) * t + T(3.0 / 6.0)) * t + T(1.0 / 6.0)) +
+      c3 * (((T(1.0 / 6.0) * t + T(0.0)) * t + T(0.0)) * t + T(0.0));
+}
+
+// orthorhombic minimum image of d = R_j - r (DTD_BConds<T,3,PPPO>)
+template<typename T>
+__device__ __forceinline__ T min_image(T d, T L, T Linv)
+{
+  const T s = d * Linv;
+  return L * (s - round(s));
+}
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+template<typename T>
+__device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sum NV values over the block; result valid in every thread. scratch: NV * 32 elements
+template<typename T, int NV>
+__device__ __forceinline__ void block_sum(T (&v)[NV], T* scratch)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++)
+    v[q] = warp_sum(v[q]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++)
+      scratch[q * 32 + wid] = v[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; q++)
+  {
+    T x = lane < nwarp ? scratch[q * 32 + lane] : T(0);
+    v[q] = warp_sum(x);
+  }
+  __syncthreads();
+}
+
+// Umrigar drift scaling (DriftModifierUNR::getDrift, a = 1)
+__device__ __forceinline__ void unr_drift(double tau, const double g[3], double d[3])
+{
+  const double vsq = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  const double sc  = vsq < 2.2204460492503131e-16 ? tau : ((-1.0 + sqrt(1.0 + 2.0 * tau * vsq)) / vsq);
+  d[0]             = g[0] * sc;
+  d[1]             = g[1] * sc;
+  d[2]             = g[2] * sc;
+}
+
+} // namespace qmcg

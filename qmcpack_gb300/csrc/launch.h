@@ -1,0 +1,27 @@
+// Host-side launch interface between the translation units of the library.
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace qmcg
+{
+template<typename T>
+cudaError_t launch_propose(const DevState<T>& s, int iat, int dc, int driver, cudaStream_t st);
+template<typename T>
+cudaError_t launch_make_move(const DevState<T>& s, int iat, cudaStream_t st);
+template<typename T>
+cudaError_t launch_ratio(const DevState<T>& s, int iat, int driver, cudaStream_t st);
+template<typename T>
+cudaError_t launch_accept(const DevState<T>& s, int iat, int dc, int driver, cudaStream_t st);
+template<typename T>
+cudaError_t launch_flush_simt(const DevState<T>& s, int spin, int dc, T* W, cudaStream_t st);
+
+template<typename T>
+cudaError_t setup_move_kernels();
+template<typename T>
+cudaError_t setup_recompute_kernels();
+
+// recompute path (recompute_kernels.cu)
+template<typename T>
+cudaError_t launch_recompute(const DevState<T>& s, double* mscratch, cudaStream_t st);
+} // namespace qmcg

@@ -1,0 +1,302 @@
+// From-scratch evaluation of the wave-function state of every walker:
+//   * all-electron orbital VGL    <- SPOSet::mw_evaluate_notranspose (SPOSet.h:453-459)
+//   * FP64 inverse and log|det|   <- DiracMatrixInverterCUDA::mw_computeInvertAndLog
+//                                    (DiracMatrixInverterCUDA.hpp:112-180), DiracMatrix::invert_transpose
+//                                    (DiracMatrix.h:189-230), computeLogDet (DiracMatrix.h:100-110)
+//   * two-body Jastrow state      <- TwoBodyJastrow::recompute (TwoBodyJastrow.cpp:662-714)
+//   * one-body Jastrow state      <- J1OrbitalSoA::recompute (J1OrbitalSoA.h:240-250)
+// This is the initial mw_evaluateLog and the periodic FP64 recompute of the
+// mixed-precision move loop.  The inverse is a Gauss-Jordan elimination with
+// partial pivoting (same pivots as LU with partial pivoting), one CTA per matrix,
+// in FP64 whatever the move-loop precision.
+#include "common.cuh"
+#include "launch.h"
+#include "spline.cuh"
+
+namespace qmcg
+{
+
+// grid (nw * ne): orbital VGL of electron e of walker iw into the FP64 Slater
+// matrix (stored transposed: Mt[slot][o][row]) and the dgrad / dlap rows.
+template<typename T, int NT>
+__global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* part      = reinterpret_cast<T*>(smem_raw);
+  const int iw = blockIdx.x / s.ne;
+  const int e  = blockIdx.x % s.ne;
+  const int spin = e >= s.nup ? 1 : 0;
+  const int row  = e - (spin ? s.nup : 0);
+  const int n    = s.norb;
+  const size_t slot = (size_t)spin * s.nw + iw;
+  double pos[3];
+  for (int d = 0; d < 3; d++)
+    pos[d] = s.R[((size_t)iw * 3 + d) * s.ne_pad + e];
+  spline_partials(s, pos, part);
+  __syncthreads();
+  double* M = Mt + slot * (size_t)n * n;
+  T* dg     = s.dgrad + ((slot * n + row) * 3) * s.lda;
+  T* dl     = s.dlap + (slot * n + row) * s.lda;
+  for (int o = threadIdx.x; o < n; o += blockDim.x)
+  {
+    T vgl[5];
+    spline_combine(s, part, o, vgl);
+    M[(size_t)o * n + row] = static_cast<double>(vgl[0]);
+    dg[o]                  = vgl[1];
+    dg[s.lda + o]          = vgl[2];
+    dg[2 * s.lda + o]      = vgl[3];
+    dl[o]                  = vgl[4];
+  }
+}
+
+// grid (2 * nw): in-place FP64 Gauss-Jordan inverse of Mt[slot] (n x n), log|det|
+// and sign; writes Ainv = Mt^-1 = (M^-1)^T in the move-loop precision.
+template<typename T, int NT>
+__global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* Mt)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = s.norb;
+  double* prow = reinterpret_cast<double*>(smem_raw); // n
+  double* pcol = prow + n;                           // n
+  int* perm    = reinterpret_cast<int*>(pcol + n);   // n
+  __shared__ double bval[32];
+  __shared__ int bidx[32];
+  __shared__ int s_piv;
+  __shared__ int s_bad;
+  const int slot = blockIdx.x;
+  double* a      = Mt + (size_t)slot * n * n;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double logabs = 0.0;
+  int sgn       = 1;
+  if (threadIdx.x == 0)
+    s_bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; k++)
+  {
+    // pivot: first row of maximal |a[i][k]|, i >= k
+    double bv = -1.0;
+    int bi    = n;
+    for (int i = k + threadIdx.x; i < n; i += NT)
+    {
+      const double v = fabs(a[(size_t)i * n + k]);
+      if (v > bv || (v == bv && i < bi))
+      {
+        bv = v;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi    = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi))
+      {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0)
+    {
+      bval[wid] = bv;
+      bidx[wid] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      double b = bval[0];
+      int p    = bidx[0];
+      for (int w = 1; w < NT / 32; w++)
+        if (bval[w] > b || (bval[w] == b && bidx[w] < p))
+        {
+          b = bval[w];
+          p = bidx[w];
+        }
+      if (!(b > 0.0))
+      {
+        s_bad = 1;
+        p     = k;
+      }
+      s_piv   = p;
+      perm[k] = p;
+    }
+    __syncthreads();
+    if (s_bad)
+      break;
+    const int p = s_piv;
+    if (p != k)
+      for (int j = threadIdx.x; j < n; j += NT)
+      {
+        const double t          = a[(size_t)k * n + j];
+        a[(size_t)k * n + j]    = a[(size_t)p * n + j];
+        a[(size_t)p * n + j]    = t;
+      }
+    __syncthreads();
+    const double d = a[(size_t)k * n + k];
+    for (int j = threadIdx.x; j < n; j += NT)
+    {
+      const double v       = (j == k ? 1.0 : a[(size_t)k * n + j]) / d;
+      prow[j]              = v;
+      a[(size_t)k * n + j] = v;
+    }
+    for (int i = threadIdx.x; i < n; i += NT)
+      pcol[i] = (i == k) ? 0.0 : a[(size_t)i * n + k];
+    if (threadIdx.x == 0)
+    {
+      logabs += log(fabs(d));
+      if (d < 0.0)
+        sgn = -sgn;
+      if (p != k)
+        sgn = -sgn;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += NT)
+    {
+      const int i = e / n, j = e % n;
+      if (i == k)
+        continue;
+      const double base = (j == k) ? 0.0 : a[e];
+      a[e]              = base - pcol[i] * prow[j];
+    }
+    __syncthreads();
+  }
+  const size_t iw_spin = slot;
+  if (s_bad)
+  {
+    if (threadIdx.x == 0)
+    {
+      atomicOr(s.status + (slot % s.nw), ST_SINGULAR);
+      s.log_abs[iw_spin] = -INFINITY;
+      s.sign[iw_spin]    = 0;
+    }
+    return;
+  }
+  // undo the row interchanges as column interchanges, in reverse order
+  for (int k = n - 1; k >= 0; k--)
+  {
+    const int p = perm[k];
+    if (p != k)
+      for (int i = threadIdx.x; i < n; i += NT)
+      {
+        const double t       = a[(size_t)i * n + k];
+        a[(size_t)i * n + k] = a[(size_t)i * n + p];
+        a[(size_t)i * n + p] = t;
+      }
+    __syncthreads();
+  }
+  T* A = s.Ainv + (size_t)slot * n * s.lda;
+  for (int e = threadIdx.x; e < n * n; e += NT)
+  {
+    const int i = e / n, j = e % n;
+    A[(size_t)i * s.lda + j] = static_cast<T>(a[e]);
+  }
+  if (threadIdx.x == 0)
+  {
+    s.log_abs[iw_spin] = logabs;
+    s.sign[iw_spin]    = sgn;
+  }
+}
+
+// grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
+// Vat, Grad, Lap over the ions.
+template<typename T, int NT>
+__global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s)
+{
+  const int iw = blockIdx.x;
+  const int i  = blockIdx.y * NT + threadIdx.x;
+  if (i >= s.ne)
+    return;
+  const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
+  const T xi = Rx[i], yi = Rx[s.ne_pad + i], zi = Rx[2 * s.ne_pad + i];
+  const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
+  const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+  {
+    T u = 0, gx = 0, gy = 0, gz = 0, lap = 0;
+    if (s.has_j2)
+      for (int j = 0; j < s.ne; j++)
+      {
+        if (j == i)
+          continue;
+        const T dx = min_image(Rx[j] - xi, L0, Li0);
+        const T dy = min_image(Rx[s.ne_pad + j] - yi, L1, Li1);
+        const T dz = min_image(Rx[2 * s.ne_pad + j] - zi, L2, Li2);
+        const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+        if (r < s.j2_rcut)
+        {
+          const int same = (j < s.nup) == (i < s.nup);
+          T du, d2u;
+          u += functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
+          du *= T(1) / r;
+          gx += du * dx;
+          gy += du * dy;
+          gz += du * dz;
+          lap += d2u + T(2) * du;
+        }
+      }
+    T* J2 = s.J2 + (size_t)iw * 5 * s.ne_pad;
+    J2[i]                = u;
+    J2[s.ne_pad + i]     = gx;
+    J2[2 * s.ne_pad + i] = gy;
+    J2[3 * s.ne_pad + i] = gz;
+    J2[4 * s.ne_pad + i] = -lap;
+  }
+  {
+    T u = 0, gx = 0, gy = 0, gz = 0, lap = 0;
+    if (s.has_j1)
+      for (int j = 0; j < s.nions; j++)
+      {
+        const T dx = min_image(s.ions[j] - xi, L0, Li0);
+        const T dy = min_image(s.ions[s.nions_pad + j] - yi, L1, Li1);
+        const T dz = min_image(s.ions[2 * s.nions_pad + j] - zi, L2, Li2);
+        const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+        if (r < s.j1_rcut)
+        {
+          T du, d2u;
+          u += functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
+          du *= T(1) / r;
+          gx += du * dx;
+          gy += du * dy;
+          gz += du * dz;
+          lap += d2u + T(2) * du;
+        }
+      }
+    T* J1 = s.J1 + (size_t)iw * 5 * s.ne_pad;
+    J1[i]                = u;
+    J1[s.ne_pad + i]     = gx;
+    J1[2 * s.ne_pad + i] = gy;
+    J1[3 * s.ne_pad + i] = gz;
+    J1[4 * s.ne_pad + i] = lap;
+  }
+}
+
+template<typename T>
+cudaError_t launch_recompute(const DevState<T>& s, double* Mt, cudaStream_t st)
+{
+  constexpr int NT = 128;
+  const size_t sm  = sizeof(T) * 4 * 7 * (size_t)s.lda;
+  vgl_all_kernel<T, NT><<<s.nw * s.ne, NT, sm, st>>>(s, Mt);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  constexpr int NTG = 256;
+  const size_t smg  = (size_t)s.norb * (2 * sizeof(double) + sizeof(int));
+  gj_inverse_kernel<T, NTG><<<2 * s.nw, NTG, smg, st>>>(s, Mt);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  dim3 grid(s.nw, (s.ne + 127) / 128);
+  jastrow_full_kernel<T, 128><<<grid, 128, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t setup_recompute_kernels()
+{
+  return cudaFuncSetAttribute(vgl_all_kernel<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+template cudaError_t setup_recompute_kernels<float>();
+template cudaError_t setup_recompute_kernels<double>();
+template cudaError_t launch_recompute<float>(const DevState<float>&, double*, cudaStream_t);
+template cudaError_t launch_recompute<double>(const DevState<double>&, double*, cudaStream_t);
+
+} // namespace qmcg
