@@ -1,0 +1,319 @@
+"""Benchmark of the batched particle-by-particle Slater-Jastrow VMC move loop.
+
+One step = one VMC sweep: every electron of every walker is proposed once
+(drift-diffusion), tested and accepted or rejected, delayed updates are flushed,
+and the FP64 recompute runs on its schedule (every 100 sweeps), all through the
+captured CUDA graph of the library.  The workload is the production-shape system
+(384 electrons, 512 walkers, delay rank 32, FP32 move loop).  Inputs are seeded
+synthetic systems; the working set (~0.9 GB) is larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Multi-GPU runs are independent replicas (walkers are independent Markov chains):
+every rank runs its own crowd with its own seed; value = all ranks' walker-moves
+divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from qmcpack_gb300.system import SPECS, make_system, make_walkers  # noqa: E402
+
+DESCRIPTIONS = {
+    "c1_384e": "384 electrons (192 up / 192 down) in a cubic cell a=15.8 bohr, 32 ions on a jittered lattice, "
+               "192 real orbitals as tricubic B-splines on a 48^3 grid (FP32 coefficients N(0,0.1)), J1/J2 B-spline "
+               "Jastrows with 10 parameters, 512 walkers, delay rank 32, tau 0.3, FP32 move loop, FP64 recompute "
+               "every 100 sweeps",
+    "c0_32e": "32 electrons, 16 orbitals on a 32^3 grid, 8 ions, a=10 bohr, 64 walkers, rank-1 updates, FP64",
+    "c2_1536e": "1536 electrons, 768 orbitals on a 60^3 grid, 128 ions, a=25 bohr, 256 walkers, delay rank 64, FP32",
+}
+
+
+def bytes_per_ratio_launch(system, nw: int) -> int:
+    """Algorithmic bytes of one ratio-kernel launch (all walkers, one electron each).
+
+    per walker: 64 coefficient rows of lda orbitals (spline), 5 x lda orbital VGL written,
+    one inverse row read, all electron positions (3 x n_e) and ion positions (3 x n_ions)
+    read in the move-loop precision.
+    """
+    s = 4 if system.spec.precision == 4 else 8
+    lda = system.npad
+    per = 64 * lda * s + 5 * lda * s + lda * s + 3 * system.n_elec * s + 3 * len(system.ion_pos) * s
+    return per * nw
+
+
+def kernel_launches_per_sweep(system, k: int) -> int:
+    ne = system.n_elec
+    n = system.norb
+    per_iat = 3 if k > 1 else 4  # propose, ratio, accept (+ rank-1 update kernel)
+    flushes = 0
+    if k > 1:
+        flushes = 2 * (n // k) + 2 * (1 if n % k else 0)
+    return ne * per_iat + 2 * flushes + 1
+
+
+def read_traffic(workload: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"ratio_kernel_{workload}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(workload: str, max_seconds: float = 15.0):
+    """The oracle (CPU restatement of the reference math) on the host cores, bounded sample.
+
+    Full VMC sweeps (VMCBatched::advanceWalkers semantics, mt19937 stream) of 4 walkers
+    per host core, repeated until about max_seconds of work; OpenMP over walkers.
+    """
+    from oracle import oracle as orc
+    spec = SPECS[workload]
+    system = make_system(spec)
+    cores = os.cpu_count() or 1
+    nw = 4 * cores
+    R = make_walkers(system, nw, seed=3)
+    orc.set_threads(cores)
+    c = orc.Crowd(system, nw, spec.delay, spec.precision)
+    c.load_walkers(R)
+    c.evaluate_log(nthreads=cores)
+    rng = orc.Rng(11)
+    sweeps = 0
+    t0 = time.perf_counter()
+    while True:
+        c.vmc_sweeps(rng, 1, spec.tau, True)
+        sweeps += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    moves = sweeps * nw * system.n_elec
+    return {"value": moves / dt, "unit": "walker-moves/s", "cores": cores, "kind": "port",
+            "sample": f"{sweeps} sweep(s) x {nw} walkers x {system.n_elec} electrons of {workload} "
+                      f"({'FP32' if spec.precision == 4 else 'FP64'} oracle, OpenMP over walkers), {dt:.1f} s"}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    spec = SPECS[args.workload]
+    base = cpu_baseline(args.workload, max_seconds=max(5.0, 60.0 / max(args.steps, 1)))
+    line = {
+        "impl": "reference", "metric": "walker-moves/s", "value": base["value"], "unit": "walker-moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": spec.walkers * SPECS[args.workload].n_up * 2 / base["value"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if spec.precision == 4 else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {DESCRIPTIONS.get(args.workload, '')}",
+                   "step": "one VMC sweep (every electron of every walker moved once)",
+                   "what_runs": "the CPU restatement of the reference algorithms (oracle/), all host cores; the "
+                                "reference's own GPU build needs LAPACK/HDF5/libxml2/Boost and an offload compiler "
+                                "that this image lacks"},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "walker-moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int):
+    import torch
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    spec = SPECS[args.workload]
+    system = make_system(spec)
+    nw, k = spec.walkers, spec.delay
+    dsys = DeviceSystem(system)
+    crowd = Crowd(dsys, nw, k)
+    R = make_walkers(system, nw, seed=100 + rank)
+    crowd.load_walkers(R)
+    crowd.mw_evaluateLog()
+    seed = 2024 + 7919 * rank
+    recompute_every = spec.recompute_every
+    # warm-up (also captures the sweep graph)
+    crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
+    stream = torch.cuda.ExternalStream(crowd.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    crowd.vmc_sweeps_async(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    acc, rej = crowd.sync()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    moves = args.steps * nw * system.n_elec * world
+    # FP64 recomputes (3 kernels each) that fell inside the timed sweeps
+    recomputes = 0
+    if recompute_every:
+        recomputes = (args.warmup + args.steps) // recompute_every - args.warmup // recompute_every
+    value = moves / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
+    Rh = torch.from_numpy(crowd.positions()).pin_memory()
+    Rnp = Rh.numpy()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        crowd.load_walkers(Rnp)
+        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
+        Rnp[...] = crowd.positions()
+        lp, _, _ = crowd.get_log()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = moves / e2e_s
+    h2d = Rnp.nbytes
+    d2h = Rnp.nbytes + lp.nbytes
+
+    # dominant kernel: per-launch CUDA-event time of the proposed-position evaluation
+    crowd.mw_completeUpdates()
+    ratio_ms = crowd.profile_ratio(system.n_elec)
+    algo = bytes_per_ratio_launch(system, nw)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = algo / (ratio_ms / 1e3) / 1e9
+    traffic = read_traffic(args.workload)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    base = cpu_baseline(args.workload) if world == 1 and not args.no_cpu_baseline else None
+    line = {
+        "metric": "walker-moves/s", "value": value, "unit": "walker-moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if spec.precision == 4 else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {DESCRIPTIONS.get(args.workload, '')}",
+                   "step": "one VMC sweep (every electron of every walker moved once), CUDA graph replay",
+                   "walkers_per_gpu": nw, "electrons": system.n_elec, "delay_rank": k,
+                   "l2": "inputs larger than L2 (spline table 102 MB + inverses/gradients ~0.8 GB per sweep)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "ratio_kernel (distance rows + J1/J2 + spline VGL + det ratio)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                     else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": ratio_ms,
+                     "algorithmic_bytes_per_launch": algo},
+        "cpu_baseline": base,
+        "e2e": {"value": e2e_value, "unit": "walker-moves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": kernel_launches_per_sweep(system, k) * args.steps + 3 * recomputes,
+        "clocks": clk,
+        "acceptance": acc / max(acc + rej, 1),
+        "walker_sweeps_per_s": value / system.n_elec,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

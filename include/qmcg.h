@@ -177,6 +177,12 @@ int qmcg_vmc_sweeps_async(qmcg_crowd crowd, int num_sweeps);
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
 
+/* Measurement helper (no reference counterpart): average device time in ms of
+ * the proposed-position evaluation kernel (distance rows, J1/J2, spline VGL and
+ * determinant ratio) over num_electrons consecutive electrons, timed with CUDA
+ * events on the crowd's stream.  Writes only move scratch. */
+int qmcg_profile_ratio(qmcg_crowd crowd, int num_electrons, double* ms_per_launch);
+
 #ifdef __cplusplus
 }
 #endif

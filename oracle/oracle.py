@@ -50,6 +50,7 @@ def lib():
         L.orc_get_ainv.argtypes = [C.c_void_p, C.c_int, _dp]
         L.orc_get_jastrow_state.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_get_phi_vgl.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.orc_set_threads.argtypes = [C.c_int]
         L.orc_rng_create.restype = C.c_void_p
         L.orc_rng_create.argtypes = [C.c_uint]
         L.orc_rng_destroy.argtypes = [C.c_void_p]
@@ -127,6 +128,10 @@ def distance_row(lattice, R, r):
     rr = _d(r)
     lib().orc_distance_row(_ptr(lat), n, _ptr(R), _ptr(rr), _ptr(dist), _ptr(dr))
     return dist, dr
+
+
+def set_threads(n: int):
+    lib().orc_set_threads(int(n))
 
 
 class Det:

@@ -864,6 +864,7 @@ struct Crowd
   {
     const int s   = group_of(iat);
     const int row = iat - first_of(s);
+#pragma omp parallel for schedule(static)
     for (int iw = 0; iw < nw; iw++)
     {
       Walker& wk = w[iw];
@@ -900,6 +901,7 @@ struct Crowd
   // ---------------- ParticleSet::mw_makeMove -------------------------------
   void make_move(int iat, const double* displ)
   {
+#pragma omp parallel for schedule(static)
     for (int iw = 0; iw < nw; iw++)
     {
       Walker& wk = w[iw];
@@ -920,6 +922,7 @@ struct Crowd
   {
     const int s   = group_of(iat);
     const int row = iat - first_of(s);
+#pragma omp parallel for schedule(static)
     for (int iw = 0; iw < nw; iw++)
     {
       Walker& wk = w[iw];
@@ -968,6 +971,7 @@ struct Crowd
   {
     const int s   = group_of(iat);
     const int row = iat - first_of(s);
+#pragma omp parallel for schedule(static)
     for (int iw = 0; iw < nw; iw++)
     {
       Walker& wk = w[iw];
@@ -1051,6 +1055,7 @@ struct Crowd
   {
     if (delay_count[s] == 0)
       return;
+#pragma omp parallel for schedule(static)
     for (int iw = 0; iw < nw; iw++)
       w[iw].det[s].eng.update_inv(w[iw].det[s].Ainv.data(), delay_count[s]);
     delay_count[s] = 0;
@@ -1400,6 +1405,16 @@ void orc_get_phi_vgl(void* hv, int s, double* out)
       }
     }
   });
+}
+
+// ---- threads used by the per-walker loops (OpenMP over walkers, like crowds) ---
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : 1);
+#else
+  (void)n;
+#endif
 }
 
 // ---- RNG stream -----------------------------------------------------------

@@ -178,6 +178,11 @@ class Crowd:
         check(self.L.qmcg_crowd_sync(self.handle, C.byref(st)))
         return st.accepted, st.rejected
 
+    def profile_ratio(self, num_electrons: int) -> float:
+        ms = C.c_double()
+        check(self.L.qmcg_profile_ratio(self.handle, num_electrons, C.byref(ms)))
+        return ms.value
+
     def stream(self) -> int:
         p = C.c_void_p()
         check(self.L.qmcg_crowd_stream(self.handle, C.byref(p)))

@@ -319,6 +319,7 @@ struct qmcg_crowd_s
   virtual int get_phi(double* phi)                       = 0;
   virtual int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) = 0;
   virtual int sweeps_async(int n)                        = 0;
+  virtual int profile_ratio(int niat, double* ms)        = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
 };
 
@@ -341,6 +342,7 @@ struct Crowd final : qmcg_crowd_s
   double graph_tau = 0;
   uint64_t graph_seed = 0;
   int sweeps_since_recompute = 0;
+  int recompute_every        = 0;
 
   ~Crowd() override
   {
@@ -799,6 +801,7 @@ struct Crowd final : qmcg_crowd_s
     int rc = build_graph(p);
     if (rc)
       return rc;
+    recompute_every = p->recompute_every;
     CUDA_TRY(cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned long long), stream));
     const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
     std::vector<int> accbuf;
@@ -875,7 +878,52 @@ struct Crowd final : qmcg_crowd_s
     if (!graph || graph_rng_mode != 1)
       return fail(QMCG_ERR_STATE, "no device-RNG sweep graph built yet");
     for (int it = 0; it < n; it++)
+    {
       CUDA_TRY(cudaGraphLaunch(graph, stream));
+      sweeps_since_recompute++;
+      if (recompute_every > 0 && sweeps_since_recompute >= recompute_every)
+      {
+        int rc = recompute_device();
+        if (rc)
+          return rc;
+        sweeps_since_recompute = 0;
+      }
+    }
+    return QMCG_OK;
+  }
+
+  // Per-launch device time of ratio_kernel over niat consecutive electrons, each
+  // preceded by its (untimed) proposal; CUDA events on the crowd's stream.  Only
+  // move scratch is written, the walker state is left unchanged.
+  int profile_ratio(int niat, double* ms) override
+  {
+    if (niat <= 0 || !ms)
+      return fail(QMCG_ERR_ARG, "bad profile arguments");
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "pending delayed updates; call complete_updates first");
+    std::vector<cudaEvent_t> ev(2 * (size_t)niat);
+    for (auto& e : ev)
+      CUDA_TRY(cudaEventCreate(&e));
+    for (int i = 0; i < niat; i++)
+    {
+      const int iat = i % sys->ne;
+      CUDA_TRY(launch_propose<T>(s, iat, 0, 1, stream));
+      CUDA_TRY(cudaEventRecord(ev[2 * i], stream));
+      CUDA_TRY(launch_ratio<T>(s, iat, 1, stream));
+      CUDA_TRY(cudaEventRecord(ev[2 * i + 1], stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    double tot = 0;
+    for (int i = 0; i < niat; i++)
+    {
+      float t = 0;
+      CUDA_TRY(cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]));
+      tot += t;
+    }
+    for (auto& e : ev)
+      cudaEventDestroy(e);
+    invrow_iat = -1;
+    *ms        = tot / niat;
     return QMCG_OK;
   }
 
@@ -996,3 +1044,4 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
 }
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
 extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }
+extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
