@@ -177,6 +177,20 @@ int qmcg_vmc_sweeps_async(qmcg_crowd crowd, int num_sweeps);
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
 
+/* ---------------------------------------------------------------- determinant engine */
+/* Delayed-update flush on caller device buffers for num_walkers walkers:
+ *   Ainv -= (Ainv U^T - E) (Binv V),  E[delay_list[c]][c] = 1 (slots with -1 skipped)
+ * DelayedUpdateBatched::mw_updateInvMat (src/QMCWaveFunctions/Fermion/DelayedUpdateBatched.h:675-738).
+ * precision 4 (float) or 8 (double); per walker, row-major and contiguous:
+ *   ainv [n][lda], u and v [delay_rank][lda], binv [delay_rank][delay_rank], delay_list [delay_rank];
+ * walker w's buffers start at w * (n*lda), w * (delay_rank*lda), w * delay_rank^2, w * delay_rank.
+ * Only the first delay_count slots are used.  Enqueued on `stream` (a cudaStream_t, NULL =
+ * the legacy default stream); a scratch buffer of num_walkers*delay_rank*lda elements is
+ * taken from the stream-ordered allocator for the duration of the call. */
+int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
+                           void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
+                           void* stream);
+
 /* Measurement helper (no reference counterpart): average device time in ms of
  * the proposed-position evaluation kernel (distance rows, J1/J2, spline VGL and
  * determinant ratio) over num_electrons consecutive electrons, timed with CUDA

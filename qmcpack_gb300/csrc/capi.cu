@@ -1045,3 +1045,68 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
 extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }
 extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
+
+// ---------------------------------------------------------------------------
+// determinant-engine flush on caller device buffers
+// (DelayedUpdateBatched::mw_updateInvMat, DelayedUpdateBatched.h:675-738)
+// ---------------------------------------------------------------------------
+static int check_flush_args(int prec, int nw, int n, int lda, int k, int dc, void* ainv, const void* u,
+                            const void* v, const void* binv, const int* dl)
+{
+  if (prec != 4 && prec != 8)
+    return fail(QMCG_ERR_ARG, "precision must be 4 or 8");
+  if (nw < 0 || n <= 0 || lda < n || k <= 0 || dc < 0 || dc > k)
+    return fail(QMCG_ERR_ARG, "need n > 0, lda >= n, 0 <= delay_count <= delay_rank");
+  if (nw > 0 && dc > 0 && (!ainv || !u || !v || !binv || !dl))
+    return fail(QMCG_ERR_ARG, "null device buffer");
+  return QMCG_OK;
+}
+
+template<typename T>
+static FlushArgs<T> make_flush_args(int nw, int n, int lda, int k, int dc, void* ainv, const void* u, const void* v,
+                                    const void* binv, const int* dl, T* w)
+{
+  FlushArgs<T> f;
+  f.nw         = nw;
+  f.n          = n;
+  f.lda        = lda;
+  f.k          = k;
+  f.dc         = dc;
+  f.sA         = (long long)n * lda;
+  f.sU         = (long long)k * lda;
+  f.sB         = (long long)k * k;
+  f.sD         = k;
+  f.ainv       = static_cast<T*>(ainv);
+  f.u          = static_cast<const T*>(u);
+  f.v          = static_cast<const T*>(v);
+  f.binv       = static_cast<const T*>(binv);
+  f.delay_list = dl;
+  f.w          = w;
+  return f;
+}
+
+template<typename T>
+static int flush_with_malloc(int nw, int n, int lda, int k, int dc, void* ainv, const void* u, const void* v,
+                             const void* binv, const int* dl, cudaStream_t st)
+{
+  CUDA_TRY(setup_move_kernels<T>());
+  T* w = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&w), std::max<size_t>(1, (size_t)nw * k * lda) * sizeof(T), st));
+  const cudaError_t e = launch_flush_args(make_flush_args<T>(nw, n, lda, k, dc, ainv, u, v, binv, dl, w), st);
+  CUDA_TRY(cudaFreeAsync(w, st));
+  CUDA_TRY(e);
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_mw_update_inv_mat(int precision, int nw, int n, int lda, int k, int dc, void* ainv, const void* u,
+                                      const void* v, const void* binv, const int* delay_list, void* stream)
+{
+  int rc = check_flush_args(precision, nw, n, lda, k, dc, ainv, u, v, binv, delay_list);
+  if (rc)
+    return rc;
+  if (nw == 0 || dc == 0)
+    return QMCG_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return precision == 8 ? flush_with_malloc<double>(nw, n, lda, k, dc, ainv, u, v, binv, delay_list, st)
+                        : flush_with_malloc<float>(nw, n, lda, k, dc, ainv, u, v, binv, delay_list, st);
+}

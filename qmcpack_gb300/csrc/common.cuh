@@ -85,6 +85,21 @@ struct DevState
   int use_drift;
 };
 
+// Arguments of the delayed-update flush Ainv -= (Ainv U^T - E)(Binv V) over a
+// batch of walkers: row-major per walker, per-walker strides in elements.
+template<typename T>
+struct FlushArgs
+{
+  int nw, n, lda, k, dc;
+  long long sA, sU, sB, sD; // walker strides of Ainv, U/V, Binv, delay_list
+  T* ainv;
+  const T* u;
+  const T* v;
+  const T* binv;
+  const int* delay_list;
+  T* w;                     // scratch [nw][k][lda]
+};
+
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
 // ---------------------------------------------------------------------------

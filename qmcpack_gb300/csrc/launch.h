@@ -5,6 +5,7 @@
 
 namespace qmcg
 {
+
 template<typename T>
 cudaError_t launch_propose(const DevState<T>& s, int iat, int dc, int driver, cudaStream_t st);
 template<typename T>
@@ -15,6 +16,8 @@ template<typename T>
 cudaError_t launch_accept(const DevState<T>& s, int iat, int dc, int driver, cudaStream_t st);
 template<typename T>
 cudaError_t launch_flush_simt(const DevState<T>& s, int spin, int dc, T* W, cudaStream_t st);
+template<typename T>
+cudaError_t launch_flush_args(const FlushArgs<T>& f, cudaStream_t st);
 
 template<typename T>
 cudaError_t setup_move_kernels();

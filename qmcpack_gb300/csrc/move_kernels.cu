@@ -598,67 +598,79 @@ __global__ void sm1_kernel(DevState<T> s, int iat)
 
 // ---------------------------------------------------------------------------
 // Delayed-update flush, SIMT form: W = Binv V, then per row block
-// Ainv[rows] -= (Ainv[rows] U^T - E[rows]) W.
+// Ainv[rows] -= (Ainv[rows] U^T - E[rows]) W.  Works on any batch of walkers
+// through FlushArgs (crowd buffers or caller device buffers).
 // ---------------------------------------------------------------------------
 template<typename T>
-__global__ void flush_w_kernel(DevState<T> s, int spin, int dc, T* W)
+__global__ void flush_w_kernel(FlushArgs<T> f)
 {
-  const int iw = blockIdx.x;
-  const size_t wslot = (size_t)spin * s.nw + iw;
-  const T* Binv = s.Binv + wslot * s.k * s.k;
-  const T* V    = s.V + wslot * s.k * s.lda;
-  T* Wi         = W + (size_t)iw * s.k * s.lda;
-  for (int e = threadIdx.x; e < dc * s.norb; e += blockDim.x)
+  const int iw  = blockIdx.x;
+  const T* Binv = f.binv + (size_t)iw * f.sB;
+  const T* V    = f.v + (size_t)iw * f.sU;
+  T* Wi         = f.w + (size_t)iw * f.k * f.lda;
+  for (int e = threadIdx.x; e < f.dc * f.n; e += blockDim.x)
   {
-    const int l = e / s.norb, i = e % s.norb;
+    const int l = e / f.n, i = e % f.n;
     T a         = 0;
-    for (int c = 0; c < dc; c++)
-      a += Binv[(size_t)l * s.k + c] * V[(size_t)c * s.lda + i];
-    Wi[(size_t)l * s.lda + i] = a;
+    for (int c = 0; c < f.dc; c++)
+      a += Binv[(size_t)l * f.k + c] * V[(size_t)c * f.lda + i];
+    Wi[(size_t)l * f.lda + i] = a;
   }
 }
 
 template<typename T, int RB>
-__global__ void flush_update_kernel(DevState<T> s, int spin, int dc, const T* W)
+__global__ void flush_update_kernel(FlushArgs<T> f)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* arows = reinterpret_cast<T*>(smem_raw); // RB x lda
-  T* t1    = arows + RB * s.lda;             // RB x k
+  T* t1    = arows + RB * f.lda;             // RB x k
   const int iw = blockIdx.x;
   const int r0 = blockIdx.y * RB;
-  const int n  = s.norb;
-  const size_t wslot = (size_t)spin * s.nw + iw;
-  T* A         = s.Ainv + wslot * n * s.lda;
-  const T* U   = s.U + wslot * s.k * s.lda;
-  const T* Wi  = W + (size_t)iw * s.k * s.lda;
-  const int* dlist = s.delay_list + wslot * s.k;
+  const int n  = f.n;
+  T* A         = f.ainv + (size_t)iw * f.sA;
+  const T* U   = f.u + (size_t)iw * f.sU;
+  const T* Wi  = f.w + (size_t)iw * f.k * f.lda;
+  const int* dlist = f.delay_list + (size_t)iw * f.sD;
   const int nr = min(RB, n - r0);
   for (int e = threadIdx.x; e < nr * n; e += blockDim.x)
   {
     const int r = e / n, i = e % n;
-    arows[r * s.lda + i] = A[(size_t)(r0 + r) * s.lda + i];
+    arows[r * f.lda + i] = A[(size_t)(r0 + r) * f.lda + i];
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int e = wid; e < nr * dc; e += nwarp)
+  for (int e = wid; e < nr * f.dc; e += nwarp)
   {
-    const int r = e / dc, c = e % dc;
+    const int r = e / f.dc, c = e % f.dc;
     T a         = 0;
     for (int i = lane; i < n; i += 32)
-      a += arows[r * s.lda + i] * U[(size_t)c * s.lda + i];
+      a += arows[r * f.lda + i] * U[(size_t)c * f.lda + i];
     a = warp_sum(a);
     if (lane == 0)
-      t1[r * s.k + c] = (dlist[c] == r0 + r) ? a - T(1) : a;
+      t1[r * f.k + c] = (dlist[c] == r0 + r) ? a - T(1) : a;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < nr * n; e += blockDim.x)
   {
     const int r = e / n, i = e % n;
     T a         = 0;
-    for (int c = 0; c < dc; c++)
-      a += t1[r * s.k + c] * Wi[(size_t)c * s.lda + i];
-    A[(size_t)(r0 + r) * s.lda + i] = arows[r * s.lda + i] - a;
+    for (int c = 0; c < f.dc; c++)
+      a += t1[r * f.k + c] * Wi[(size_t)c * f.lda + i];
+    A[(size_t)(r0 + r) * f.lda + i] = arows[r * f.lda + i] - a;
   }
+}
+
+template<typename T>
+cudaError_t launch_flush_args(const FlushArgs<T>& f, cudaStream_t st)
+{
+  if (f.dc <= 0 || f.nw <= 0)
+    return cudaSuccess;
+  flush_w_kernel<T><<<f.nw, 256, 0, st>>>(f);
+  constexpr int RB = 16;
+  const size_t sm = sizeof(T) * ((size_t)RB * f.lda + (size_t)RB * f.k);
+  dim3 grid(f.nw, (f.n + RB - 1) / RB);
+  flush_update_kernel<T, RB><<<grid, 256, sm, st>>>(f);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -712,14 +724,23 @@ cudaError_t launch_accept(const DevState<T>& s, int iat, int dc, int driver, cud
 template<typename T>
 cudaError_t launch_flush_simt(const DevState<T>& s, int spin, int dc, T* W, cudaStream_t st)
 {
-  if (dc <= 0)
-    return cudaSuccess;
-  flush_w_kernel<T><<<s.nw, 256, 0, st>>>(s, spin, dc, W);
-  constexpr int RB = 16;
-  const size_t sm = sizeof(T) * ((size_t)RB * s.lda + (size_t)RB * s.k);
-  dim3 grid(s.nw, (s.norb + RB - 1) / RB);
-  flush_update_kernel<T, RB><<<grid, 256, sm, st>>>(s, spin, dc, W);
-  return cudaGetLastError();
+  FlushArgs<T> f;
+  f.nw         = s.nw;
+  f.n          = s.norb;
+  f.lda        = s.lda;
+  f.k          = s.k;
+  f.dc         = dc;
+  f.sA         = (long long)s.norb * s.lda;
+  f.sU         = (long long)s.k * s.lda;
+  f.sB         = (long long)s.k * s.k;
+  f.sD         = s.k;
+  f.ainv       = s.Ainv + (size_t)spin * s.nw * f.sA;
+  f.u          = s.U + (size_t)spin * s.nw * f.sU;
+  f.v          = s.V + (size_t)spin * s.nw * f.sU;
+  f.binv       = s.Binv + (size_t)spin * s.nw * f.sB;
+  f.delay_list = s.delay_list + (size_t)spin * s.nw * f.sD;
+  f.w          = W;
+  return launch_flush_args(f, st);
 }
 
 template<typename T>
@@ -738,7 +759,8 @@ cudaError_t setup_move_kernels()
   template cudaError_t launch_make_move<T>(const DevState<T>&, int, cudaStream_t);                                     \
   template cudaError_t launch_ratio<T>(const DevState<T>&, int, int, cudaStream_t);                                    \
   template cudaError_t launch_accept<T>(const DevState<T>&, int, int, int, cudaStream_t);                              \
-  template cudaError_t launch_flush_simt<T>(const DevState<T>&, int, int, T*, cudaStream_t);
+  template cudaError_t launch_flush_simt<T>(const DevState<T>&, int, int, T*, cudaStream_t);                        \
+  template cudaError_t launch_flush_args<T>(const FlushArgs<T>&, cudaStream_t);
 INSTANTIATE(float)
 INSTANTIATE(double)
 #undef INSTANTIATE
