@@ -191,6 +191,30 @@ int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int d
                            void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                            void* stream);
 
+/* Allocation-free variant of qmcg_mw_update_inv_mat.  It has no counterpart in
+ * the reference: QMCPACK's engine always allocates its own scratch.  It exists for
+ * callers that cannot call cudaMalloc or a stream-ordered allocator: code whose
+ * device memory is owned entirely by another allocator (a framework's caching
+ * allocator, an offload runtime that reserves the device), code that cannot
+ * afford the device-wide synchronisation cudaFree implies while other streams run,
+ * and code running where allocation is forbidden (driver callbacks, real-time
+ * threads).  Same arguments, layout and result as qmcg_mw_update_inv_mat; the
+ * caller still passes every input and output.
+ * Limit: its scratch is one fixed device array of QMCG_NOALLOC_SCRATCH_BYTES
+ * (16 MiB) that every GPU on which this code is loaded holds until the process
+ * exits; calls needing num_walkers*delay_rank*lda*element_size bytes beyond it
+ * return QMCG_ERR_ARG and the caller splits its walkers into batches.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  Every call shares the array and it keeps the last call's contents;
+ * nothing in it has to start at zero (every element a call reads is written
+ * earlier by the same call), but calls that overlap on the GPU race and must be
+ * ordered by the caller, for example by issuing them on one stream. */
+#define QMCG_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int qmcg_mw_update_inv_mat_noalloc(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
+                                   void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
+                                   void* stream);
+
 /* Measurement helper (no reference counterpart): average device time in ms of
  * the proposed-position evaluation kernel (distance rows, J1/J2, spline VGL and
  * determinant ratio) over num_electrons consecutive electrons, timed with CUDA

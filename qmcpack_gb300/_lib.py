@@ -18,7 +18,7 @@ EXPORTS = [
     "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
-    "qmcg_mw_update_inv_mat", "qmcg_profile_ratio",
+    "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
 ]
 
 
@@ -87,6 +87,8 @@ def load(path: str = LIB_PATH):
         "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
+        "qmcg_mw_update_inv_mat_noalloc": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
+                                           vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

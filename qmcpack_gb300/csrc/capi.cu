@@ -40,6 +40,11 @@ static int fail(int code, const std::string& msg)
 
 extern "C" const char* qmcg_last_error(void) { return g_last_error.c_str(); }
 
+namespace qmcg
+{
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+} // namespace qmcg
+
 extern "C" int qmcg_device_count(int* count)
 {
   int n = 0;

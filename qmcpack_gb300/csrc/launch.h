@@ -1,10 +1,13 @@
 // Host-side launch interface between the translation units of the library.
 #pragma once
 #include <cuda_runtime.h>
+#include <string>
 #include "common.cuh"
 
 namespace qmcg
 {
+// records the message returned by qmcg_last_error() and returns code
+int set_error(int code, const std::string& msg);
 
 template<typename T>
 cudaError_t launch_propose(const DevState<T>& s, int iat, int dc, int driver, cudaStream_t st);
