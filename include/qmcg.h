@@ -84,6 +84,8 @@ typedef struct
   int rng_mode;
   uint64_t seed;
   int recompute_every; /* FP64 recompute after every this many sweeps; 0 = never */
+  int path;            /* 0: walker-resident sweep kernel when rng_mode is 1 (one CTA owns a walker for a whole
+                          sweep), else the staged per-electron kernels; 1: always the staged kernels */
 } qmcg_sweep_params;
 
 typedef struct

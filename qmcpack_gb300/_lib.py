@@ -35,7 +35,7 @@ class SystemDesc(C.Structure):
 
 class SweepParams(C.Structure):
     _fields_ = [("tau", C.c_double), ("use_drift", C.c_int), ("rng_mode", C.c_int), ("seed", C.c_uint64),
-                ("recompute_every", C.c_int)]
+                ("recompute_every", C.c_int), ("path", C.c_int)]
 
 
 class SweepStats(C.Structure):

@@ -343,7 +343,8 @@ struct Crowd final : qmcg_crowd_s
   bool stream_seeded = false;
   uint64_t hs_seed    = 0;
   cudaGraphExec_t graph = nullptr;
-  int graph_rng_mode = -1, graph_use_drift = -1;
+  int graph_rng_mode = -1, graph_use_drift = -1, graph_path = -1;
+  int sweep_grid_size = 0;
   double graph_tau = 0;
   uint64_t graph_seed = 0;
   int sweeps_since_recompute = 0;
@@ -368,6 +369,7 @@ struct Crowd final : qmcg_crowd_s
     k   = k_;
     CUDA_TRY(setup_move_kernels<T>());
     CUDA_TRY(setup_recompute_kernels<T>());
+    CUDA_TRY(setup_sweep_kernel<T>());
     CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     DevState<T>& d = s;
     d.nw        = nw;
@@ -441,6 +443,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&unif_d, nu));
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
+    CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size));
     d.gauss     = gauss_d;
     d.uniform   = unif_d;
     d.rng_mode  = 1;
@@ -754,10 +757,21 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 
+  bool resident(const qmcg_sweep_params* p) const { return p->rng_mode == 1 && p->path == 0; }
+
+  // one sweep of the walker-resident kernel: every walker's whole sweep in one launch
+  int enqueue_sweep_resident()
+  {
+    CUDA_TRY(launch_sweep<T>(s, W, sweep_grid_size, stream));
+    bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
+    CUDA_TRY(cudaGetLastError());
+    return QMCG_OK;
+  }
+
   int build_graph(const qmcg_sweep_params* p)
   {
     if (graph && graph_rng_mode == p->rng_mode && graph_use_drift == p->use_drift && graph_tau == p->tau &&
-        graph_seed == p->seed)
+        graph_seed == p->seed && graph_path == (resident(p) ? 0 : 1))
       return QMCG_OK;
     if (graph)
     {
@@ -770,7 +784,7 @@ struct Crowd final : qmcg_crowd_s
     s.seed      = p->seed;
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_sweep();
+    int rc = resident(p) ? enqueue_sweep_resident() : enqueue_sweep();
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (rc)
       return rc;
@@ -784,6 +798,7 @@ struct Crowd final : qmcg_crowd_s
     graph_use_drift = p->use_drift;
     graph_tau       = p->tau;
     graph_seed      = p->seed;
+    graph_path      = resident(p) ? 0 : 1;
     return QMCG_OK;
   }
 

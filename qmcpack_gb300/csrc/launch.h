@@ -27,6 +27,16 @@ cudaError_t setup_move_kernels();
 template<typename T>
 cudaError_t setup_recompute_kernels();
 
+// walker-resident sweep (sweep_kernel.cu)
+template<typename T>
+cudaError_t setup_sweep_kernel();
+template<typename T>
+size_t sweep_smem_bytes(const DevState<T>& s);
+template<typename T>
+cudaError_t sweep_grid(const DevState<T>& s, int* grid);
+template<typename T>
+cudaError_t launch_sweep(const DevState<T>& s, T* W, int grid, cudaStream_t st);
+
 // recompute path (recompute_kernels.cu)
 template<typename T>
 cudaError_t launch_recompute(const DevState<T>& s, double* mscratch, cudaStream_t st);
