@@ -41,32 +41,45 @@ DESCRIPTIONS = {
 }
 
 
-def bytes_per_ratio_launch(system, nw: int) -> int:
-    """Algorithmic bytes of one ratio-kernel launch (all walkers, one electron each).
+def flush_bytes_per_launch(system, k: int, nw: int) -> int:
+    """Algorithmic bytes of one batched flush of one spin: the inverse read and written,
+    U, V (k x lda) and Binv (k x k) read, per walker."""
+    s = 4 if system.spec.precision == 4 else 8
+    lda, n = system.npad, system.norb
+    return int(s * nw * (2 * n * lda + 2 * k * lda + k * k))
 
-    per walker: 64 coefficient rows of lda orbitals (spline), 5 x lda orbital VGL written,
-    one inverse row read, all electron positions (3 x n_e) and ion positions (3 x n_ions)
-    read in the move-loop precision.
+
+def bytes_per_walker_move(system, k: int, with_flush: bool = True) -> int:
+    """Algorithmic bytes of one walker-move of the walker-resident sweep kernel.
+
+    spline: 64 coefficient rows of lda orbitals; inverse row: lda; delayed-update rows
+    U and V read for the inverse row: 2 x (k-1)/2 rows of lda on average; current-row
+    orbital gradients and values: 4 x lda; delayed-update flush: the inverse read and
+    written once every k moves, 2 x N x lda / k.  Positions and the two-body Jastrow
+    state live in shared memory for the whole sweep and are not counted.
     """
     s = 4 if system.spec.precision == 4 else 8
-    lda = system.npad
-    per = 64 * lda * s + 5 * lda * s + lda * s + 3 * system.n_elec * s + 3 * len(system.ion_pos) * s
-    return per * nw
+    lda, n = system.npad, system.norb
+    elems = 64 * lda + lda + (k - 1) * lda + 4 * lda
+    if with_flush:
+        elems += (2 * n * lda) / max(k, 1)
+    return int(elems * s)
 
 
-def kernel_launches_per_sweep(system, k: int) -> int:
-    ne = system.n_elec
-    n = system.norb
-    per_iat = 3 if k > 1 else 4  # propose, ratio, accept (+ rank-1 update kernel)
-    flushes = 0
+def launches_per_sweep(system, k: int) -> int:
+    """Kernels per sweep on the walker-resident path: one resident launch and one batched
+    flush per segment of up to k electrons of a spin group (one resident launch for the
+    sweep with rank-1 updates), the masked FP64 repair (vgl_all, gj_inverse, jastrow_full,
+    finish_repair) and the counter bump."""
     if k > 1:
-        flushes = 2 * (n // k) + 2 * (1 if n % k else 0)
-    return ne * per_iat + 2 * flushes + 1
+        segs = 2 * ((system.spec.n_up + k - 1) // k)
+        return 2 * segs + 5
+    return 1 + 5
 
 
 def read_traffic(workload: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"ratio_kernel_{workload}.md")
+    path = os.path.join(ROOT, "profiles", f"sweep_kernel_{workload}.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -198,7 +211,9 @@ def run_ours(args, rank: int, world: int):
     crowd.mw_evaluateLog()
     seed = 2024 + 7919 * rank
     recompute_every = spec.recompute_every
-    # warm-up (also captures the sweep graph)
+    # equilibration from the uniform start (untimed), then warm-up (also captures the sweep graph)
+    if args.equil > 0:
+        crowd.vmc_sweeps(args.equil, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
     crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
     stream = torch.cuda.ExternalStream(crowd.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -217,16 +232,17 @@ def run_ours(args, rank: int, world: int):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     acc, rej = crowd.sync()
+    repaired = crowd.last_repaired
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     moves = args.steps * nw * system.n_elec * world
-    # FP64 recomputes (3 kernels each) that fell inside the timed sweeps
+    value = moves / (ms / 1e3)
+    sweeps_done = args.equil + args.warmup
     recomputes = 0
     if recompute_every:
-        recomputes = (args.warmup + args.steps) // recompute_every - args.warmup // recompute_every
-    value = moves / (ms / 1e3)
+        recomputes = (sweeps_done + args.steps) // recompute_every - sweeps_done // recompute_every
 
     # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
     Rh = torch.from_numpy(crowd.positions()).pin_memory()
@@ -250,10 +266,12 @@ def run_ours(args, rank: int, world: int):
     h2d = Rnp.nbytes
     d2h = Rnp.nbytes + lp.nbytes
 
-    # dominant kernel: per-launch CUDA-event time of the proposed-position evaluation
-    crowd.mw_completeUpdates()
-    ratio_ms = crowd.profile_ratio(system.n_elec)
-    algo = bytes_per_ratio_launch(system, nw)
+    # dominant kernel: per-launch CUDA-event time of the walker-resident kernel (one
+    # launch = one segment of up to k electrons of every walker); the batched flush
+    # is timed alongside
+    seg_ms, flush_ms, seg_per_sweep, flush_per_sweep = crowd.profile_sweep(3)
+    algo = bytes_per_walker_move(system, k, with_flush=False) * nw * system.n_elec // seg_per_sweep
+    flush_bytes = flush_bytes_per_launch(system, k, nw)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -262,7 +280,7 @@ def run_ours(args, rank: int, world: int):
     peak = peaks.get("hbm_gbs")
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    achieved = algo / (ratio_ms / 1e3) / 1e9
+    achieved = algo / (seg_ms / 1e3) / 1e9
     traffic = read_traffic(args.workload)
     if rank != 0:
         if dist:
@@ -279,16 +297,22 @@ def run_ours(args, rank: int, world: int):
                    "walkers_per_gpu": nw, "electrons": system.n_elec, "delay_rank": k,
                    "l2": "inputs larger than L2 (spline table 102 MB + inverses/gradients ~0.8 GB per sweep)",
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "ratio_kernel (distance rows + J1/J2 + spline VGL + det ratio)",
+        "roofline": {"bound": "hbm", "kernel": "sweep_kernel (walker-resident; one launch = up to k electrons "
+                                                 "of every walker)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
-                     else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": ratio_ms,
-                     "algorithmic_bytes_per_launch": algo},
+                     else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": seg_ms,
+                     "algorithmic_bytes_per_launch": algo, "launches_per_sweep": seg_per_sweep,
+                     "flush": {"kernel": "flush_fused_kernel", "ms_per_launch": flush_ms,
+                               "launches_per_sweep": flush_per_sweep, "algorithmic_bytes_per_launch": flush_bytes,
+                               "achieved_gbs": flush_bytes / (flush_ms / 1e3) / 1e9 if flush_ms else None}},
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "walker-moves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": kernel_launches_per_sweep(system, k) * args.steps + 3 * recomputes,
+        "gpu_launches": launches_per_sweep(system, k) * args.steps + 3 * recomputes,
         "clocks": clk,
         "acceptance": acc / max(acc + rej, 1),
+        "walkers_repaired_in_timed_sweeps": repaired,
+        "equilibration_sweeps": args.equil,
         "walker_sweeps_per_s": value / system.n_elec,
     }
     print(json.dumps(line), flush=True)
@@ -304,6 +328,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--equil", type=int, default=20, help="untimed equilibration sweeps before the warm-up")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -92,6 +92,9 @@ typedef struct
 {
   uint64_t accepted;
   uint64_t rejected;
+  uint64_t repaired;   /* walkers whose state was rebuilt by an FP64 recompute after a sweep because the
+                          tracked inverse failed its health check |Ainv[row] . phi(r_row) - 1| > tol
+                          (1e-3 in FP32, 1e-7 in FP64) or produced a non-finite ratio */
   int status;          /* OR of walker status bits since the last call */
 } qmcg_sweep_stats;
 
@@ -222,6 +225,14 @@ int qmcg_mw_update_inv_mat_noalloc(int precision, int num_walkers, int n, int ld
  * determinant ratio) over num_electrons consecutive electrons, timed with CUDA
  * events on the crowd's stream.  Writes only move scratch. */
 int qmcg_profile_ratio(qmcg_crowd crowd, int num_electrons, double* ms_per_launch);
+
+/* Measurement helper (no reference counterpart): device time of the
+ * walker-resident path over num_sweeps real sweeps, every launch bracketed by
+ * CUDA events on the crowd's stream.  out[0] = ms per walker-resident kernel
+ * launch (a segment of up to delay_rank electrons of every walker), out[1] = ms
+ * per batched flush launch, out[2] and out[3] = launches of each per sweep.
+ * Needs a graph built by qmcg_vmc_sweeps with rng_mode 1 and path 0. */
+int qmcg_profile_sweep(qmcg_crowd crowd, int num_sweeps, double* out4);
 
 #ifdef __cplusplus
 }

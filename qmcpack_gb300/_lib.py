@@ -18,7 +18,7 @@ EXPORTS = [
     "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
-    "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
+    "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio", "qmcg_profile_sweep",
 ]
 
 
@@ -39,7 +39,7 @@ class SweepParams(C.Structure):
 
 
 class SweepStats(C.Structure):
-    _fields_ = [("accepted", C.c_uint64), ("rejected", C.c_uint64), ("status", C.c_int)]
+    _fields_ = [("accepted", C.c_uint64), ("rejected", C.c_uint64), ("repaired", C.c_uint64), ("status", C.c_int)]
 
 
 _LIB = None
@@ -86,6 +86,7 @@ def load(path: str = LIB_PATH):
         "qmcg_vmc_sweeps_async": [vp, C.c_int],
         "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
+        "qmcg_profile_sweep": [vp, C.c_int, _dp],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_noalloc": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                            vp],

@@ -168,6 +168,7 @@ class Crowd:
         acc = np.zeros((nsweeps, self.ne, self.nw), np.int32) if log_accepts else None
         check(self.L.qmcg_vmc_sweeps(self.handle, C.byref(p), nsweeps, C.byref(st),
                                      _p(acc, _ip) if acc is not None else None))
+        self.last_repaired = st.repaired
         return st.accepted, st.rejected, acc
 
     def vmc_sweeps_async(self, nsweeps: int):
@@ -176,12 +177,19 @@ class Crowd:
     def sync(self):
         st = SweepStats()
         check(self.L.qmcg_crowd_sync(self.handle, C.byref(st)))
+        self.last_repaired = st.repaired
         return st.accepted, st.rejected
 
     def profile_ratio(self, num_electrons: int) -> float:
         ms = C.c_double()
         check(self.L.qmcg_profile_ratio(self.handle, num_electrons, C.byref(ms)))
         return ms.value
+
+    def profile_sweep(self, nsweeps: int):
+        """(ms per resident-kernel launch, ms per flush launch, resident launches per sweep, flushes per sweep)"""
+        out = np.zeros(4)
+        check(self.L.qmcg_profile_sweep(self.handle, nsweeps, _p(out)))
+        return float(out[0]), float(out[1]), int(out[2]), int(out[3])
 
     def stream(self) -> int:
         p = C.c_void_p()

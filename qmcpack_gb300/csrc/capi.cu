@@ -325,6 +325,7 @@ struct qmcg_crowd_s
   virtual int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) = 0;
   virtual int sweeps_async(int n)                        = 0;
   virtual int profile_ratio(int niat, double* ms)        = 0;
+  virtual int profile_sweep(int n, double* out)          = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
 };
 
@@ -370,6 +371,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(setup_move_kernels<T>());
     CUDA_TRY(setup_recompute_kernels<T>());
     CUDA_TRY(setup_sweep_kernel<T>());
+    CUDA_TRY(setup_flush_fused<T>());
     CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     DevState<T>& d = s;
     d.nw        = nw;
@@ -410,6 +412,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.Ainv, 2 * (size_t)nw * N * lda));
     CUDA_TRY(mem.alloc(&d.dgrad, 2 * (size_t)nw * N * 3 * lda));
     CUDA_TRY(mem.alloc(&d.dlap, 2 * (size_t)nw * N * lda));
+    CUDA_TRY(mem.alloc(&d.psiv, 2 * (size_t)nw * N * lda));
     CUDA_TRY(mem.alloc(&d.U, 2 * (size_t)nw * k * lda));
     CUDA_TRY(mem.alloc(&d.V, 2 * (size_t)nw * k * lda));
     CUDA_TRY(mem.alloc(&d.Binv, 2 * (size_t)nw * k * k));
@@ -433,7 +436,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.flag, (size_t)nw));
     CUDA_TRY(mem.alloc(&d.accepted, (size_t)nw));
     CUDA_TRY(mem.alloc(&d.status, (size_t)nw));
-    CUDA_TRY(mem.alloc(&d.counters, 2));
+    CUDA_TRY(mem.alloc(&d.counters, 3));
     CUDA_TRY(mem.alloc(&d.ucursor, 2));
     CUDA_TRY(mem.alloc(&d.sweep_counter, 1));
     CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
@@ -513,7 +516,7 @@ struct Crowd final : qmcg_crowd_s
 
   int recompute_device()
   {
-    CUDA_TRY(launch_recompute<T>(s, Mt, stream));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 0, stream));
     dc[0] = dc[1] = 0;
     invrow_iat    = -1;
     return QMCG_OK;
@@ -752,6 +755,7 @@ struct Crowd final : qmcg_crowd_s
     for (int sp = 0; sp < 2; sp++)
       if (k > 1 && d[sp] > 0)
         CUDA_TRY(launch_flush_simt<T>(s, sp, d[sp], W, stream));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
     CUDA_TRY(cudaGetLastError());
     return QMCG_OK;
@@ -759,10 +763,27 @@ struct Crowd final : qmcg_crowd_s
 
   bool resident(const qmcg_sweep_params* p) const { return p->rng_mode == 1 && p->path == 0; }
 
-  // one sweep of the walker-resident kernel: every walker's whole sweep in one launch
+  // one sweep on the walker-resident path: with delayed updates, one resident
+  // launch per segment of up to k electrons of one spin group followed by the
+  // batched flush of that spin; with rank-1 updates one launch for the sweep
   int enqueue_sweep_resident()
   {
-    CUDA_TRY(launch_sweep<T>(s, W, sweep_grid_size, stream));
+    if (k > 1)
+    {
+      for (int g = 0; g < 2; g++)
+      {
+        const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
+        for (int i0 = first; i0 < last; i0 += k)
+        {
+          const int i1 = std::min(i0 + k, last);
+          CUDA_TRY(launch_sweep_segment<T>(s, W, sweep_grid_size, i0, i1, 0, stream));
+          CUDA_TRY(launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream));
+        }
+      }
+    }
+    else
+      CUDA_TRY(launch_sweep<T>(s, W, sweep_grid_size, stream));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
     CUDA_TRY(cudaGetLastError());
     return QMCG_OK;
@@ -822,7 +843,7 @@ struct Crowd final : qmcg_crowd_s
     if (rc)
       return rc;
     recompute_every = p->recompute_every;
-    CUDA_TRY(cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned long long), stream));
+    CUDA_TRY(cudaMemsetAsync(s.counters, 0, 3 * sizeof(unsigned long long), stream));
     const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
     std::vector<int> accbuf;
     for (int it = 0; it < n; it++)
@@ -888,6 +909,7 @@ struct Crowd final : qmcg_crowd_s
     for (int sp = 0; sp < 2; sp++)
       if (k > 1 && d[sp] > 0)
         CUDA_TRY(launch_flush_simt<T>(s, sp, d[sp], W, stream));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
     CUDA_TRY(cudaStreamSynchronize(stream));
     return QMCG_OK;
@@ -909,6 +931,96 @@ struct Crowd final : qmcg_crowd_s
         sweeps_since_recompute = 0;
       }
     }
+    return QMCG_OK;
+  }
+
+  // Device time of the walker-resident path over n real sweeps, split by kernel:
+  // out[0] = ms per sweep-kernel launch, out[1] = ms per flush launch,
+  // out[2] = sweep-kernel launches per sweep, out[3] = flush launches per sweep.
+  // CUDA events on the crowd's stream around every launch; the repair and counter
+  // kernels run between sweeps untimed.
+  int profile_sweep(int n, double* out) override
+  {
+    if (n <= 0 || !out)
+      return fail(QMCG_ERR_ARG, "bad profile arguments");
+    if (!graph || graph_path != 0)
+      return fail(QMCG_ERR_STATE, "no walker-resident sweep graph built yet");
+    struct Rec
+    {
+      cudaEvent_t a, b;
+      int flush;
+    };
+    std::vector<Rec> recs;
+    auto timed = [&](int is_flush, auto&& launch) -> int {
+      Rec r{nullptr, nullptr, is_flush};
+      CUDA_TRY(cudaEventCreate(&r.a));
+      CUDA_TRY(cudaEventCreate(&r.b));
+      CUDA_TRY(cudaEventRecord(r.a, stream));
+      CUDA_TRY(launch());
+      CUDA_TRY(cudaEventRecord(r.b, stream));
+      recs.push_back(r);
+      return QMCG_OK;
+    };
+    int nsk = 0, nfl = 0;
+    for (int it = 0; it < n; it++)
+    {
+      if (k > 1)
+      {
+        for (int g = 0; g < 2; g++)
+        {
+          const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
+          for (int i0 = first; i0 < last; i0 += k)
+          {
+            const int i1 = std::min(i0 + k, last);
+            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, W, sweep_grid_size, i0, i1, 0, stream); });
+            if (rc)
+              return rc;
+            rc = timed(1, [&] { return launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream); });
+            if (rc)
+              return rc;
+            if (it == 0)
+            {
+              nsk++;
+              nfl++;
+            }
+          }
+        }
+      }
+      else
+      {
+        int rc = timed(0, [&] { return launch_sweep<T>(s, W, sweep_grid_size, stream); });
+        if (rc)
+          return rc;
+        if (it == 0)
+          nsk++;
+      }
+      CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
+      bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    double ts = 0, tf = 0;
+    int cs = 0, cf = 0;
+    for (auto& r : recs)
+    {
+      float t = 0;
+      CUDA_TRY(cudaEventElapsedTime(&t, r.a, r.b));
+      if (r.flush)
+      {
+        tf += t;
+        cf++;
+      }
+      else
+      {
+        ts += t;
+        cs++;
+      }
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    out[0] = cs ? ts / cs : 0.0;
+    out[1] = cf ? tf / cf : 0.0;
+    out[2] = nsk;
+    out[3] = nfl;
     return QMCG_OK;
   }
 
@@ -949,7 +1061,7 @@ struct Crowd final : qmcg_crowd_s
 
   int sync(qmcg_sweep_stats* st) override
   {
-    unsigned long long c[2];
+    unsigned long long c[3];
     std::vector<int> stv(nw);
     CUDA_TRY(cudaMemcpyAsync(c, s.counters, sizeof(c), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaMemcpyAsync(stv.data(), s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -962,6 +1074,7 @@ struct Crowd final : qmcg_crowd_s
     {
       st->accepted = c[0];
       st->rejected = c[1];
+      st->repaired = c[2];
       st->status   = any;
     }
     if (any & ST_SINGULAR)
@@ -1065,6 +1178,7 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
 extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }
 extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
+extern "C" int qmcg_profile_sweep(qmcg_crowd c, int n, double* ms) { CROWD_CALL(c, profile_sweep(n, ms)); }
 
 // ---------------------------------------------------------------------------
 // determinant-engine flush on caller device buffers

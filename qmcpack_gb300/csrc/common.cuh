@@ -22,6 +22,22 @@ enum : int
   ST_ZERO_RATIO  = 1,  // accepted move with a zero determinant ratio
   ST_NONFINITE   = 2,  // NaN/Inf ratio or gradient
   ST_SINGULAR    = 4,  // exact zero pivot in the FP64 inverse
+  ST_ILLCOND     = 8,  // the tracked inverse lost accuracy: |Ainv[row] . phi(r_row) - 1| above tolerance
+  ST_REPAIR_MASK = ST_NONFINITE | ST_ILLCOND,
+};
+
+// tolerance of the self-ratio health check |Ainv[row] . phi(r_row) - 1|
+template<typename T>
+struct HealthTol;
+template<>
+struct HealthTol<float>
+{
+  static constexpr float v = 1e-3f;
+};
+template<>
+struct HealthTol<double>
+{
+  static constexpr double v = 1e-7;
 };
 
 template<typename T>
@@ -49,6 +65,7 @@ struct DevState
   T* Ainv;
   T* dgrad;
   T* dlap;
+  T* psiv;   // [2][nw][N][lda] orbital values of the current electron positions
   T* U;
   T* V;
   T* Binv;
@@ -73,7 +90,7 @@ struct DevState
   int* flag;          // [nw]  valid && p >= eps (a uniform is consumed)
   int* accepted;      // [nw]
   int* status;        // [nw]
-  unsigned long long* counters; // [0] accepted, [1] rejected
+  unsigned long long* counters; // [0] accepted, [1] rejected, [2] walkers repaired by an FP64 recompute
   // ---------------- random numbers
   const double* gauss;   // stream mode: [ne][nw][3] unit Gaussians of the current sweep
   const double* uniform; // stream mode: uniforms, consumed in walker order

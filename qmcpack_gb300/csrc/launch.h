@@ -36,8 +36,39 @@ template<typename T>
 cudaError_t sweep_grid(const DevState<T>& s, int* grid);
 template<typename T>
 cudaError_t launch_sweep(const DevState<T>& s, T* W, int grid, cudaStream_t st);
+template<typename T>
+cudaError_t launch_sweep_segment(const DevState<T>& s, T* W, int grid, int i0, int i1, int dc0, cudaStream_t st);
+// batched, shared-memory-staged flush of one spin for all walkers (flush_kernels.cu);
+// falls back to the two-kernel SIMT flush when the tiles do not fit
+template<typename T>
+cudaError_t launch_flush_fused(const FlushArgs<T>& f, cudaStream_t st);
+template<typename T>
+cudaError_t setup_flush_fused();
+
+// flush arguments of one spin of a crowd
+template<typename T>
+inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* W)
+{
+  FlushArgs<T> f;
+  f.nw         = s.nw;
+  f.n          = s.norb;
+  f.lda        = s.lda;
+  f.k          = s.k;
+  f.dc         = dc;
+  f.sA         = (long long)s.norb * s.lda;
+  f.sU         = (long long)s.k * s.lda;
+  f.sB         = (long long)s.k * s.k;
+  f.sD         = s.k;
+  f.ainv       = s.Ainv + (size_t)spin * s.nw * f.sA;
+  f.u          = s.U + (size_t)spin * s.nw * f.sU;
+  f.v          = s.V + (size_t)spin * s.nw * f.sU;
+  f.binv       = s.Binv + (size_t)spin * s.nw * f.sB;
+  f.delay_list = s.delay_list + (size_t)spin * s.nw * f.sD;
+  f.w          = W;
+  return f;
+}
 
 // recompute path (recompute_kernels.cu)
 template<typename T>
-cudaError_t launch_recompute(const DevState<T>& s, double* mscratch, cudaStream_t st);
+cudaError_t launch_recompute(const DevState<T>& s, double* mscratch, int masked, cudaStream_t st);
 } // namespace qmcg

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(NT) propose_kernel(DevState<T> s, int iat, int
   T* arow   = reinterpret_cast<T*>(smem_raw);  // lda
   T* pvec   = arow + s.lda;                    // k
   T* tvec   = pvec + s.k;                      // k
-  __shared__ T red[3 * 32];
+  __shared__ T red[4 * 32];
   const int iw   = blockIdx.x;
   const int spin = iat >= s.nup ? 1 : 0;
   const int row  = iat - (spin ? s.nup : 0);
@@ -91,19 +91,23 @@ __global__ void __launch_bounds__(NT) propose_kernel(DevState<T> s, int iat, int
         invRow[j] = arow[j];
     }
   }
-  // gradient of the determinant part: invRow . dgrad[row]
+  // gradient of the determinant part: invRow . dgrad[row]; self ratio invRow . psiv[row] (= 1)
   const T* dg = s.dgrad + ((wslot * n + row) * 3) * s.lda;
-  T g[3]      = {0, 0, 0};
+  const T* pv0 = s.psiv + (wslot * n + row) * s.lda;
+  T g[4]      = {0, 0, 0, 0};
   for (int j = threadIdx.x; j < n; j += blockDim.x)
   {
     const T x = inv[j];
     g[0] += x * dg[j];
     g[1] += x * dg[s.lda + j];
     g[2] += x * dg[2 * s.lda + j];
+    g[3] += x * pv0[j];
   }
-  block_sum<T, 3>(g, red);
+  block_sum<T, 4>(g, red);
   if (threadIdx.x == 0)
   {
+    if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
+      atomicOr(s.status + iw, ST_ILLCOND);
     double gn[3];
     for (int d = 0; d < 3; d++)
     {
@@ -303,7 +307,7 @@ __global__ void __launch_bounds__(NT) ratio_kernel(DevState<T> s, int iat, int d
     s.ratios[iw] = ratio;
     for (int d = 0; d < 3; d++)
       s.grads_new[iw * 3 + d] = g[d];
-    if (!isfinite(ratio) || !isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))
+    if (!isfinite(ratio) || (ratio != 0.0 && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
       atomicOr(s.status + iw, ST_NONFINITE);
     if (driver)
     {
@@ -484,8 +488,10 @@ __global__ void __launch_bounds__(NT) accept_kernel(DevState<T> s, int iat, int 
   {
     T* dg = s.dgrad + ((wslot * n + row) * 3) * s.lda;
     T* dl = s.dlap + (wslot * n + row) * s.lda;
+    T* pv0 = s.psiv + (wslot * n + row) * s.lda;
     for (int j = threadIdx.x; j < n; j += blockDim.x)
     {
+      pv0[j]            = phi[j];
       dg[j]             = phi[1 * s.lda + j];
       dg[s.lda + j]     = phi[2 * s.lda + j];
       dg[2 * s.lda + j] = phi[3 * s.lda + j];

@@ -16,15 +16,31 @@
 namespace qmcg
 {
 
-// grid (nw * ne): orbital VGL of electron e of walker iw into the FP64 Slater
-// matrix (stored transposed: Mt[slot][o][row]) and the dgrad / dlap rows.
+// A walker takes part in a masked (repair) recompute only if its status has a
+// repair bit; an unmasked recompute takes every walker.
+template<typename T>
+__device__ __forceinline__ bool skip_walker(const DevState<T>& s, int iw, int masked)
+{
+  return masked && !(s.status[iw] & ST_REPAIR_MASK);
+}
+
+constexpr int VGL_EPB = 8; // electrons per CTA of the all-electron VGL
+
+// grid (nw * ceil(ne / VGL_EPB)): orbital VGL of VGL_EPB electrons of walker iw into
+// the FP64 Slater matrix (stored transposed: Mt[slot][o][row]) and the psiv / dgrad /
+// dlap rows.
 template<typename T, int NT>
-__global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt)
+__global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt, int masked)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* part      = reinterpret_cast<T*>(smem_raw);
-  const int iw = blockIdx.x / s.ne;
-  const int e  = blockIdx.x % s.ne;
+  T* part        = reinterpret_cast<T*>(smem_raw);
+  const int nblk = (s.ne + VGL_EPB - 1) / VGL_EPB;
+  const int iw   = blockIdx.x / nblk;
+  if (skip_walker(s, iw, masked))
+    return;
+  const int e0 = (blockIdx.x % nblk) * VGL_EPB;
+  for (int e = e0; e < min(e0 + VGL_EPB, s.ne); e++)
+  {
   const int spin = e >= s.nup ? 1 : 0;
   const int row  = e - (spin ? s.nup : 0);
   const int n    = s.norb;
@@ -37,23 +53,29 @@ __global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt)
   double* M = Mt + slot * (size_t)n * n;
   T* dg     = s.dgrad + ((slot * n + row) * 3) * s.lda;
   T* dl     = s.dlap + (slot * n + row) * s.lda;
+  T* pv     = s.psiv + (slot * n + row) * s.lda;
   for (int o = threadIdx.x; o < n; o += blockDim.x)
   {
     T vgl[5];
     spline_combine(s, part, o, vgl);
     M[(size_t)o * n + row] = static_cast<double>(vgl[0]);
+    pv[o]                  = vgl[0];
     dg[o]                  = vgl[1];
     dg[s.lda + o]          = vgl[2];
     dg[2 * s.lda + o]      = vgl[3];
     dl[o]                  = vgl[4];
+  }
+  __syncthreads();
   }
 }
 
 // grid (2 * nw): in-place FP64 Gauss-Jordan inverse of Mt[slot] (n x n), log|det|
 // and sign; writes Ainv = Mt^-1 = (M^-1)^T in the move-loop precision.
 template<typename T, int NT>
-__global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* Mt)
+__global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* Mt, int masked)
 {
+  if (skip_walker(s, blockIdx.x % s.nw, masked))
+    return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = s.norb;
   double* prow = reinterpret_cast<double*>(smem_raw); // n
@@ -200,11 +222,11 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
 // grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
 // Vat, Grad, Lap over the ions.
 template<typename T, int NT>
-__global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s)
+__global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int masked)
 {
   const int iw = blockIdx.x;
   const int i  = blockIdx.y * NT + threadIdx.x;
-  if (i >= s.ne)
+  if (i >= s.ne || skip_walker(s, iw, masked))
     return;
   const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
   const T xi = Rx[i], yi = Rx[s.ne_pad + i], zi = Rx[2 * s.ne_pad + i];
@@ -269,23 +291,43 @@ __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s)
   }
 }
 
+// after a masked recompute: count and clear the repaired walkers' repair bits
 template<typename T>
-cudaError_t launch_recompute(const DevState<T>& s, double* Mt, cudaStream_t st)
+__global__ void finish_repair_kernel(DevState<T> s)
+{
+  const int iw = blockIdx.x * blockDim.x + threadIdx.x;
+  if (iw >= s.nw)
+    return;
+  const int st = s.status[iw];
+  if (st & ST_REPAIR_MASK)
+  {
+    s.status[iw] = st & ~ST_REPAIR_MASK;
+    atomicAdd(s.counters + 2, 1ull);
+  }
+}
+
+template<typename T>
+cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaStream_t st)
 {
   constexpr int NT = 128;
   const size_t sm  = sizeof(T) * 4 * 7 * (size_t)s.lda;
-  vgl_all_kernel<T, NT><<<s.nw * s.ne, NT, sm, st>>>(s, Mt);
+  const int nblk   = (s.ne + VGL_EPB - 1) / VGL_EPB;
+  vgl_all_kernel<T, NT><<<s.nw * nblk, NT, sm, st>>>(s, Mt, masked);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
-  constexpr int NTG = 256;
+  constexpr int NTG = 512;
   const size_t smg  = (size_t)s.norb * (2 * sizeof(double) + sizeof(int));
-  gj_inverse_kernel<T, NTG><<<2 * s.nw, NTG, smg, st>>>(s, Mt);
+  gj_inverse_kernel<T, NTG><<<2 * s.nw, NTG, smg, st>>>(s, Mt, masked);
   e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
   dim3 grid(s.nw, (s.ne + 127) / 128);
-  jastrow_full_kernel<T, 128><<<grid, 128, 0, st>>>(s);
+  jastrow_full_kernel<T, 128><<<grid, 128, 0, st>>>(s, masked);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !masked)
+    return e;
+  finish_repair_kernel<T><<<(s.nw + 127) / 128, 128, 0, st>>>(s);
   return cudaGetLastError();
 }
 
@@ -296,7 +338,7 @@ cudaError_t setup_recompute_kernels()
 }
 template cudaError_t setup_recompute_kernels<float>();
 template cudaError_t setup_recompute_kernels<double>();
-template cudaError_t launch_recompute<float>(const DevState<float>&, double*, cudaStream_t);
-template cudaError_t launch_recompute<double>(const DevState<double>&, double*, cudaStream_t);
+template cudaError_t launch_recompute<float>(const DevState<float>&, double*, int, cudaStream_t);
+template cudaError_t launch_recompute<double>(const DevState<double>&, double*, int, cudaStream_t);
 
 } // namespace qmcg

@@ -87,7 +87,7 @@ __device__ void flush_walker(const DevState<T>& s, int w, int spin, int dc, T* W
 }
 
 template<typename T, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
+__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf, int i0, int i1, int dc0, int inline_flush)
 {
   constexpr int RB = 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -126,12 +126,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
     for (int e = threadIdx.x; e < 5 * s.ne_pad; e += NT)
       J2s[e] = s.J2[(size_t)w * 5 * s.ne_pad + e];
     __syncthreads();
-    int dc = 0;
-    for (int iat = 0; iat < s.ne; iat++)
+    int dc = dc0;
+    for (int iat = i0; iat < i1; iat++)
     {
       const int spin = iat >= s.nup ? 1 : 0;
       const int row  = iat - (spin ? s.nup : 0);
-      if (iat == s.nup && s.k > 1 && dc > 0)
+      if (inline_flush && iat == s.nup && s.k > 1 && dc > 0)
       {
         // the up-spin delays are complete: flush them now (same result as at the sweep end)
         flush_walker<T, NT, RB>(s, w, 0, dc, Wg, rows, t1);
@@ -180,18 +180,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
         inv = invrow;
       }
       {
-        const T* dg = s.dgrad + ((slot * n + row) * 3) * s.lda;
-        T g[3]      = {0, 0, 0};
+        const T* dg  = s.dgrad + ((slot * n + row) * 3) * s.lda;
+        const T* pv0 = s.psiv + (slot * n + row) * s.lda;
+        T g[4]       = {0, 0, 0, 0};
         for (int j = threadIdx.x; j < n; j += NT)
         {
           const T x = inv[j];
           g[0] += x * dg[j];
           g[1] += x * dg[s.lda + j];
           g[2] += x * dg[2 * s.lda + j];
+          g[3] += x * pv0[j];
         }
-        block_sum<T, 3>(g, red);
+        block_sum<T, 4>(g, red);
         if (threadIdx.x == 0)
         {
+          if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
+            atomicOr(s.status + w, ST_ILLCOND);
           double gn[3];
           for (int d = 0; d < 3; d++)
           {
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
           g[1] += static_cast<double>(acc[7]);
           g[2] += static_cast<double>(acc[8]);
         }
-        if (!isfinite(ratio) || !isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))
+        if (!isfinite(ratio) || (ratio != 0.0 && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
           atomicOr(s.status + w, ST_NONFINITE);
         const double p = ratio * ratio;
         double log_gb  = 0.0;
@@ -451,10 +455,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
       }
       if (accd)
       {
-        T* dg = s.dgrad + ((slot * n + row) * 3) * s.lda;
-        T* dl = s.dlap + (slot * n + row) * s.lda;
+        T* dg  = s.dgrad + ((slot * n + row) * 3) * s.lda;
+        T* dl  = s.dlap + (slot * n + row) * s.lda;
+        T* pv0 = s.psiv + (slot * n + row) * s.lda;
         for (int j = threadIdx.x; j < n; j += NT)
         {
+          pv0[j]            = phi[j];
           dg[j]             = phi[1 * s.lda + j];
           dg[s.lda + j]     = phi[2 * s.lda + j];
           dg[2 * s.lda + j] = phi[3 * s.lda + j];
@@ -514,14 +520,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf)
       if (s.k > 1)
       {
         dc++;
-        if (dc == s.k)
+        if (inline_flush && dc == s.k)
         {
           flush_walker<T, NT, RB>(s, w, spin, dc, Wg, rows, t1);
           dc = 0;
         }
       }
     }
-    if (s.k > 1 && dc > 0)
+    if (inline_flush && s.k > 1 && dc > 0 && i1 == s.ne)
       flush_walker<T, NT, RB>(s, w, 1, dc, Wg, rows, t1);
     for (int e = threadIdx.x; e < 3 * s.ne_pad; e += NT)
       s.Rt[(size_t)w * 3 * s.ne_pad + e] = Rs[e];
@@ -551,7 +557,16 @@ size_t sweep_smem_bytes(const DevState<T>& s)
 template<typename T>
 cudaError_t launch_sweep(const DevState<T>& s, T* W, int grid, cudaStream_t st)
 {
-  sweep_kernel<T, 128, 4><<<grid, 128, sweep_smem_bytes(s), st>>>(s, W);
+  sweep_kernel<T, 128, 4><<<grid, 128, sweep_smem_bytes(s), st>>>(s, W, 0, s.ne, 0, 1);
+  return cudaGetLastError();
+}
+
+// electrons [i0, i1) of every walker starting at delay count dc0; a segment that
+// would fill the delay window is cut by the host so the flush runs batched
+template<typename T>
+cudaError_t launch_sweep_segment(const DevState<T>& s, T* W, int grid, int i0, int i1, int dc0, cudaStream_t st)
+{
+  sweep_kernel<T, 128, 4><<<grid, 128, sweep_smem_bytes(s), st>>>(s, W, i0, i1, dc0, 0);
   return cudaGetLastError();
 }
 
@@ -580,6 +595,9 @@ template size_t sweep_smem_bytes<float>(const DevState<float>&);
 template size_t sweep_smem_bytes<double>(const DevState<double>&);
 template cudaError_t launch_sweep<float>(const DevState<float>&, float*, int, cudaStream_t);
 template cudaError_t launch_sweep<double>(const DevState<double>&, double*, int, cudaStream_t);
+template cudaError_t launch_sweep_segment<float>(const DevState<float>&, float*, int, int, int, int, cudaStream_t);
+template cudaError_t launch_sweep_segment<double>(const DevState<double>&, double*, int, int, int, int,
+                                                  cudaStream_t);
 template cudaError_t sweep_grid<float>(const DevState<float>&, int*);
 template cudaError_t sweep_grid<double>(const DevState<double>&, int*);
 

@@ -3,6 +3,10 @@
 tracked log|psi| and inverses equal a from-scratch FP64 recompute (the reference's
 checkLogAndGL debug check, src/QMCDrivers/QMCDriverNew.cpp:492-560) within the
 FP32 tolerance, runs are deterministic for a seed, and no walker reports a status.
+
+From a uniform (non-equilibrated) start a few walkers sit close to a node where
+the FP32 inverse loses accuracy; the sweep's health check flags them and the
+masked FP64 recompute rebuilds them, so every walker is within tolerance.
 """
 import numpy as np
 import pytest
@@ -26,6 +30,7 @@ def test_fullsize_tracked_state_matches_recompute(c1):
     g.load_walkers(make_walkers(s, 512, seed=21))
     l0, _ = g.mw_evaluateLog()
     acc, rej, _ = g.vmc_sweeps(2, 0.3, 3, rng_mode=1)
+    print("full size: acceptance", acc / (acc + rej), "walkers repaired", g.last_repaired)
     assert 0.05 < acc / (acc + rej) < 0.95
     tracked, sg_t, _ = g.get_log()
     A_t = g.inverse(0)[:8]
