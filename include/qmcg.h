@@ -94,7 +94,7 @@ typedef struct
   uint64_t rejected;
   uint64_t repaired;   /* walkers whose state was rebuilt by an FP64 recompute after a sweep because the
                           tracked inverse failed its health check |Ainv[row] . phi(r_row) - 1| > tol
-                          (1e-3 in FP32, 1e-7 in FP64) or produced a non-finite ratio */
+                          (1e-2 in FP32, 1e-7 in FP64) or produced a non-finite ratio */
   int status;          /* OR of walker status bits since the last call */
 } qmcg_sweep_stats;
 

@@ -776,13 +776,16 @@ struct Crowd final : qmcg_crowd_s
         for (int i0 = first; i0 < last; i0 += k)
         {
           const int i1 = std::min(i0 + k, last);
-          CUDA_TRY(launch_sweep_segment<T>(s, W, sweep_grid_size, i0, i1, 0, stream));
+          CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream));
           CUDA_TRY(launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream));
         }
       }
     }
     else
-      CUDA_TRY(launch_sweep<T>(s, W, sweep_grid_size, stream));
+    {
+      CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, 0, sys->nup, stream));
+      CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, sys->nup, sys->ne, stream));
+    }
     CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
     CUDA_TRY(cudaGetLastError());
@@ -972,7 +975,7 @@ struct Crowd final : qmcg_crowd_s
           for (int i0 = first; i0 < last; i0 += k)
           {
             const int i1 = std::min(i0 + k, last);
-            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, W, sweep_grid_size, i0, i1, 0, stream); });
+            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream); });
             if (rc)
               return rc;
             rc = timed(1, [&] { return launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream); });
@@ -988,11 +991,15 @@ struct Crowd final : qmcg_crowd_s
       }
       else
       {
-        int rc = timed(0, [&] { return launch_sweep<T>(s, W, sweep_grid_size, stream); });
-        if (rc)
-          return rc;
-        if (it == 0)
-          nsk++;
+        for (int g = 0; g < 2; g++)
+        {
+          const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
+          int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, first, last, stream); });
+          if (rc)
+            return rc;
+          if (it == 0)
+            nsk++;
+        }
       }
       CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
       bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);

@@ -32,7 +32,7 @@ struct HealthTol;
 template<>
 struct HealthTol<float>
 {
-  static constexpr float v = 1e-3f;
+  static constexpr float v = 1e-2f;
 };
 template<>
 struct HealthTol<double>
@@ -275,6 +275,34 @@ __device__ __forceinline__ void unr_drift(double tau, const double g[3], double 
   d[0]             = g[0] * sc;
   d[1]             = g[1] * sc;
   d[2]             = g[2] * sc;
+}
+
+// Box-Muller (RandomSeqGenerator.h:33-51) on counter-based uniforms
+template<typename T>
+__device__ __forceinline__ void gaussians(uint32_t w, uint32_t iat, uint32_t sweep, uint32_t k0, uint32_t k1, T out[3])
+{
+  const u4 r0 = philox4x32_10(u4{w, iat, sweep, 0u}, k0, k1);
+  const u4 r1 = philox4x32_10(u4{w, iat, sweep, 1u}, k0, k1);
+  const T one_m = T(1) - Eps<T>::v;
+  const T twopi = T(6.283185307179586476925286766559);
+  const T t1    = sqrt(T(-2) * log(T(1) - one_m * T(u01(r0.x, r0.y))));
+  const T t2    = twopi * T(u01(r0.z, r0.w));
+  const T t3    = sqrt(T(-2) * log(T(1) - one_m * T(u01(r1.x, r1.y))));
+  const T t4    = twopi * T(u01(r1.z, r1.w));
+  out[0]        = t1 * cos(t2);
+  out[1]        = t1 * sin(t2);
+  out[2]        = t3 * cos(t4);
+}
+
+// Umrigar drift (DriftModifierUNR::getDrift, a = 1) in precision T
+template<typename T>
+__device__ __forceinline__ void unr_drift_t(T tau, const T g[3], T d[3])
+{
+  const T vsq = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  const T sc  = vsq < Eps<T>::v ? tau : ((T(-1) + sqrt(T(1) + T(2) * tau * vsq)) / vsq);
+  d[0]        = g[0] * sc;
+  d[1]        = g[1] * sc;
+  d[2]        = g[2] * sc;
 }
 
 } // namespace qmcg

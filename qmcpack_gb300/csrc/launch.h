@@ -35,9 +35,7 @@ size_t sweep_smem_bytes(const DevState<T>& s);
 template<typename T>
 cudaError_t sweep_grid(const DevState<T>& s, int* grid);
 template<typename T>
-cudaError_t launch_sweep(const DevState<T>& s, T* W, int grid, cudaStream_t st);
-template<typename T>
-cudaError_t launch_sweep_segment(const DevState<T>& s, T* W, int grid, int i0, int i1, int dc0, cudaStream_t st);
+cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st);
 // batched, shared-memory-staged flush of one spin for all walkers (flush_kernels.cu);
 // falls back to the two-kernel SIMT flush when the tiles do not fit
 template<typename T>

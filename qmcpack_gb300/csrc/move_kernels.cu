@@ -121,36 +121,39 @@ __global__ void __launch_bounds__(NT) propose_kernel(DevState<T> s, int iat, int
     }
     if (driver)
     {
-      double delta[3];
-      const double sqrttau = sqrt(s.tau);
+      // driver arithmetic in the move-loop precision (RealType of the reference)
+      T gt[3];
+      for (int d = 0; d < 3; d++)
+      {
+        T gs = g[d];
+        if (s.has_j1)
+          gs += s.J1[((size_t)iw * 5 + 1 + d) * s.ne_pad + iat];
+        if (s.has_j2)
+          gs += s.J2[((size_t)iw * 5 + 1 + d) * s.ne_pad + iat];
+        gt[d] = gs;
+      }
+      (void)gn;
+      const T tau = T(s.tau);
+      T delta[3];
       if (s.rng_mode == 0)
       {
         const double* gz = s.gauss + ((size_t)iat * s.nw + iw) * 3;
-        delta[0]         = gz[0];
-        delta[1]         = gz[1];
-        delta[2]         = gz[2];
+        for (int d = 0; d < 3; d++)
+          delta[d] = T(gz[d]);
       }
       else
       {
-        const unsigned long long sw = *s.sweep_counter;
-        const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
-        const u4 r0 = philox4x32_10(u4{(uint32_t)iw, (uint32_t)iat, (uint32_t)sw, 0u}, k0, k1);
-        const u4 r1 = philox4x32_10(u4{(uint32_t)iw, (uint32_t)iat, (uint32_t)sw, 1u}, k0, k1);
-        const double one_m = 1.0 - 2.2204460492503131e-16;
-        const double t1 = sqrt(-2.0 * log(1.0 - one_m * u01(r0.x, r0.y)));
-        const double t2 = 2.0 * 3.14159265358979323846 * u01(r0.z, r0.w);
-        const double t3 = sqrt(-2.0 * log(1.0 - one_m * u01(r1.x, r1.y)));
-        const double t4 = 2.0 * 3.14159265358979323846 * u01(r1.z, r1.w);
-        delta[0]        = t1 * cos(t2);
-        delta[1]        = t1 * sin(t2);
-        delta[2]        = t3 * cos(t4);
+        const uint32_t sw = static_cast<uint32_t>(*s.sweep_counter);
+        gaussians<T>((uint32_t)iw, (uint32_t)iat, sw, static_cast<uint32_t>(s.seed),
+                     static_cast<uint32_t>(s.seed >> 32), delta);
       }
+      const T sqrttau = sqrt(tau);
       for (int d = 0; d < 3; d++)
         delta[d] *= sqrttau;
-      double drift[3];
+      T drift[3];
       if (s.use_drift)
       {
-        unr_drift(s.tau, gn, drift);
+        unr_drift_t(tau, gt, drift);
         for (int d = 0; d < 3; d++)
           drift[d] += delta[d];
       }
@@ -159,11 +162,12 @@ __global__ void __launch_bounds__(NT) propose_kernel(DevState<T> s, int iat, int
           drift[d] = delta[d];
       for (int d = 0; d < 3; d++)
       {
-        s.disp[iw * 3 + d]       = drift[d];
-        s.active_pos[iw * 3 + d] = s.R[((size_t)iw * 3 + d) * s.ne_pad + iat] + drift[d];
+        s.disp[iw * 3 + d]       = static_cast<double>(drift[d]);
+        s.active_pos[iw * 3 + d] = s.R[((size_t)iw * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
       }
-      s.log_gf[iw] = s.use_drift ? -(0.5 / s.tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
-                                 : 0.0;
+      s.log_gf[iw] = s.use_drift
+          ? static_cast<double>(-(T(0.5) / tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2]))
+          : 0.0;
     }
   }
 }
@@ -311,18 +315,36 @@ __global__ void __launch_bounds__(NT) ratio_kernel(DevState<T> s, int iat, int d
       atomicOr(s.status + iw, ST_NONFINITE);
     if (driver)
     {
-      const double p = ratio * ratio;
-      double log_gb  = 0.0;
+      // driver arithmetic in the move-loop precision: |ratio|^2 = det^2 exp(2 log J)
+      T logj = T(0);
+      T gt[3] = {acc[1] / detr, acc[2] / detr, acc[3] / detr};
+      if (s.has_j1)
+      {
+        logj += s.J1[((size_t)iw * 5) * s.ne_pad + iat] - acc[10];
+        gt[0] += acc[11];
+        gt[1] += acc[12];
+        gt[2] += acc[13];
+      }
+      if (s.has_j2)
+      {
+        logj += s.J2[((size_t)iw * 5) * s.ne_pad + iat] - acc[5];
+        gt[0] += acc[6];
+        gt[1] += acc[7];
+        gt[2] += acc[8];
+      }
+      const T tau = T(s.tau);
+      const T p   = detr * detr * exp(T(2) * logj);
+      T log_gb    = T(0);
       if (s.use_drift)
       {
-        double dr[3];
-        unr_drift(s.tau, g, dr);
+        T dr[3];
+        unr_drift_t(tau, gt, dr);
         for (int d = 0; d < 3; d++)
-          dr[d] += s.disp[iw * 3 + d];
-        log_gb = -(0.5 / s.tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+          dr[d] += T(s.disp[iw * 3 + d]);
+        log_gb = -(T(0.5) / tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
       }
-      s.flag[iw] = (p >= static_cast<double>(Eps<T>::v)) ? 1 : 0;
-      s.prob[iw] = p * exp(log_gb - s.log_gf[iw]);
+      s.flag[iw] = (p >= Eps<T>::v) ? 1 : 0;
+      s.prob[iw] = static_cast<double>(p * exp(log_gb - T(s.log_gf[iw])));
     }
   }
 }
@@ -375,17 +397,17 @@ __global__ void __launch_bounds__(NT) accept_kernel(DevState<T> s, int iat, int 
       int acc = 0;
       if (s.flag[iw])
       {
-        double u;
+        T u;
         if (s.rng_mode == 0)
-          u = s.uniform[s.ucursor[iat & 1] + s_before];
+          u = T(s.uniform[s.ucursor[iat & 1] + s_before]);
         else
         {
-          const unsigned long long sw = *s.sweep_counter;
+          const uint32_t sw = static_cast<uint32_t>(*s.sweep_counter);
           const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
-          const u4 r2 = philox4x32_10(u4{(uint32_t)iw, (uint32_t)iat, (uint32_t)sw, 2u}, k0, k1);
-          u           = u01(r2.x, r2.y);
+          const u4 r2 = philox4x32_10(u4{(uint32_t)iw, (uint32_t)iat, sw, 2u}, k0, k1);
+          u           = T(u01(r2.x, r2.y));
         }
-        acc = u < s.prob[iw] ? 1 : 0;
+        acc = u < T(s.prob[iw]) ? 1 : 0;
       }
       s.accepted[iw] = acc;
       if (iw == 0 && s.rng_mode == 0)

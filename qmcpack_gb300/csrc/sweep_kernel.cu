@@ -1,17 +1,23 @@
-// Walker-resident sweep: one CTA owns one walker for a whole VMC sweep.
+// Walker-resident sweep: one CTA owns one walker for a segment of up to k
+// electrons of one spin group (k = delay rank; the whole spin group with rank-1
+// updates).
 //
 // With counter-based random numbers every walker's Markov chain is independent
-// of the others (no cross-walker random-number cursor), so the whole body of
-// VMCBatched::advanceWalkers (src/QMCDrivers/VMC/VMCBatched.cpp:106-177) for one
-// walker runs inside one CTA: for every electron the proposal (mw_evalGrad +
-// drift-diffusion), the evaluation at the proposed position (mw_makeMove +
-// mw_calcRatioGrad), the accept test and the state update
-// (mw_accept_rejectMove), and every k moves the delayed-update flush
-// (DelayedUpdateBatched::mw_updateInvMat, DelayedUpdateBatched.h:675-738).
-// The walker's positions and two-body Jastrow state stay in shared memory for
-// the whole sweep; the inverse, U, V, Binv and the orbital-gradient rows stay in
-// HBM/L2.  The arithmetic is the staged kernels' (same device routines), so the
-// two paths agree to rounding.
+// of the others, so the body of VMCBatched::advanceWalkers
+// (src/QMCDrivers/VMC/VMCBatched.cpp:106-177) for one walker runs inside one CTA:
+// for every electron the proposal (mw_evalGrad + drift-diffusion), the evaluation
+// at the proposed position (mw_makeMove + mw_calcRatioGrad), the accept test and
+// the state update (mw_accept_rejectMove).  Segments end where the delayed
+// update fills its window (DelayedUpdateBatched::mw_updateInvMat,
+// DelayedUpdateBatched.h:675-738); that flush runs batched over all walkers in
+// flush_kernels.cu.
+//
+// Per CTA the walker's positions, two-body Jastrow state and the delayed-update
+// matrix Binv stay in shared memory for the segment; the next electron's inverse
+// row, orbital-gradient rows and orbital values are prefetched with cp.async
+// while the current electron is evaluated.  Driver arithmetic (Box-Muller
+// Gaussians, drift, Green's functions) runs in the move-loop precision, as the
+// reference's mixed-precision build does in RealType.
 #include <algorithm>
 
 #include "common.cuh"
@@ -22,139 +28,117 @@ namespace qmcg
 {
 
 template<typename T>
-struct SweepSmem
+struct SweepCfg
 {
-  // sizes in elements of T
-  static size_t bytes(const DevState<T>& s, int rb)
-  {
-    const size_t part  = (size_t)28 * s.lda;
-    const size_t flush = (size_t)rb * s.lda + (size_t)rb * s.k;
-    return sizeof(T) * (std::max(part, flush) + 7 * (size_t)s.lda + 8 * (size_t)s.ne_pad + 3 * (size_t)s.k + 16 * 32);
-  }
+  static constexpr int NT   = 128;
+  static constexpr int MINB = sizeof(T) == 4 ? 4 : 2;
 };
 
-// Ainv -= (Ainv U^T - E)(Binv V) for one walker and spin, by the whole CTA.
-template<typename T, int NT, int RB>
-__device__ void flush_walker(const DevState<T>& s, int w, int spin, int dc, T* W, T* rows, T* t1)
+template<typename T>
+static size_t sweep_smem_elems(const DevState<T>& s)
 {
-  const size_t slot = (size_t)spin * s.nw + w;
-  const int n       = s.norb;
-  T* A              = s.Ainv + slot * n * s.lda;
-  const T* U        = s.U + slot * s.k * s.lda;
-  const T* V        = s.V + slot * s.k * s.lda;
-  const T* Binv     = s.Binv + slot * s.k * s.k;
-  const int* dlist  = s.delay_list + slot * s.k;
-  for (int e = threadIdx.x; e < dc * n; e += NT)
+  return (size_t)28 * s.lda    // spline partials
+      + (size_t)10 * s.lda     // prefetch double buffer (inverse row, dgrad xyz, orbital values)
+      + 2 * (size_t)s.lda      // up-to-date inverse row, spare row (keeps 16-byte alignment)
+      + 5 * (size_t)s.lda      // orbital VGL at the proposed position
+      + 8 * (size_t)s.ne_pad   // positions, J2 state
+      + (size_t)s.k * s.k      // Binv
+      + 3 * (size_t)s.k        // p, t, y
+      + 16 * 32;               // block reductions
+}
+
+// cp.async of n_elems elements (a multiple of 16 bytes) from global to shared
+template<typename T>
+__device__ __forceinline__ void async_copy(T* dst, const T* src, int n_elems, int tid, int nt)
+{
+  const int chunks = n_elems * (int)sizeof(T) / 16;
+  for (int c = tid; c < chunks; c += nt)
   {
-    const int l = e / n, i = e % n;
-    T a         = 0;
-    for (int c = 0; c < dc; c++)
-      a += Binv[(size_t)l * s.k + c] * V[(size_t)c * s.lda + i];
-    W[(size_t)l * s.lda + i] = a;
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(reinterpret_cast<char*>(dst) + 16 * c));
+    const char* ga    = reinterpret_cast<const char*>(src) + 16 * c;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(ga) : "memory");
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int r0 = 0; r0 < n; r0 += RB)
-  {
-    const int nr = min(RB, n - r0);
-    for (int e = threadIdx.x; e < nr * n; e += NT)
-    {
-      const int r = e / n, i = e % n;
-      rows[r * s.lda + i] = A[(size_t)(r0 + r) * s.lda + i];
-    }
-    __syncthreads();
-    for (int e = wid; e < nr * dc; e += NT / 32)
-    {
-      const int r = e / dc, c = e % dc;
-      T a         = 0;
-      for (int i = lane; i < n; i += 32)
-        a += rows[r * s.lda + i] * U[(size_t)c * s.lda + i];
-      a = warp_sum(a);
-      if (lane == 0)
-        t1[r * s.k + c] = (dlist[c] == r0 + r) ? a - T(1) : a;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nr * n; e += NT)
-    {
-      const int r = e / n, i = e % n;
-      T a         = 0;
-      for (int c = 0; c < dc; c++)
-        a += t1[r * s.k + c] * W[(size_t)c * s.lda + i];
-      A[(size_t)(r0 + r) * s.lda + i] = rows[r * s.lda + i] - a;
-    }
-    __syncthreads();
-  }
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// rows of electron `row` of spin slot into pre[5][lda]: inverse row, dgrad xyz, orbital values
+template<typename T>
+__device__ __forceinline__ void prefetch_rows(const DevState<T>& s, size_t slot, int row, T* pre, int tid, int nt)
+{
+  const int n = s.norb;
+  async_copy(pre, s.Ainv + (slot * n + row) * s.lda, s.lda, tid, nt);
+  async_copy(pre + s.lda, s.dgrad + ((slot * n + row) * 3) * s.lda, 3 * s.lda, tid, nt);
+  async_copy(pre + 4 * s.lda, s.psiv + (slot * n + row) * s.lda, s.lda, tid, nt);
+  async_commit();
 }
 
 template<typename T, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf, int i0, int i1, int dc0, int inline_flush)
+__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
 {
-  constexpr int RB = 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* part   = reinterpret_cast<T*>(smem_raw);
-  const size_t big = std::max((size_t)28 * s.lda, (size_t)RB * s.lda + (size_t)RB * s.k);
-  T* arow   = part + big;
-  T* invrow = arow + s.lda;
-  T* phi    = invrow + s.lda; // 5 x lda
-  T* Rs     = phi + 5 * s.lda; // 3 x ne_pad
-  T* J2s    = Rs + 3 * s.ne_pad; // 5 x ne_pad
-  T* pv     = J2s + 5 * s.ne_pad; // k
-  T* tv     = pv + s.k;          // k
-  T* yv     = tv + s.k;          // k
-  T* red    = yv + s.k;          // 16 x 32
-  T* rows   = part;
-  T* t1     = part + RB * s.lda;
+  const int lda = s.lda, n = s.norb, K = s.k;
+  T* part   = reinterpret_cast<T*>(smem_raw); // 28 x lda
+  T* pre    = part + 28 * lda;                // 2 x 5 x lda prefetch buffers
+  T* invrow = pre + 10 * lda;                 // lda
+  T* spare  = invrow + lda;                   // lda
+  T* phi    = spare + lda;                    // 5 x lda
+  T* Rs     = phi + 5 * lda;                  // 3 x ne_pad
+  T* J2s    = Rs + 3 * s.ne_pad;              // 5 x ne_pad
+  T* Bs     = J2s + 5 * s.ne_pad;             // K x K
+  T* pv     = Bs + K * K;                     // K
+  T* tv     = pv + K;                         // K
+  T* yv     = tv + K;                         // K
+  T* red    = yv + K;                         // 16 x 32
   __shared__ double s_pos[3];
-  __shared__ double s_disp[3];
-  __shared__ double s_loggf;
+  __shared__ T s_disp[3];
+  __shared__ T s_gauss[3];
+  __shared__ T s_loggf;
   __shared__ int s_acc;
   __shared__ T s_det;
   __shared__ T s_cur[10];
 
-  const unsigned long long sweep = *s.sweep_counter;
+  const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
-  const int n = s.norb;
   unsigned long long n_acc = 0, n_rej = 0;
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
   const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+  const T tau       = T(s.tau);
+  const int spin    = i0 >= s.nup ? 1 : 0;
+  const int first   = spin ? s.nup : 0;
+  const int lane    = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  (void)spare;
 
   for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
   {
-    T* Wg = Wbuf + (size_t)w * s.k * s.lda;
+    const size_t slot = (size_t)spin * s.nw + w;
     for (int e = threadIdx.x; e < 3 * s.ne_pad; e += NT)
       Rs[e] = s.Rt[(size_t)w * 3 * s.ne_pad + e];
     for (int e = threadIdx.x; e < 5 * s.ne_pad; e += NT)
       J2s[e] = s.J2[(size_t)w * 5 * s.ne_pad + e];
-    __syncthreads();
-    int dc = dc0;
+    prefetch_rows(s, slot, i0 - first, pre, threadIdx.x, NT);
+    int dc = 0;
     for (int iat = i0; iat < i1; iat++)
     {
-      const int spin = iat >= s.nup ? 1 : 0;
-      const int row  = iat - (spin ? s.nup : 0);
-      if (inline_flush && iat == s.nup && s.k > 1 && dc > 0)
-      {
-        // the up-spin delays are complete: flush them now (same result as at the sweep end)
-        flush_walker<T, NT, RB>(s, w, 0, dc, Wg, rows, t1);
-        dc = 0;
-      }
-      const size_t slot = (size_t)spin * s.nw + w;
-      const T* A        = s.Ainv + (slot * n + row) * s.lda;
-      // ------------------------------------------------ proposal
-      for (int j = threadIdx.x; j < n; j += NT)
-        arow[j] = A[j];
+      const int row = iat - first;
+      T* arow       = pre + ((iat - i0) & 1) * 5 * lda; // this electron's prefetched rows
+      const T* dg   = arow + lda;
+      const T* pv0  = arow + 4 * lda;
+      if (threadIdx.x == 32)
+        gaussians<T>((uint32_t)w, (uint32_t)iat, sweep, k0, k1, s_gauss);
+      async_wait_all();
       __syncthreads();
+      // ------------------------------------------------ up-to-date inverse row
       const T* inv = arow;
-      if (s.k > 1 && dc > 0)
+      if (K > 1 && dc > 0)
       {
-        const T* U = s.U + slot * s.k * s.lda;
-        const T* V = s.V + slot * s.k * s.lda;
-        T* Binv    = s.Binv + slot * s.k * s.k;
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        const T* U = s.U + slot * K * lda;
+        const T* V = s.V + slot * K * lda;
         for (int c = wid; c < dc; c += NT / 32)
         {
           T a = 0;
           for (int j = lane; j < n; j += 32)
-            a += U[(size_t)c * s.lda + j] * arow[j];
+            a += U[(size_t)c * lda + j] * arow[j];
           a = warp_sum(a);
           if (lane == 0)
             pv[c] = a;
@@ -164,31 +148,33 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
         {
           T a = 0;
           for (int c = 0; c < dc; c++)
-            a += Binv[(size_t)c * s.k + i] * pv[c];
-          tv[i]                      = -a;
-          Binv[(size_t)dc * s.k + i] = -a;
+            a += Bs[c * K + i] * pv[c];
+          tv[i]          = -a;
+          Bs[dc * K + i] = -a;
         }
         __syncthreads();
         for (int j = threadIdx.x; j < n; j += NT)
         {
           T a = 0;
           for (int c = 0; c < dc; c++)
-            a += V[(size_t)c * s.lda + j] * tv[c];
+            a += V[(size_t)c * lda + j] * tv[c];
           invrow[j] = arow[j] + a;
         }
         __syncthreads();
         inv = invrow;
       }
+      // the next electron's rows arrive while this one is evaluated
+      if (iat + 1 < i1)
+        prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
+      // ------------------------------------------------ gradient, health check, proposal
       {
-        const T* dg  = s.dgrad + ((slot * n + row) * 3) * s.lda;
-        const T* pv0 = s.psiv + (slot * n + row) * s.lda;
-        T g[4]       = {0, 0, 0, 0};
+        T g[4] = {0, 0, 0, 0};
         for (int j = threadIdx.x; j < n; j += NT)
         {
           const T x = inv[j];
           g[0] += x * dg[j];
-          g[1] += x * dg[s.lda + j];
-          g[2] += x * dg[2 * s.lda + j];
+          g[1] += x * dg[lda + j];
+          g[2] += x * dg[2 * lda + j];
           g[3] += x * pv0[j];
         }
         block_sum<T, 4>(g, red);
@@ -196,31 +182,23 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
         {
           if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
             atomicOr(s.status + w, ST_ILLCOND);
-          double gn[3];
+          T gn[3];
           for (int d = 0; d < 3; d++)
           {
-            double gs = static_cast<double>(g[d]);
+            T gs = g[d];
             if (s.has_j1)
-              gs += static_cast<double>(s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat]);
+              gs += s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat];
             if (s.has_j2)
-              gs += static_cast<double>(J2s[(1 + d) * s.ne_pad + iat]);
+              gs += J2s[(1 + d) * s.ne_pad + iat];
             gn[d] = gs;
           }
-          const u4 r0 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, (uint32_t)sweep, 0u}, k0, k1);
-          const u4 r1 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, (uint32_t)sweep, 1u}, k0, k1);
-          const double one_m = 1.0 - 2.2204460492503131e-16;
-          const double t1_   = sqrt(-2.0 * log(1.0 - one_m * u01(r0.x, r0.y)));
-          const double t2_   = 2.0 * 3.14159265358979323846 * u01(r0.z, r0.w);
-          const double t3_   = sqrt(-2.0 * log(1.0 - one_m * u01(r1.x, r1.y)));
-          const double t4_   = 2.0 * 3.14159265358979323846 * u01(r1.z, r1.w);
-          double delta[3]    = {t1_ * cos(t2_), t1_ * sin(t2_), t3_ * cos(t4_)};
-          const double sqrttau = sqrt(s.tau);
+          const T sqrttau = sqrt(tau);
+          T delta[3], drift[3];
           for (int d = 0; d < 3; d++)
-            delta[d] *= sqrttau;
-          double drift[3];
+            delta[d] = s_gauss[d] * sqrttau;
           if (s.use_drift)
           {
-            unr_drift(s.tau, gn, drift);
+            unr_drift_t(tau, gn, drift);
             for (int d = 0; d < 3; d++)
               drift[d] += delta[d];
           }
@@ -230,10 +208,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
           for (int d = 0; d < 3; d++)
           {
             s_disp[d] = drift[d];
-            s_pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + drift[d];
+            s_pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
           }
-          s_loggf = s.use_drift ? -(0.5 / s.tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
-                                : 0.0;
+          s_loggf = s.use_drift
+              ? -(T(0.5) / tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
+              : T(0);
         }
         __syncthreads();
       }
@@ -294,7 +273,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
         spline_combine(s, part, o, vgl);
 #pragma unroll
         for (int q = 0; q < 5; q++)
-          phi[q * s.lda + o] = vgl[q];
+          phi[q * lda + o] = vgl[q];
         const T x = inv[o];
         acc[0] += x * vgl[0];
         acc[1] += x * vgl[1];
@@ -305,55 +284,52 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
       if (threadIdx.x == 0)
       {
         const T detr = acc[0];
-        double ratio = static_cast<double>(detr);
-        double g[3]  = {static_cast<double>(acc[1] / detr), static_cast<double>(acc[2] / detr),
-                        static_cast<double>(acc[3] / detr)};
+        T g[3]       = {acc[1] / detr, acc[2] / detr, acc[3] / detr};
+        T logj       = T(0);
         if (s.has_j1)
         {
-          ratio *= exp(static_cast<double>(s.J1[((size_t)w * 5) * s.ne_pad + iat] - acc[10]));
-          g[0] += static_cast<double>(acc[11]);
-          g[1] += static_cast<double>(acc[12]);
-          g[2] += static_cast<double>(acc[13]);
+          logj += s.J1[((size_t)w * 5) * s.ne_pad + iat] - acc[10];
+          g[0] += acc[11];
+          g[1] += acc[12];
+          g[2] += acc[13];
         }
         if (s.has_j2)
         {
-          ratio *= exp(static_cast<double>(J2s[iat] - acc[5]));
-          g[0] += static_cast<double>(acc[6]);
-          g[1] += static_cast<double>(acc[7]);
-          g[2] += static_cast<double>(acc[8]);
+          logj += J2s[iat] - acc[5];
+          g[0] += acc[6];
+          g[1] += acc[7];
+          g[2] += acc[8];
         }
-        if (!isfinite(ratio) || (ratio != 0.0 && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
+        // |ratio|^2 = det^2 exp(2 log J)
+        const T p = detr * detr * exp(T(2) * logj);
+        if (!isfinite(p) || (p != T(0) && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
           atomicOr(s.status + w, ST_NONFINITE);
-        const double p = ratio * ratio;
-        double log_gb  = 0.0;
+        T log_gb = T(0);
         if (s.use_drift)
         {
-          double dr[3];
-          unr_drift(s.tau, g, dr);
+          T dr[3];
+          unr_drift_t(tau, g, dr);
           for (int d = 0; d < 3; d++)
             dr[d] += s_disp[d];
-          log_gb = -(0.5 / s.tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+          log_gb = -(T(0.5) / tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
         }
         int a = 0;
-        if (p >= static_cast<double>(Eps<T>::v))
+        if (p >= Eps<T>::v)
         {
-          const u4 r2    = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, (uint32_t)sweep, 2u}, k0, k1);
-          const double u = u01(r2.x, r2.y);
-          a              = u < p * exp(log_gb - s_loggf) ? 1 : 0;
+          const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
+          a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - s_loggf) ? 1 : 0;
         }
         if (a)
         {
           n_acc++;
-          if (detr == T(0))
-            atomicOr(s.status + w, ST_ZERO_RATIO);
           s.log_abs[slot] += log(fabs(static_cast<double>(detr)));
           if (detr < T(0))
             s.sign[slot] = -s.sign[slot];
         }
         else
           n_rej++;
-        s_acc = a;
-        s_det = detr;
+        s_acc    = a;
+        s_det    = detr;
         s_cur[0] = acc[10];
         s_cur[1] = acc[11];
         s_cur[2] = acc[12];
@@ -368,23 +344,21 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
       __syncthreads();
       // ------------------------------------------------ accept / reject
       const bool accd = s_acc != 0;
-      if (s.k > 1)
+      if (K > 1)
       {
-        T* U       = s.U + slot * s.k * s.lda;
-        T* V       = s.V + slot * s.k * s.lda;
-        T* Binv    = s.Binv + slot * s.k * s.k;
-        int* dlist = s.delay_list + slot * s.k;
+        T* U       = s.U + slot * K * lda;
+        T* V       = s.V + slot * K * lda;
+        int* dlist = s.delay_list + slot * K;
         for (int j = threadIdx.x; j < n; j += NT)
-          V[(size_t)dc * s.lda + j] = arow[j];
+          V[(size_t)dc * lda + j] = arow[j];
         if (accd)
         {
           const T sigma = T(1) / s_det;
-          const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
           for (int c = wid; c < dc; c += NT / 32)
           {
             T a = 0;
             for (int j = lane; j < n; j += 32)
-              a += V[(size_t)c * s.lda + j] * phi[j];
+              a += V[(size_t)c * lda + j] * phi[j];
             a = warp_sum(a);
             if (lane == 0)
               pv[c] = -a;
@@ -394,53 +368,52 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
           {
             T a = 0;
             for (int c = 0; c < dc; c++)
-              a += Binv[(size_t)i * s.k + c] * pv[c];
+              a += Bs[i * K + c] * pv[c];
             yv[i] = sigma * a;
           }
           __syncthreads();
           for (int e = threadIdx.x; e < dc * dc; e += NT)
           {
             const int i = e / dc, j = e % dc;
-            Binv[(size_t)i * s.k + j] += Binv[(size_t)dc * s.k + j] * yv[i];
+            Bs[i * K + j] += Bs[dc * K + j] * yv[i];
           }
           __syncthreads();
           for (int i = threadIdx.x; i < dc; i += NT)
           {
-            Binv[(size_t)i * s.k + dc] = yv[i];
-            Binv[(size_t)dc * s.k + i] *= sigma;
+            Bs[i * K + dc] = yv[i];
+            Bs[dc * K + i] *= sigma;
           }
           if (threadIdx.x == 0)
           {
-            Binv[(size_t)dc * s.k + dc] = sigma;
-            dlist[dc]                   = row;
+            Bs[dc * K + dc] = sigma;
+            dlist[dc]       = row;
           }
           for (int j = threadIdx.x; j < n; j += NT)
-            U[(size_t)dc * s.lda + j] = phi[j];
+            U[(size_t)dc * lda + j] = phi[j];
         }
         else
         {
           for (int j = threadIdx.x; j < n; j += NT)
-            U[(size_t)dc * s.lda + j] = T(0);
+            U[(size_t)dc * lda + j] = T(0);
           for (int i = threadIdx.x; i < dc; i += NT)
-            Binv[(size_t)i * s.k + dc] = T(0);
+            Bs[i * K + dc] = T(0);
           if (threadIdx.x == 0)
           {
-            Binv[(size_t)dc * s.k + dc] = T(1);
-            dlist[dc]                   = -1;
+            Bs[dc * K + dc] = T(1);
+            dlist[dc]       = -1;
           }
         }
       }
       else if (accd)
       {
         // rank-1 Sherman-Morrison on the whole inverse (arow holds the old row)
-        T* Aw = s.Ainv + slot * n * s.lda;
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        T* tmp = part; // n
+        T* Aw  = s.Ainv + slot * n * lda;
+        T* tmp = part;
         for (int j = wid; j < n; j += NT / 32)
         {
           T a = 0;
           for (int i = lane; i < n; i += 32)
-            a += Aw[(size_t)j * s.lda + i] * phi[i];
+            a += Aw[(size_t)j * lda + i] * phi[i];
           a = warp_sum(a);
           if (lane == 0)
             tmp[j] = (j == row) ? a - T(1) : a;
@@ -450,21 +423,29 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
         for (int e = threadIdx.x; e < n * n; e += NT)
         {
           const int j = e / n, i = e % n;
-          Aw[(size_t)j * s.lda + i] += c * arow[i] * tmp[j];
+          Aw[(size_t)j * lda + i] += c * arow[i] * tmp[j];
+        }
+        // the prefetched rows of the next electron predate this update: fetch them again
+        __syncthreads();
+        if (iat + 1 < i1)
+        {
+          async_wait_all();
+          __syncthreads();
+          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
         }
       }
       if (accd)
       {
-        T* dg  = s.dgrad + ((slot * n + row) * 3) * s.lda;
-        T* dl  = s.dlap + (slot * n + row) * s.lda;
-        T* pv0 = s.psiv + (slot * n + row) * s.lda;
+        T* dgo = s.dgrad + ((slot * n + row) * 3) * lda;
+        T* dlo = s.dlap + (slot * n + row) * lda;
+        T* pvo = s.psiv + (slot * n + row) * lda;
         for (int j = threadIdx.x; j < n; j += NT)
         {
-          pv0[j]            = phi[j];
-          dg[j]             = phi[1 * s.lda + j];
-          dg[s.lda + j]     = phi[2 * s.lda + j];
-          dg[2 * s.lda + j] = phi[3 * s.lda + j];
-          dl[j]             = phi[4 * s.lda + j];
+          pvo[j]           = phi[j];
+          dgo[j]           = phi[1 * lda + j];
+          dgo[lda + j]     = phi[2 * lda + j];
+          dgo[2 * lda + j] = phi[3 * lda + j];
+          dlo[j]           = phi[4 * lda + j];
         }
         if (s.has_j2)
         {
@@ -517,18 +498,17 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
         }
       }
       __syncthreads();
-      if (s.k > 1)
-      {
+      if (K > 1)
         dc++;
-        if (inline_flush && dc == s.k)
-        {
-          flush_walker<T, NT, RB>(s, w, spin, dc, Wg, rows, t1);
-          dc = 0;
-        }
-      }
     }
-    if (inline_flush && s.k > 1 && dc > 0 && i1 == s.ne)
-      flush_walker<T, NT, RB>(s, w, 1, dc, Wg, rows, t1);
+    async_wait_all();
+    // hand the segment's Binv to the batched flush, positions and J2 state back to HBM
+    if (K > 1)
+    {
+      T* Binv = s.Binv + slot * K * K;
+      for (int e = threadIdx.x; e < dc * K; e += NT)
+        Binv[e] = Bs[e];
+    }
     for (int e = threadIdx.x; e < 3 * s.ne_pad; e += NT)
       s.Rt[(size_t)w * 3 * s.ne_pad + e] = Rs[e];
     for (int e = threadIdx.x; e < 5 * s.ne_pad; e += NT)
@@ -545,28 +525,25 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, T* Wbuf,
 template<typename T>
 cudaError_t setup_sweep_kernel()
 {
-  return cudaFuncSetAttribute(sweep_kernel<T, 128, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
 }
 
 template<typename T>
 size_t sweep_smem_bytes(const DevState<T>& s)
 {
-  return SweepSmem<T>::bytes(s, 16);
+  return sizeof(T) * sweep_smem_elems(s);
 }
 
+// electrons [i0, i1) of every walker, inside one spin group; with delayed updates
+// i1 - i0 <= k and the host flushes after the launch
 template<typename T>
-cudaError_t launch_sweep(const DevState<T>& s, T* W, int grid, cudaStream_t st)
+cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st)
 {
-  sweep_kernel<T, 128, 4><<<grid, 128, sweep_smem_bytes(s), st>>>(s, W, 0, s.ne, 0, 1);
-  return cudaGetLastError();
-}
-
-// electrons [i0, i1) of every walker starting at delay count dc0; a segment that
-// would fill the delay window is cut by the host so the flush runs batched
-template<typename T>
-cudaError_t launch_sweep_segment(const DevState<T>& s, T* W, int grid, int i0, int i1, int dc0, cudaStream_t st)
-{
-  sweep_kernel<T, 128, 4><<<grid, 128, sweep_smem_bytes(s), st>>>(s, W, i0, i1, dc0, 0);
+  if (i0 < 0 || i1 > s.ne || i1 <= i0 || (i0 < s.nup) != (i1 - 1 < s.nup) || (s.k > 1 && i1 - i0 > s.k))
+    return cudaErrorInvalidValue;
+  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
+  sweep_kernel<T, NT, MINB><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
   return cudaGetLastError();
 }
 
@@ -580,7 +557,8 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid)
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess)
     return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, 128, 4>, 128, sweep_smem_bytes(s));
+  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB>, NT, sweep_smem_bytes(s));
   if (e != cudaSuccess)
     return e;
   if (per_sm < 1)
@@ -593,11 +571,8 @@ template cudaError_t setup_sweep_kernel<float>();
 template cudaError_t setup_sweep_kernel<double>();
 template size_t sweep_smem_bytes<float>(const DevState<float>&);
 template size_t sweep_smem_bytes<double>(const DevState<double>&);
-template cudaError_t launch_sweep<float>(const DevState<float>&, float*, int, cudaStream_t);
-template cudaError_t launch_sweep<double>(const DevState<double>&, double*, int, cudaStream_t);
-template cudaError_t launch_sweep_segment<float>(const DevState<float>&, float*, int, int, int, int, cudaStream_t);
-template cudaError_t launch_sweep_segment<double>(const DevState<double>&, double*, int, int, int, int,
-                                                  cudaStream_t);
+template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t);
+template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t);
 template cudaError_t sweep_grid<float>(const DevState<float>&, int*);
 template cudaError_t sweep_grid<double>(const DevState<double>&, int*);
 
