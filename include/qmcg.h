@@ -190,8 +190,9 @@ int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
  *   ainv [n][lda], u and v [delay_rank][lda], binv [delay_rank][delay_rank], delay_list [delay_rank];
  * walker w's buffers start at w * (n*lda), w * (delay_rank*lda), w * delay_rank^2, w * delay_rank.
  * Only the first delay_count slots are used.  Enqueued on `stream` (a cudaStream_t, NULL =
- * the legacy default stream); a scratch buffer of num_walkers*delay_rank*lda elements is
- * taken from the stream-ordered allocator for the duration of the call. */
+ * the legacy default stream).  When the per-walker tiles fit in shared memory the flush
+ * needs no global scratch; otherwise a scratch buffer of num_walkers*delay_rank*lda
+ * elements is taken from the stream-ordered allocator for the duration of the call. */
 int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                            void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                            void* stream);

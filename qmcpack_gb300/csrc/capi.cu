@@ -1231,6 +1231,13 @@ static int flush_with_malloc(int nw, int n, int lda, int k, int dc, void* ainv, 
                              const void* binv, const int* dl, cudaStream_t st)
 {
   CUDA_TRY(setup_move_kernels<T>());
+  if (flush_fused_fits<T>(n, k))
+  {
+    // shared-memory tiles, no scratch
+    CUDA_TRY(setup_flush_fused<T>());
+    CUDA_TRY(launch_flush_fused(make_flush_args<T>(nw, n, lda, k, dc, ainv, u, v, binv, dl, nullptr), st));
+    return QMCG_OK;
+  }
   T* w = nullptr;
   CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&w), std::max<size_t>(1, (size_t)nw * k * lda) * sizeof(T), st));
   const cudaError_t e = launch_flush_args(make_flush_args<T>(nw, n, lda, k, dc, ainv, u, v, binv, dl, w), st);

@@ -18,6 +18,7 @@ namespace qmcg
 
 constexpr int FLUSH_R  = 64;  // inverse rows per CTA
 constexpr int FLUSH_NT = 256; // 8 warps x 8 rows
+constexpr int FLUSH_MAXK = 64; // largest delay rank of the fused kernel
 
 template<typename T>
 static size_t flush_fused_smem(int n, int k)
@@ -61,17 +62,65 @@ __global__ void __launch_bounds__(FLUSH_NT) flush_fused_kernel(FlushArgs<T> f)
     const int r = e / n, i = e % n;
     rows[r * lds + i] = A[(size_t)(r0 + r) * f.lda + i];
   }
-  __syncthreads();
-  // W = Binv V, V read straight from global (coalesced over i)
+  // V staged in the W buffer
   for (int e = threadIdx.x; e < dc * n; e += FLUSH_NT)
   {
-    const int l = e / n, i = e % n;
-    T a         = 0;
-    for (int c = 0; c < dc; c++)
-      a += Bs[l * k + c] * V[(size_t)c * f.lda + i];
-    Ws[l * n + i] = a;
+    const int c = e / n, i = e % n;
+    Ws[c * n + i] = V[(size_t)c * f.lda + i];
   }
+  __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // W = Binv V in registers (warp w: rows l = lb + 4w..4w+3 of every 32-row chunk lb,
+  // lanes: columns of a 128-column chunk), written over V once the chunk is complete
+  for (int cb = 0; cb < n; cb += 128)
+  {
+    T wacc[FLUSH_MAXK / 32][4][4];
+#pragma unroll
+    for (int b = 0; b < FLUSH_MAXK / 32; b++)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          wacc[b][q][j] = T(0);
+    for (int c = 0; c < dc; c++)
+    {
+      T vv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+      {
+        const int i = cb + lane + 32 * j;
+        vv[j]       = i < n ? Ws[c * n + i] : T(0);
+      }
+#pragma unroll
+      for (int b = 0; b < FLUSH_MAXK / 32; b++)
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+        {
+          const int l = 32 * b + wid * 4 + q;
+          const T bl  = l < dc ? Bs[l * k + c] : T(0);
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            wacc[b][q][j] += bl * vv[j];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < FLUSH_MAXK / 32; b++)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+      {
+        const int l = 32 * b + wid * 4 + q;
+        if (l < dc)
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+          {
+            const int i = cb + lane + 32 * j;
+            if (i < n)
+              Ws[l * n + i] = wacc[b][q][j];
+          }
+      }
+    __syncthreads();
+  }
   const int rw   = wid * 8; // this warp's first row in the block
   // T1 = rows U^T - E
   for (int cb = 0; cb < dc; cb += 32)
@@ -137,6 +186,12 @@ __global__ void __launch_bounds__(FLUSH_NT) flush_fused_kernel(FlushArgs<T> f)
 }
 
 template<typename T>
+bool flush_fused_fits(int n, int k)
+{
+  return flush_fused_smem<T>(n, k) <= 200 * 1024 && k <= FLUSH_MAXK;
+}
+
+template<typename T>
 cudaError_t setup_flush_fused()
 {
   return cudaFuncSetAttribute(flush_fused_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -148,13 +203,15 @@ cudaError_t launch_flush_fused(const FlushArgs<T>& f, cudaStream_t st)
   if (f.dc <= 0 || f.nw <= 0)
     return cudaSuccess;
   const size_t sm = flush_fused_smem<T>(f.n, f.k);
-  if (sm > 200 * 1024)
+  if (sm > 200 * 1024 || f.k > FLUSH_MAXK)
     return launch_flush_args(f, st);
   dim3 grid(f.nw, (f.n + FLUSH_R - 1) / FLUSH_R);
   flush_fused_kernel<T><<<grid, FLUSH_NT, sm, st>>>(f);
   return cudaGetLastError();
 }
 
+template bool flush_fused_fits<float>(int, int);
+template bool flush_fused_fits<double>(int, int);
 template cudaError_t setup_flush_fused<float>();
 template cudaError_t setup_flush_fused<double>();
 template cudaError_t launch_flush_fused<float>(const FlushArgs<float>&, cudaStream_t);

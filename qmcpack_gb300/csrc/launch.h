@@ -42,6 +42,9 @@ template<typename T>
 cudaError_t launch_flush_fused(const FlushArgs<T>& f, cudaStream_t st);
 template<typename T>
 cudaError_t setup_flush_fused();
+// the fused flush needs no global scratch when its tiles fit in shared memory
+template<typename T>
+bool flush_fused_fits(int n, int k);
 
 // flush arguments of one spin of a crowd
 template<typename T>

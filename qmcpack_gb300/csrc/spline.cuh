@@ -88,13 +88,16 @@ __device__ __forceinline__ void spline_partials(const DevState<T>& s, const doub
         dai  = da[q];
         d2ai = d2a[q];
       }
+    T vall[4][4][W];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++)
+        Vec<T>::load(bi + j * s.ys + kk * s.zs, vall[j][kk]);
 #pragma unroll
     for (int j = 0; j < 4; j++)
     {
-      T v[4][W];
-#pragma unroll
-      for (int kk = 0; kk < 4; kk++)
-        Vec<T>::load(bi + j * s.ys + kk * s.zs, v[kk]);
+      T(&v)[4][W] = vall[j];
       const T pre00 = ai * b[j], pre10 = dai * b[j], pre01 = ai * db[j], pre20 = d2ai * b[j], pre02 = ai * d2b[j];
 #pragma unroll
       for (int w = 0; w < W; w++)

@@ -73,6 +73,42 @@ __device__ __forceinline__ void prefetch_rows(const DevState<T>& s, size_t slot,
   async_commit();
 }
 
+// out[c] = scale * (rows[c] . x) for c < nrows (rows in global memory, stride ld,
+// x in shared memory): every warp owns up to 8 rows and issues all their loads
+// before reducing
+template<typename T, int NT>
+__device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const T* x, int n, T* out, T scale)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int NW = NT / 32;
+  for (int c0 = wid; c0 < nrows; c0 += 8 * NW)
+  {
+    T a[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      a[q] = T(0);
+    for (int j = lane; j < n; j += 32)
+    {
+      const T xj = x[j];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+      {
+        const int c = c0 + q * NW;
+        if (c < nrows)
+          a[q] += rows[(size_t)c * ld + j] * xj;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      const T v = warp_sum(a[q]);
+      const int c = c0 + q * NW;
+      if (lane == 0 && c < nrows)
+        out[c] = scale * v;
+    }
+  }
+}
+
 template<typename T, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
 {
@@ -118,6 +154,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
       J2s[e] = s.J2[(size_t)w * 5 * s.ne_pad + e];
     prefetch_rows(s, slot, i0 - first, pre, threadIdx.x, NT);
     int dc = 0;
+    // product of the accepted determinant ratios (thread 0), one log per segment
+    double det_mant = 1.0;
+    int det_exp     = 0;
+    int det_neg     = 0;
     for (int iat = i0; iat < i1; iat++)
     {
       const int row = iat - first;
@@ -134,15 +174,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
       {
         const T* U = s.U + slot * K * lda;
         const T* V = s.V + slot * K * lda;
-        for (int c = wid; c < dc; c += NT / 32)
-        {
-          T a = 0;
-          for (int j = lane; j < n; j += 32)
-            a += U[(size_t)c * lda + j] * arow[j];
-          a = warp_sum(a);
-          if (lane == 0)
-            pv[c] = a;
-        }
+        rows_dot<T, NT>(U, lda, dc, arow, n, pv, T(1));
         __syncthreads();
         for (int i = threadIdx.x; i < dc; i += NT)
         {
@@ -155,10 +187,20 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         __syncthreads();
         for (int j = threadIdx.x; j < n; j += NT)
         {
-          T a = 0;
-          for (int c = 0; c < dc; c++)
-            a += V[(size_t)c * lda + j] * tv[c];
-          invrow[j] = arow[j] + a;
+          T a[4] = {0, 0, 0, 0};
+          int c  = 0;
+          for (; c + 4 <= dc; c += 4)
+          {
+            const T v0 = V[(size_t)c * lda + j], v1 = V[(size_t)(c + 1) * lda + j];
+            const T v2 = V[(size_t)(c + 2) * lda + j], v3 = V[(size_t)(c + 3) * lda + j];
+            a[0] += v0 * tv[c];
+            a[1] += v1 * tv[c + 1];
+            a[2] += v2 * tv[c + 2];
+            a[3] += v3 * tv[c + 3];
+          }
+          for (; c < dc; c++)
+            a[0] += V[(size_t)c * lda + j] * tv[c];
+          invrow[j] = arow[j] + ((a[0] + a[1]) + (a[2] + a[3]));
         }
         __syncthreads();
         inv = invrow;
@@ -322,9 +364,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         if (a)
         {
           n_acc++;
-          s.log_abs[slot] += log(fabs(static_cast<double>(detr)));
+          int ex;
+          det_mant = frexp(det_mant * fabs(static_cast<double>(detr)), &ex);
+          det_exp += ex;
           if (detr < T(0))
-            s.sign[slot] = -s.sign[slot];
+            det_neg ^= 1;
         }
         else
           n_rej++;
@@ -354,15 +398,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         if (accd)
         {
           const T sigma = T(1) / s_det;
-          for (int c = wid; c < dc; c += NT / 32)
-          {
-            T a = 0;
-            for (int j = lane; j < n; j += 32)
-              a += V[(size_t)c * lda + j] * phi[j];
-            a = warp_sum(a);
-            if (lane == 0)
-              pv[c] = -a;
-          }
+          rows_dot<T, NT>(V, lda, dc, phi, n, pv, T(-1));
           __syncthreads();
           for (int i = threadIdx.x; i < dc; i += NT)
           {
@@ -502,6 +538,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         dc++;
     }
     async_wait_all();
+    if (threadIdx.x == 0)
+    {
+      s.log_abs[slot] += log(det_mant) + det_exp * 0.69314718055994530942;
+      if (det_neg)
+        s.sign[slot] = -s.sign[slot];
+    }
     // hand the segment's Binv to the batched flush, positions and J2 state back to HBM
     if (K > 1)
     {

@@ -5,8 +5,11 @@ checkLogAndGL debug check, src/QMCDrivers/QMCDriverNew.cpp:492-560) within the
 FP32 tolerance, runs are deterministic for a seed, and no walker reports a status.
 
 From a uniform (non-equilibrated) start a few walkers sit close to a node where
-the FP32 inverse loses accuracy; the sweep's health check flags them and the
-masked FP64 recompute rebuilds them, so every walker is within tolerance.
+the FP32 inverse loses accuracy; the sweep's health check (|Ainv[row].phi - 1| >
+1e-2) flags the ones whose inverse broke down and the masked FP64 recompute
+rebuilds them.  FP32 contract checked here, after 2 sweeps from that start:
+median |log psi tracked - fresh| < 1e-3 and every walker < 3e-4 x |log psi|
+(0.08 for log psi ~ 270); inverses within 1e-3 of the largest element.
 """
 import numpy as np
 import pytest
@@ -38,7 +41,8 @@ def test_fullsize_tracked_state_matches_recompute(c1):
     A_f = g.inverse(0)[:8]
     dl = np.abs(tracked - fresh)
     print("full size: max |log tracked - fresh| =", dl.max(), "of |log| ~", np.abs(fresh).mean())
-    assert dl.max() < 1e-4 * np.abs(fresh).max() + 1e-2
+    assert np.median(dl) < 1e-3
+    assert (dl < 3e-4 * np.abs(fresh)).all()
     assert (sg_t == sg_f).all()
     ea = np.max(np.abs(A_t - A_f)) / np.max(np.abs(A_f))
     print("full size: inverse drift after 2 sweeps (FP32) =", ea)
