@@ -213,8 +213,8 @@ def run_ours(args, rank: int, world: int):
     recompute_every = spec.recompute_every
     # equilibration from the uniform start (untimed), then warm-up (also captures the sweep graph)
     if args.equil > 0:
-        crowd.vmc_sweeps(args.equil, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
-    crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
+        crowd.vmc_sweeps(args.equil, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
+    crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
     stream = torch.cuda.ExternalStream(crowd.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(dev)
@@ -253,7 +253,7 @@ def run_ours(args, rank: int, world: int):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         crowd.load_walkers(Rnp)
-        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=recompute_every)
+        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
         Rnp[...] = crowd.positions()
         lp, _, _ = crowd.get_log()
     torch.cuda.synchronize()
@@ -295,6 +295,7 @@ def run_ours(args, rank: int, world: int):
         "config": {"workload": f"{args.workload}: {DESCRIPTIONS.get(args.workload, '')}",
                    "step": "one VMC sweep (every electron of every walker moved once), CUDA graph replay",
                    "walkers_per_gpu": nw, "electrons": system.n_elec, "delay_rank": k,
+                   "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32"}[args.flush],
                    "l2": "inputs larger than L2 (spline table 102 MB + inverses/gradients ~0.8 GB per sweep)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": "sweep_kernel (walker-resident; one launch = up to k electrons "
@@ -303,7 +304,9 @@ def run_ours(args, rank: int, world: int):
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                      else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": seg_ms,
                      "algorithmic_bytes_per_launch": algo, "launches_per_sweep": seg_per_sweep,
-                     "flush": {"kernel": "flush_fused_kernel", "ms_per_launch": flush_ms,
+                     "flush": {"kernel": {0: "flush_fused_kernel (SIMT)", 1: "flush_tc_kernel (tcgen05 TF32)",
+                                          3: "flush_tc_kernel (tcgen05 3xTF32)"}[args.flush],
+                               "ms_per_launch": flush_ms,
                                "launches_per_sweep": flush_per_sweep, "algorithmic_bytes_per_launch": flush_bytes,
                                "achieved_gbs": flush_bytes / (flush_ms / 1e3) / 1e9 if flush_ms else None}},
         "cpu_baseline": base,
@@ -329,6 +332,8 @@ def main():
     ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--equil", type=int, default=20, help="untimed equilibration sweeps before the warm-up")
+    ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
+                    help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -86,6 +86,9 @@ typedef struct
   int recompute_every; /* FP64 recompute after every this many sweeps; 0 = never */
   int path;            /* 0: walker-resident sweep kernel when rng_mode is 1 (one CTA owns a walker for a whole
                           sweep), else the staged per-electron kernels; 1: always the staged kernels */
+  int flush;           /* delayed-update flush of the walker-resident path: 0 = SIMT (FP32 or FP64),
+                          1 = tensor cores TF32, 3 = tensor cores 3xTF32 split precision (FP32 move loop,
+                          delay rank <= 32; otherwise the SIMT flush is used) */
 } qmcg_sweep_params;
 
 typedef struct
@@ -196,6 +199,14 @@ int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
 int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                            void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                            void* stream);
+
+/* qmcg_mw_update_inv_mat with a choice of method: 0 = SIMT, 1 = tcgen05 tensor cores
+ * in TF32, 3 = tcgen05 tensor cores in 3xTF32 split precision.  Methods 1 and 3 need
+ * precision 4, delay_rank <= 32 and n, lda multiples of 4; other cases return
+ * QMCG_ERR_ARG.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
+int qmcg_mw_update_inv_mat_ex(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
+                              void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
+                              int method, void* stream);
 
 /* Allocation-free variant of qmcg_mw_update_inv_mat.  It has no counterpart in
  * the reference: QMCPACK's engine always allocates its own scratch.  It exists for

@@ -18,7 +18,8 @@ EXPORTS = [
     "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
-    "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio", "qmcg_profile_sweep",
+    "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_ex", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
+    "qmcg_profile_sweep",
 ]
 
 
@@ -35,7 +36,7 @@ class SystemDesc(C.Structure):
 
 class SweepParams(C.Structure):
     _fields_ = [("tau", C.c_double), ("use_drift", C.c_int), ("rng_mode", C.c_int), ("seed", C.c_uint64),
-                ("recompute_every", C.c_int), ("path", C.c_int)]
+                ("recompute_every", C.c_int), ("path", C.c_int), ("flush", C.c_int)]
 
 
 class SweepStats(C.Structure):
@@ -88,6 +89,8 @@ def load(path: str = LIB_PATH):
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
         "qmcg_profile_sweep": [vp, C.c_int, _dp],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
+        "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
+                                      C.c_int, vp],
         "qmcg_mw_update_inv_mat_noalloc": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                            vp],
     }

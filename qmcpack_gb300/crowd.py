@@ -161,9 +161,9 @@ class Crowd:
 
     # ---- device-resident sweeps
     def vmc_sweeps(self, nsweeps: int, tau: float, seed: int, rng_mode: int = 1, use_drift: bool = True,
-                   recompute_every: int = 0, log_accepts: bool = False, staged: bool = False):
+                   recompute_every: int = 0, log_accepts: bool = False, staged: bool = False, flush: int = 0):
         p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=rng_mode, seed=seed,
-                        recompute_every=recompute_every, path=1 if staged else 0)
+                        recompute_every=recompute_every, path=1 if staged else 0, flush=flush)
         st = SweepStats()
         acc = np.zeros((nsweeps, self.ne, self.nw), np.int32) if log_accepts else None
         check(self.L.qmcg_vmc_sweeps(self.handle, C.byref(p), nsweeps, C.byref(st),

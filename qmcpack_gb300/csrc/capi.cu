@@ -11,6 +11,7 @@
 #include <memory>
 #include <random>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/qmcg.h"
@@ -346,6 +347,9 @@ struct Crowd final : qmcg_crowd_s
   cudaGraphExec_t graph = nullptr;
   int graph_rng_mode = -1, graph_use_drift = -1, graph_path = -1;
   int sweep_grid_size = 0;
+  int flush_kind      = 0;
+  int graph_flush     = -1;
+  int* tc_err         = nullptr;
   double graph_tau = 0;
   uint64_t graph_seed = 0;
   int sweeps_since_recompute = 0;
@@ -437,6 +441,9 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.accepted, (size_t)nw));
     CUDA_TRY(mem.alloc(&d.status, (size_t)nw));
     CUDA_TRY(mem.alloc(&d.counters, 3));
+    CUDA_TRY(mem.alloc(&tc_err, 1));
+    if (std::is_same<T, float>::value)
+      CUDA_TRY(setup_flush_tc());
     CUDA_TRY(mem.alloc(&d.ucursor, 2));
     CUDA_TRY(mem.alloc(&d.sweep_counter, 1));
     CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
@@ -763,6 +770,15 @@ struct Crowd final : qmcg_crowd_s
 
   bool resident(const qmcg_sweep_params* p) const { return p->rng_mode == 1 && p->path == 0; }
 
+  // the flush of one spin after a resident segment: tensor cores when asked for and possible
+  cudaError_t launch_flush_choice(int spin, int dc)
+  {
+    if constexpr (std::is_same<T, float>::value)
+      if ((flush_kind == 1 || flush_kind == 3) && flush_tc_supported(sys->norb, k, sys->lda))
+        return launch_flush_tc(crowd_flush_args<float>(s, spin, dc, W), flush_kind, tc_err, stream);
+    return launch_flush_fused<T>(crowd_flush_args<T>(s, spin, dc, W), stream);
+  }
+
   // one sweep on the walker-resident path: with delayed updates, one resident
   // launch per segment of up to k electrons of one spin group followed by the
   // batched flush of that spin; with rank-1 updates one launch for the sweep
@@ -777,7 +793,7 @@ struct Crowd final : qmcg_crowd_s
         {
           const int i1 = std::min(i0 + k, last);
           CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream));
-          CUDA_TRY(launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream));
+          CUDA_TRY(launch_flush_choice(g, i1 - i0));
         }
       }
     }
@@ -795,7 +811,7 @@ struct Crowd final : qmcg_crowd_s
   int build_graph(const qmcg_sweep_params* p)
   {
     if (graph && graph_rng_mode == p->rng_mode && graph_use_drift == p->use_drift && graph_tau == p->tau &&
-        graph_seed == p->seed && graph_path == (resident(p) ? 0 : 1))
+        graph_seed == p->seed && graph_path == (resident(p) ? 0 : 1) && graph_flush == p->flush)
       return QMCG_OK;
     if (graph)
     {
@@ -806,6 +822,7 @@ struct Crowd final : qmcg_crowd_s
     s.use_drift = p->use_drift;
     s.tau       = p->tau;
     s.seed      = p->seed;
+    flush_kind  = p->flush;
     cudaGraph_t g;
     CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = resident(p) ? enqueue_sweep_resident() : enqueue_sweep();
@@ -823,6 +840,7 @@ struct Crowd final : qmcg_crowd_s
     graph_tau       = p->tau;
     graph_seed      = p->seed;
     graph_path      = resident(p) ? 0 : 1;
+    graph_flush     = p->flush;
     return QMCG_OK;
   }
 
@@ -978,7 +996,7 @@ struct Crowd final : qmcg_crowd_s
             int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream); });
             if (rc)
               return rc;
-            rc = timed(1, [&] { return launch_flush_fused<T>(crowd_flush_args<T>(s, g, i1 - i0, W), stream); });
+            rc = timed(1, [&] { return launch_flush_choice(g, i1 - i0); });
             if (rc)
               return rc;
             if (it == 0)
@@ -1069,6 +1087,8 @@ struct Crowd final : qmcg_crowd_s
   int sync(qmcg_sweep_stats* st) override
   {
     unsigned long long c[3];
+    int tce = 0;
+    CUDA_TRY(cudaMemcpyAsync(&tce, tc_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
     std::vector<int> stv(nw);
     CUDA_TRY(cudaMemcpyAsync(c, s.counters, sizeof(c), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaMemcpyAsync(stv.data(), s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -1083,6 +1103,11 @@ struct Crowd final : qmcg_crowd_s
       st->rejected = c[1];
       st->repaired = c[2];
       st->status   = any;
+    }
+    if (tce)
+    {
+      CUDA_TRY(cudaMemsetAsync(tc_err, 0, sizeof(int), stream));
+      return fail(QMCG_ERR_CUDA, "tensor-core flush: an mbarrier wait timed out");
     }
     if (any & ST_SINGULAR)
       return fail(QMCG_ERR_SINGULAR, "singular Slater matrix");
@@ -1191,6 +1216,9 @@ extern "C" int qmcg_profile_sweep(qmcg_crowd c, int n, double* ms) { CROWD_CALL(
 // determinant-engine flush on caller device buffers
 // (DelayedUpdateBatched::mw_updateInvMat, DelayedUpdateBatched.h:675-738)
 // ---------------------------------------------------------------------------
+extern "C" int qmcg_mw_update_inv_mat(int precision, int nw, int n, int lda, int k, int dc, void* ainv, const void* u,
+                                      const void* v, const void* binv, const int* delay_list, void* stream);
+
 static int check_flush_args(int prec, int nw, int n, int lda, int k, int dc, void* ainv, const void* u,
                             const void* v, const void* binv, const int* dl)
 {
@@ -1243,6 +1271,38 @@ static int flush_with_malloc(int nw, int n, int lda, int k, int dc, void* ainv, 
   const cudaError_t e = launch_flush_args(make_flush_args<T>(nw, n, lda, k, dc, ainv, u, v, binv, dl, w), st);
   CUDA_TRY(cudaFreeAsync(w, st));
   CUDA_TRY(e);
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_mw_update_inv_mat_ex(int precision, int nw, int n, int lda, int k, int dc, void* ainv,
+                                         const void* u, const void* v, const void* binv, const int* delay_list,
+                                         int method, void* stream)
+{
+  if (method == 0)
+    return qmcg_mw_update_inv_mat(precision, nw, n, lda, k, dc, ainv, u, v, binv, delay_list, stream);
+  if (method != 1 && method != 3)
+    return fail(QMCG_ERR_ARG, "method must be 0, 1 or 3");
+  int rc = check_flush_args(precision, nw, n, lda, k, dc, ainv, u, v, binv, delay_list);
+  if (rc)
+    return rc;
+  if (precision != 4 || !flush_tc_supported(n, k, lda))
+    return fail(QMCG_ERR_ARG, "tensor-core flush needs precision 4, delay_rank <= 32, n and lda multiples of 4");
+  if (nw == 0 || dc == 0)
+    return QMCG_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CUDA_TRY(setup_flush_tc());
+  int* err = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&err), sizeof(int), st));
+  CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  const cudaError_t e =
+      launch_flush_tc(make_flush_args<float>(nw, n, lda, k, dc, ainv, u, v, binv, delay_list, nullptr), method, err, st);
+  int herr = 0;
+  CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaFreeAsync(err, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  CUDA_TRY(e);
+  if (herr)
+    return fail(QMCG_ERR_CUDA, "tensor-core flush: an mbarrier wait timed out");
   return QMCG_OK;
 }
 

@@ -1,0 +1,412 @@
+// Delayed-update flush on the 5th-generation tensor cores (tcgen05, kind::tf32):
+//   T1 = Ainv[rows] U^T            (128 x k,   K = n)   -> TMEM columns [0, 32..64)
+//   P  = (T1 - E) W,  W = Binv V   (128 x n,   K = k)   -> TMEM columns [64, 64+n)
+//   Ainv[rows] -= P
+// DelayedUpdateBatched::mw_updateInvMat (DelayedUpdateBatched.h:675-738) for one
+// walker and a block of 128 inverse rows per CTA.  Operands are staged in shared
+// memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core
+// matrix), the MMAs are issued by one thread, accumulate in TMEM and are read
+// back with tcgen05.ld for the epilogue.
+//
+// Split precision (3xTF32): every FP32 operand x is split as hi = rna_tf32(x),
+// lo = x - hi, and each product is accumulated as hi*hi + hi*lo + lo*hi in FP32,
+// which keeps the flush close to FP32 accuracy; with one term (TF32) the products
+// carry the 2^-11 relative error of TF32.
+//
+// Every wait on an mbarrier is bounded; on timeout the CTA records an error in
+// *err, skips its epilogue, frees its TMEM and returns.
+#include <cstdint>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace qmcg
+{
+
+constexpr int TC_M     = 128; // rows per CTA (TMEM lanes)
+constexpr int TC_NT    = 128; // 4 warps: warp w owns TMEM lanes 32w..32w+31
+constexpr int TC_KC    = 64;  // K chunk of the first product
+// TMEM columns allocated: T1 in [0, 32), P in [64, 64 + n_pad); a power of two
+__host__ __device__ constexpr int tc_cols(int npad) { return 64 + npad <= 256 ? 256 : 512; }
+constexpr long long TC_WAIT_LIMIT = 1ll << 26;
+
+// byte offset of element (r, k) of an R x KC tile in the K-major core-matrix layout
+__device__ __forceinline__ uint32_t cm_off(int r, int k, int kc)
+{
+  return (uint32_t)(((r >> 3) * (kc >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major, LBO = 128 B (next core
+// matrix along K), SBO = (kc/4)*128 B (next 8-row group), descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int kc)
+{
+  const uint64_t lbo = 128 >> 4;
+  const uint64_t sbo = (uint64_t)((kc >> 2) * 128) >> 4;
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+// instruction descriptor: kind::tf32, FP32 accumulate, both operands K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n)
+{
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ float tf32_hi(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accum)
+{
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+               "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+               "l"(a), "l"(b), "r"(idesc), "r"(accum)
+               : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+
+// bounded wait on an mbarrier phase; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+  for (long long it = 0; it < TC_WAIT_LIMIT; it++)
+  {
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(done)
+                 : "r"(mbar), "r"(parity)
+                 : "memory");
+    if (done)
+      return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+  uint32_t r[32];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+               "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                 "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                 "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                 "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    v[i] = __uint_as_float(r[i]);
+}
+
+// shared memory plan (bytes), all tiles 1024-byte aligned
+struct TcPlan
+{
+  int n, k1, kc;   // n = orbitals, k1 = delay rank padded to 32, kc = K chunk
+  uint32_t a_hi, a_lo, b_hi, b_lo; // first product: 128 x kc and k1 x kc tiles
+  uint32_t a2_hi, a2_lo, w_hi, w_lo; // second product: 128 x k1 and n_pad x k1 tiles
+  uint32_t v, binv, dl, bar, tslot, total;
+  int npad;        // n padded to 16 (N of the second product)
+};
+
+__host__ __device__ inline TcPlan tc_plan(int n, int k)
+{
+  TcPlan p;
+  p.n     = n;
+  p.k1    = ((k + 31) / 32) * 32;
+  p.kc    = TC_KC;
+  p.npad  = ((n + 15) / 16) * 16;
+  auto al = [](uint32_t x) { return (x + 1023u) & ~1023u; };
+  uint32_t o = 0;
+  p.a_hi  = o; o = al(o + TC_M * p.kc * 4);
+  p.a_lo  = o; o = al(o + TC_M * p.kc * 4);
+  p.b_hi  = o; o = al(o + p.k1 * p.kc * 4);
+  p.b_lo  = o; o = al(o + p.k1 * p.kc * 4);
+  // the second product reuses the first product's region
+  uint32_t o2 = 0;
+  p.a2_hi = o2; o2 = al(o2 + TC_M * p.k1 * 4);
+  p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
+  p.w_hi  = o2; o2 = al(o2 + p.npad * p.k1 * 4);
+  p.w_lo  = o2; o2 = al(o2 + p.npad * p.k1 * 4);
+  o = o > o2 ? o : o2;
+  p.v     = o; o = al(o + k * n * 4);
+  p.binv  = o; o = al(o + k * k * 4);
+  p.dl    = o; o = al(o + k * 4);
+  p.bar   = o; o += 16;
+  p.tslot = o; o += 16;
+  p.total = al(o);
+  return p;
+}
+
+template<int TERMS>
+__global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, int* err)
+{
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const TcPlan P = tc_plan(f.n, f.k);
+  const int n = f.n, k = f.k, dc = f.dc, lda = f.lda;
+  const int iw = blockIdx.x, r0 = blockIdx.y * TC_M;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float* A             = f.ainv + (size_t)iw * f.sA;
+  const float* U       = f.u + (size_t)iw * f.sU;
+  const float* V       = f.v + (size_t)iw * f.sU;
+  const float* Binv    = f.binv + (size_t)iw * f.sB;
+  const int* dlist     = f.delay_list + (size_t)iw * f.sD;
+  float* Vs            = reinterpret_cast<float*>(sm + P.v);
+  float* Bs            = reinterpret_cast<float*>(sm + P.binv);
+  int* dls             = reinterpret_cast<int*>(sm + P.dl);
+  const uint32_t bar   = smem_u32(sm + P.bar);
+  uint32_t* tslot      = reinterpret_cast<uint32_t*>(sm + P.tslot);
+  __shared__ int s_fail;
+
+  if (tid == 0)
+  {
+    s_fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  const int cols = tc_cols(P.npad);
+  if (warp == 0)
+  {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                 "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  for (int e = tid; e < dc * n; e += TC_NT)
+    Vs[e] = V[(size_t)(e / n) * lda + (e % n)];
+  for (int e = tid; e < dc * dc; e += TC_NT)
+    Bs[e] = Binv[(size_t)(e / dc) * k + (e % dc)];
+  for (int e = tid; e < dc; e += TC_NT)
+    dls[e] = dlist[e];
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const uint32_t d1   = tmem;      // columns [0, k1)
+  const uint32_t d2   = tmem + 64; // columns [64, 64 + npad)
+  uint32_t phase      = 0;
+  bool ok             = true;
+
+  // ---------------- T1 = Ainv[rows] U^T, K in chunks of kc
+  const int nchunks = (n + P.kc - 1) / P.kc;
+  for (int ch = 0; ch < nchunks && ok; ch++)
+  {
+    const int k0 = ch * P.kc;
+    // Ainv rows: 128 rows x kc columns, 16-byte groups of 4 columns
+    for (int e = tid; e < TC_M * (P.kc / 4); e += TC_NT)
+    {
+      const int r = e / (P.kc / 4), c4 = (e % (P.kc / 4)) * 4;
+      const int gr = r0 + r, gc = k0 + c4;
+      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gr < n && gc < n)
+        x = *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc);
+      float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+      float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+      const uint32_t off = cm_off(r, c4, P.kc);
+      *reinterpret_cast<float4*>(sm + P.a_hi + off) = h;
+      if (TERMS > 1)
+        *reinterpret_cast<float4*>(sm + P.a_lo + off) = l;
+    }
+    // U rows: k1 rows x kc columns, rows >= dc are zero
+    for (int e = tid; e < P.k1 * (P.kc / 4); e += TC_NT)
+    {
+      const int r = e / (P.kc / 4), c4 = (e % (P.kc / 4)) * 4;
+      const int gc = k0 + c4;
+      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < dc && gc < n)
+        x = *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc);
+      float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+      float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+      const uint32_t off = cm_off(r, c4, P.kc);
+      *reinterpret_cast<float4*>(sm + P.b_hi + off) = h;
+      if (TERMS > 1)
+        *reinterpret_cast<float4*>(sm + P.b_lo + off) = l;
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0)
+    {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t idesc = idesc_tf32(TC_M, P.k1);
+      const uint32_t ah = smem_u32(sm + P.a_hi), al = smem_u32(sm + P.a_lo);
+      const uint32_t bh = smem_u32(sm + P.b_hi), bl = smem_u32(sm + P.b_lo);
+      for (int ks = 0; ks < P.kc / 8; ks++)
+      {
+        const uint32_t adv = ks * 256; // two core matrices along K per k-step of 8
+        const int first    = (ch == 0 && ks == 0);
+        mma_tf32(d1, smem_desc(ah + adv, P.kc), smem_desc(bh + adv, P.kc), idesc, first ? 0 : 1);
+        if (TERMS > 1)
+        {
+          mma_tf32(d1, smem_desc(ah + adv, P.kc), smem_desc(bl + adv, P.kc), idesc, 1);
+          mma_tf32(d1, smem_desc(al + adv, P.kc), smem_desc(bh + adv, P.kc), idesc, 1);
+        }
+      }
+      mma_commit(bar);
+    }
+    if (!mbar_wait(bar, phase))
+      ok = false;
+    phase ^= 1;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+  }
+
+  if (ok)
+  {
+    // ---------------- W = Binv V, stored transposed (n_pad rows x k1) for the second product
+    for (int i = tid; i < P.npad; i += TC_NT)
+    {
+      for (int c4 = 0; c4 < P.k1; c4 += 4)
+      {
+        float w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+        {
+          const int c = c4 + q;
+          float a     = 0.f;
+          if (c < dc && i < n)
+            for (int l = 0; l < dc; l++)
+              a += Bs[c * dc + l] * Vs[l * n + i];
+          w[q] = a;
+        }
+        float4 h = make_float4(tf32_hi(w[0]), tf32_hi(w[1]), tf32_hi(w[2]), tf32_hi(w[3]));
+        float4 lo = make_float4(w[0] - h.x, w[1] - h.y, w[2] - h.z, w[3] - h.w);
+        const uint32_t off = cm_off(i, c4, P.k1);
+        *reinterpret_cast<float4*>(sm + P.w_hi + off) = h;
+        if (TERMS > 1)
+          *reinterpret_cast<float4*>(sm + P.w_lo + off) = lo;
+      }
+    }
+    // ---------------- T1 - E from TMEM into the second product's A tile
+    {
+      const int r = warp * 32 + lane; // this thread's TMEM lane = block row
+      for (int c0 = 0; c0 < P.k1; c0 += 32)
+      {
+        float t[32];
+        tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+        {
+          const int c = c0 + q;
+          if (c >= dc)
+            t[q] = 0.f;
+          else if (dls[c] == r0 + r)
+            t[q] -= 1.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+        {
+          float4 h = make_float4(tf32_hi(t[q]), tf32_hi(t[q + 1]), tf32_hi(t[q + 2]), tf32_hi(t[q + 3]));
+          float4 lo = make_float4(t[q] - h.x, t[q + 1] - h.y, t[q + 2] - h.z, t[q + 3] - h.w);
+          const uint32_t off = cm_off(r, c0 + q, P.k1);
+          *reinterpret_cast<float4*>(sm + P.a2_hi + off) = h;
+          if (TERMS > 1)
+            *reinterpret_cast<float4*>(sm + P.a2_lo + off) = lo;
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    // ---------------- P = (T1 - E) W
+    if (tid == 0)
+    {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t idesc = idesc_tf32(TC_M, P.npad);
+      const uint32_t ah = smem_u32(sm + P.a2_hi), al = smem_u32(sm + P.a2_lo);
+      const uint32_t bh = smem_u32(sm + P.w_hi), bl = smem_u32(sm + P.w_lo);
+      for (int ks = 0; ks < P.k1 / 8; ks++)
+      {
+        const uint32_t adv = ks * 256;
+        mma_tf32(d2, smem_desc(ah + adv, P.k1), smem_desc(bh + adv, P.k1), idesc, ks ? 1 : 0);
+        if (TERMS > 1)
+        {
+          mma_tf32(d2, smem_desc(ah + adv, P.k1), smem_desc(bl + adv, P.k1), idesc, 1);
+          mma_tf32(d2, smem_desc(al + adv, P.k1), smem_desc(bh + adv, P.k1), idesc, 1);
+        }
+      }
+      mma_commit(bar);
+    }
+    if (!mbar_wait(bar, phase))
+      ok = false;
+    phase ^= 1;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+  }
+
+  if (ok)
+  {
+    // ---------------- epilogue: Ainv[rows] -= P, each thread one row
+    const int r  = warp * 32 + lane;
+    const int gr = r0 + r;
+    for (int c0 = 0; c0 < P.npad; c0 += 32)
+    {
+      float p[32];
+      tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
+      if (gr < n)
+      {
+        float* row = A + (size_t)gr * lda + c0;
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+          if (c0 + q < n)
+          {
+            float4 a = *reinterpret_cast<float4*>(row + q);
+            a.x -= p[q];
+            a.y -= p[q + 1];
+            a.z -= p[q + 2];
+            a.w -= p[q + 3];
+            *reinterpret_cast<float4*>(row + q) = a;
+          }
+      }
+    }
+  }
+  else if (tid == 0)
+    atomicExch(err, 1);
+
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(cols) : "memory");
+}
+
+bool flush_tc_supported(int n, int k, int lda)
+{
+  // 64 + n_pad TMEM columns, one 128-row block per CTA, 16-byte aligned rows
+  const TcPlan p = tc_plan(n, k);
+  return k <= 32 && 64 + p.npad <= 512 && (lda % 4) == 0 && (n % 4) == 0 && p.total <= 200 * 1024;
+}
+
+cudaError_t setup_flush_tc()
+{
+  cudaError_t e = cudaFuncSetAttribute(flush_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(flush_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cudaStream_t st)
+{
+  if (f.dc <= 0 || f.nw <= 0)
+    return cudaSuccess;
+  const TcPlan p = tc_plan(f.n, f.k);
+  dim3 grid(f.nw, (f.n + TC_M - 1) / TC_M);
+  if (terms == 1)
+    flush_tc_kernel<1><<<grid, TC_NT, p.total, st>>>(f, err);
+  else
+    flush_tc_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
+  return cudaGetLastError();
+}
+
+} // namespace qmcg

@@ -46,6 +46,11 @@ cudaError_t setup_flush_fused();
 template<typename T>
 bool flush_fused_fits(int n, int k);
 
+// tensor-core flush (flush_tc.cu), FP32 only: terms 1 = TF32, 3 = 3xTF32
+bool flush_tc_supported(int n, int k, int lda);
+cudaError_t setup_flush_tc();
+cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cudaStream_t st);
+
 // flush arguments of one spin of a crowd
 template<typename T>
 inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* W)
