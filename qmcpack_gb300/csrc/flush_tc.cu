@@ -151,7 +151,7 @@ __host__ __device__ inline TcPlan tc_plan(int n, int k)
 }
 
 template<int TERMS>
-__global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, int* err)
+__global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, int* err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   const TcPlan P = tc_plan(f.n, f.k);
@@ -199,40 +199,60 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, 
   uint32_t phase      = 0;
   bool ok             = true;
 
-  // ---------------- T1 = Ainv[rows] U^T, K in chunks of kc
+  // ---------------- T1 = Ainv[rows] U^T, K in chunks of kc.  The next chunk's
+  // global loads are issued before waiting for the current chunk's MMAs.
+  constexpr int AV = TC_M * (TC_KC / 4) / TC_NT; // float4 of the Ainv chunk per thread (16)
   const int nchunks = (n + P.kc - 1) / P.kc;
+  const int ub      = P.k1 * (P.kc / 4);         // float4 of the U chunk (all threads)
+  float4 ra[AV];
+  float4 ru[(32 * (TC_KC / 4) + TC_NT - 1) / TC_NT * 2];
+  // slot e of a (rows x kc) tile: 8 consecutive slots are the 8 rows of one core
+  // matrix (conflict-free 16-byte shared stores), 32 consecutive slots cover 64
+  // contiguous bytes of 8 rows (full global sectors)
+  auto slot_row = [](int e) { return (e / (8 * (TC_KC / 4))) * 8 + (e & 7); };
+  auto slot_col = [](int e) { return ((e >> 3) % (TC_KC / 4)) * 4; };
+  auto load_chunk = [&](int ch) {
+    const int k0 = ch * P.kc;
+#pragma unroll
+    for (int q = 0; q < AV; q++)
+    {
+      const int e = tid + q * TC_NT;
+      const int r = slot_row(e), c4 = slot_col(e);
+      const int gr = r0 + r, gc = k0 + c4;
+      ra[q] = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(ru) / sizeof(float4)); q++)
+    {
+      const int e = tid + q * TC_NT;
+      const int r = slot_row(e), c4 = slot_col(e);
+      const int gc = k0 + c4;
+      ru[q] = (e < ub && r < dc && gc < n) ? *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc)
+                                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  auto split_store = [&](float4 x, uint32_t hi_base, uint32_t lo_base, uint32_t off) {
+    float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+    *reinterpret_cast<float4*>(sm + hi_base + off) = h;
+    if (TERMS > 1)
+      *reinterpret_cast<float4*>(sm + lo_base + off) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+  };
+  load_chunk(0);
   for (int ch = 0; ch < nchunks && ok; ch++)
   {
-    const int k0 = ch * P.kc;
-    // Ainv rows: 128 rows x kc columns, 16-byte groups of 4 columns
-    for (int e = tid; e < TC_M * (P.kc / 4); e += TC_NT)
+#pragma unroll
+    for (int q = 0; q < AV; q++)
     {
-      const int r = e / (P.kc / 4), c4 = (e % (P.kc / 4)) * 4;
-      const int gr = r0 + r, gc = k0 + c4;
-      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gr < n && gc < n)
-        x = *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc);
-      float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-      float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
-      const uint32_t off = cm_off(r, c4, P.kc);
-      *reinterpret_cast<float4*>(sm + P.a_hi + off) = h;
-      if (TERMS > 1)
-        *reinterpret_cast<float4*>(sm + P.a_lo + off) = l;
+      const int e = tid + q * TC_NT;
+      split_store(ra[q], P.a_hi, P.a_lo, cm_off(slot_row(e), slot_col(e), P.kc));
     }
-    // U rows: k1 rows x kc columns, rows >= dc are zero
-    for (int e = tid; e < P.k1 * (P.kc / 4); e += TC_NT)
+#pragma unroll
+    for (int q = 0; q < (int)(sizeof(ru) / sizeof(float4)); q++)
     {
-      const int r = e / (P.kc / 4), c4 = (e % (P.kc / 4)) * 4;
-      const int gc = k0 + c4;
-      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r < dc && gc < n)
-        x = *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc);
-      float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
-      float4 l = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
-      const uint32_t off = cm_off(r, c4, P.kc);
-      *reinterpret_cast<float4*>(sm + P.b_hi + off) = h;
-      if (TERMS > 1)
-        *reinterpret_cast<float4*>(sm + P.b_lo + off) = l;
+      const int e = tid + q * TC_NT;
+      if (e < ub)
+        split_store(ru[q], P.b_hi, P.b_lo, cm_off(slot_row(e), slot_col(e), P.kc));
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -256,6 +276,8 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, 
       }
       mma_commit(bar);
     }
+    if (ch + 1 < nchunks)
+      load_chunk(ch + 1);
     if (!mbar_wait(bar, phase))
       ok = false;
     phase ^= 1;
@@ -268,6 +290,10 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, 
     // ---------------- W = Binv V, stored transposed (n_pad rows x k1) for the second product
     for (int i = tid; i < P.npad; i += TC_NT)
     {
+      float vcol[32];
+#pragma unroll
+      for (int l = 0; l < 32; l++)
+        vcol[l] = (l < dc && i < n) ? Vs[l * n + i] : 0.f;
       for (int c4 = 0; c4 < P.k1; c4 += 4)
       {
         float w[4];
@@ -276,9 +302,11 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, 
         {
           const int c = c4 + q;
           float a     = 0.f;
-          if (c < dc && i < n)
-            for (int l = 0; l < dc; l++)
-              a += Bs[c * dc + l] * Vs[l * n + i];
+          if (c < dc)
+#pragma unroll
+            for (int l = 0; l < 32; l++)
+              if (l < dc)
+                a += Bs[c * dc + l] * vcol[l];
           w[q] = a;
         }
         float4 h = make_float4(tf32_hi(w[0]), tf32_hi(w[1]), tf32_hi(w[2]), tf32_hi(w[3]));
@@ -348,28 +376,42 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_kernel(FlushArgs<float> f, 
 
   if (ok)
   {
-    // ---------------- epilogue: Ainv[rows] -= P, each thread one row
+    // ---------------- epilogue: Ainv[rows] -= P, each thread one row; the next
+    // 32-column piece of the row is loaded while the current one is written
     const int r  = warp * 32 + lane;
     const int gr = r0 + r;
+    float* row   = A + (size_t)(gr < n ? gr : 0) * lda;
+    float4 cur[8], nxt[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      cur[q] = (gr < n && 4 * q < n) ? *reinterpret_cast<const float4*>(row + 4 * q) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c0 = 0; c0 < P.npad; c0 += 32)
     {
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+      {
+        const int c = c0 + 32 + 4 * q;
+        nxt[q] = (gr < n && c < n) ? *reinterpret_cast<const float4*>(row + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
       float p[32];
       tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
       if (gr < n)
       {
-        float* row = A + (size_t)gr * lda + c0;
 #pragma unroll
-        for (int q = 0; q < 32; q += 4)
-          if (c0 + q < n)
+        for (int q = 0; q < 8; q++)
+          if (c0 + 4 * q < n)
           {
-            float4 a = *reinterpret_cast<float4*>(row + q);
-            a.x -= p[q];
-            a.y -= p[q + 1];
-            a.z -= p[q + 2];
-            a.w -= p[q + 3];
-            *reinterpret_cast<float4*>(row + q) = a;
+            float4 a = cur[q];
+            a.x -= p[4 * q];
+            a.y -= p[4 * q + 1];
+            a.z -= p[4 * q + 2];
+            a.w -= p[4 * q + 3];
+            *reinterpret_cast<float4*>(row + c0 + 4 * q) = a;
           }
       }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        cur[q] = nxt[q];
     }
   }
   else if (tid == 0)
