@@ -67,6 +67,8 @@ typedef struct
   double j2_rcut;
   const double* j2_params; /* [2][j2_num_params] */
   const double* j2_cusp;   /* [2] */
+  const double* ion_charges; /* [num_ion_species] valence charges for the Coulomb energy; NULL = a
+                                neutral cell, (n_up + n_dn) / num_ions on every ion */
 } qmcg_system_desc;
 
 /* Driver parameters of one VMC sweep loop (VMCBatched::advanceWalkers,
@@ -181,6 +183,24 @@ int qmcg_vmc_sweeps(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_s
  * numbers and returns without synchronizing (timing helper for benchmarks; the
  * graph must have been built by a previous qmcg_vmc_sweeps with rng_mode 1). */
 int qmcg_vmc_sweeps_async(qmcg_crowd crowd, int num_sweeps);
+
+/* Local energy E_L = T + V of every walker after all delayed updates
+ * (QMCHamiltonian::mw_evaluate over BareKineticEnergy::mw_evaluate,
+ * src/QMCHamiltonians/BareKineticEnergy.cpp:102-160, and the Coulomb terms
+ * CoulombPBCAA (e-e, i-i) + CoulombPBCAB (e-i)).  T = -1/2 sum_i (|G_i|^2 + L_i) from
+ * the tracked gradients and Laplacians of log psi (mw_evaluateGL); V is the Ewald
+ * energy of the electrons (charge -1) and the ions, the quantity the reference's
+ * standalone sum src/QMCHamiltonians/EwaldRef.cpp:337-398 computes, evaluated with a
+ * real/reciprocal split to 1e-7 (FP32 systems) or 1e-12 (FP64) relative tolerance.
+ * Outputs are host arrays of num_walkers doubles; any may be NULL.  Returns
+ * QMCG_ERR_STATE while delayed updates are pending. */
+int qmcg_mw_evaluate_local_energy(qmcg_crowd crowd, double* e_local, double* kinetic, double* potential);
+
+/* qmcg_vmc_sweeps (without an accept log) with the local energy of every walker
+ * measured after every sweep, as the VMC driver's estimator step does:
+ * e_local and kinetic (may be NULL) are host arrays [num_sweeps][num_walkers]. */
+int qmcg_vmc_sweeps_measure(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, double* e_local,
+                            double* kinetic, qmcg_sweep_stats* stats);
 
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);

@@ -21,8 +21,8 @@ _lp = C.POINTER(C.c_long)
 
 def build(force: bool = False) -> str:
     so = os.path.join(_HERE, "liboracle.so")
-    src = os.path.join(_HERE, "qmc_oracle.cpp")
-    if force or not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("qmc_oracle.cpp", "ewald_oracle.cpp", "Makefile")]
+    if force or not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(f) for f in srcs):
         subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
     return so
 
@@ -73,6 +73,12 @@ def lib():
         L.orc_det_accept_reject.argtypes = [C.c_void_p, C.c_int, _dp, C.c_double, C.c_int]
         L.orc_det_complete.argtypes = [C.c_void_p]
         L.orc_det_get_ainv.argtypes = [C.c_void_p, _dp]
+        L.orc_kinetic.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_ewald_ref_energy.argtypes = [_dp, C.c_int, _dp, _dp, C.c_double]
+        L.orc_ewald_ref_energy.restype = C.c_double
+        L.orc_madelung.argtypes = [_dp, C.c_double]
+        L.orc_madelung.restype = C.c_double
+        L.orc_ewald_split_energy.argtypes = [_dp, C.c_int, _dp, _dp, C.c_double, _dp]
     return _LIB
 
 
@@ -128,6 +134,30 @@ def distance_row(lattice, R, r):
     rr = _d(r)
     lib().orc_distance_row(_ptr(lat), n, _ptr(R), _ptr(rr), _ptr(dist), _ptr(dr))
     return dist, dr
+
+
+def ewald_ref_energy(cell_rows, R, Q, tol: float = 1e-10) -> float:
+    """Total Ewald energy of point charges (EwaldRef restatement); cell_rows: 3x3, rows = cell vectors."""
+    a = _d(cell_rows).reshape(9)
+    R = _d(R).reshape(-1, 3)
+    Q = _d(Q)
+    return lib().orc_ewald_ref_energy(_ptr(a), len(Q), _ptr(R), _ptr(Q), tol)
+
+
+def madelung(cell_rows, tol: float = 1e-12) -> float:
+    a = _d(cell_rows).reshape(9)
+    return lib().orc_madelung(_ptr(a), tol)
+
+
+def ewald_split_energy(lattice, R, Q, eps: float = 1e-14):
+    """Same energy by the real/reciprocal split of the GPU kernel (orthorhombic cell, FP64).
+    Returns (real-space, reciprocal, constant, total)."""
+    L = _d(lattice)
+    R = _d(R).reshape(-1, 3)
+    Q = _d(Q)
+    out = np.zeros(4)
+    lib().orc_ewald_split_energy(_ptr(L), len(Q), _ptr(R), _ptr(Q), eps, _ptr(out))
+    return out
 
 
 def set_threads(n: int):
@@ -281,3 +311,24 @@ class Crowd:
         lib().orc_vmc_sweeps(self.h, rng.h, nsteps, tau, int(use_drift), C.byref(na), C.byref(nr),
                              _ptr(acc, _ip) if acc is not None else None)
         return na.value, nr.value, acc
+
+    def kinetic(self, with_gl: bool = False):
+        """Kinetic energy per walker from the tracked state (call complete_updates first);
+        with_gl also returns [nw][ne][4] = grad log psi (xyz) and Laplacian of log psi."""
+        ke = np.zeros(self.nw)
+        gl = np.zeros((self.nw, self.ne, 4)) if with_gl else None
+        lib().orc_kinetic(self.h, _ptr(ke), _ptr(gl) if gl is not None else None)
+        return (ke, gl) if with_gl else ke
+
+    def potential(self, eps: float = 1e-14):
+        """Ewald energy of electrons (charge -1) and ions (the system's charges) per walker."""
+        s = self.system
+        R = self.positions()
+        Q = np.concatenate([-np.ones(self.ne), s.ion_charges[s.ion_species]])
+        return np.array([ewald_split_energy(s.lattice, np.concatenate([R[iw], s.ion_pos]), Q, eps)[3]
+                         for iw in range(self.nw)])
+
+    def local_energy(self, eps: float = 1e-14):
+        ke = self.kinetic()
+        v = self.potential(eps)
+        return ke + v, ke, v

@@ -843,6 +843,8 @@ struct Crowd
   std::vector<T> dgrad, dlap;
   T* dgrad_row(int iw, int s, int e) { return dgrad.data() + (((size_t)iw * 2 + s) * norb + e) * 3 * norb; }
   T* dlap_row(int iw, int s, int e) { return dlap.data() + (((size_t)iw * 2 + s) * norb + e) * norb; }
+  const T* dgrad_row(int iw, int s, int e) const { return dgrad.data() + (((size_t)iw * 2 + s) * norb + e) * 3 * norb; }
+  const T* dlap_row(int iw, int s, int e) const { return dlap.data() + (((size_t)iw * 2 + s) * norb + e) * norb; }
 
   double log_j2(int iw) const
   {
@@ -857,6 +859,57 @@ struct Crowd
     for (int i = 0; i < ne; i++)
       s += static_cast<double>(w[iw].Vat[i]);
     return -s;
+  }
+
+  // ---------------- TrialWaveFunction::mw_evaluateGL + BareKineticEnergy ----
+  // With all delayed updates applied, per electron i of spin s and row r:
+  //   G_i = Ainv[r].dphi_i + dUat_i + Grad1_i
+  //   L_i = Ainv[r].d2phi_i - |Ainv[r].dphi_i|^2 + d2Uat_i - Lap1_i
+  // (DiracDeterminantBatched.cpp:594-603, TwoBodyJastrow.cpp:774-775,
+  // J1OrbitalSoA.h:119-120) and KE = -1/2 sum_i (|G_i|^2 + L_i) for unit mass
+  // (BareKineticEnergy.cpp:110-117).  gl (optional): [ne][4] = G xyz, L.
+  double kinetic(int iw, double* gl) const
+  {
+    const Walker& wk = w[iw];
+    double ke        = 0;
+    for (int iat = 0; iat < ne; iat++)
+    {
+      const int s   = group_of(iat);
+      const int row = iat - first_of(s);
+      const T* inv  = wk.det[s].Ainv.data() + (size_t)row * norb;
+      const T* gr   = dgrad_row(iw, s, row);
+      const T* lp   = dlap_row(iw, s, row);
+      double g[3], l = 0;
+      for (int dd = 0; dd < 3; dd++)
+      {
+        double acc = 0;
+        for (int o = 0; o < norb; o++)
+          acc += static_cast<double>(inv[o]) * static_cast<double>(gr[(size_t)dd * norb + o]);
+        g[dd] = acc;
+      }
+      for (int o = 0; o < norb; o++)
+        l += static_cast<double>(inv[o]) * static_cast<double>(lp[o]);
+      l -= g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+      for (int dd = 0; dd < 3; dd++)
+      {
+        if (has_j1)
+          g[dd] += static_cast<double>(wk.Grad[(size_t)dd * ne + iat]);
+        if (has_j2)
+          g[dd] += static_cast<double>(wk.dUat[(size_t)dd * ne + iat]);
+      }
+      if (has_j1)
+        l -= static_cast<double>(wk.Lap[iat]);
+      if (has_j2)
+        l += static_cast<double>(wk.d2Uat[iat]);
+      ke += -0.5 * (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + l);
+      if (gl)
+      {
+        for (int dd = 0; dd < 3; dd++)
+          gl[(size_t)iat * 4 + dd] = g[dd];
+        gl[(size_t)iat * 4 + 3] = l;
+      }
+    }
+    return ke;
   }
 
   // ---------------- TrialWaveFunction::mw_evalGrad -------------------------
@@ -1408,6 +1461,18 @@ void orc_get_phi_vgl(void* hv, int s, double* out)
 }
 
 // ---- threads used by the per-walker loops (OpenMP over walkers, like crowds) ---
+// kinetic energy per walker from the tracked state (after complete_updates);
+// gl (optional): [nw][ne][4] gradient and Laplacian of log psi per electron
+void orc_kinetic(void* hv, double* ke, double* gl)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  dispatch(h, [&](auto* c) {
+#pragma omp parallel for schedule(static)
+    for (int iw = 0; iw < c->nw; iw++)
+      ke[iw] = c->kinetic(iw, gl ? gl + (size_t)iw * c->ne * 4 : nullptr);
+  });
+}
+
 void orc_set_threads(int n)
 {
 #ifdef _OPENMP

@@ -19,7 +19,7 @@ EXPORTS = [
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
     "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_ex", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
-    "qmcg_profile_sweep",
+    "qmcg_profile_sweep", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
 ]
 
 
@@ -30,7 +30,7 @@ class SystemDesc(C.Structure):
         ("ion_pos", _dp), ("ion_species", _ip), ("num_ion_species", C.c_int), ("grid", C.c_int * 3),
         ("spline_coefs", C.c_void_p), ("j1_num_params", C.c_int), ("j1_rcut", C.c_double),
         ("j1_params", _dp), ("j1_cusp", _dp), ("j2_num_params", C.c_int), ("j2_rcut", C.c_double),
-        ("j2_params", _dp), ("j2_cusp", _dp),
+        ("j2_params", _dp), ("j2_cusp", _dp), ("ion_charges", _dp),
     ]
 
 
@@ -88,6 +88,8 @@ def load(path: str = LIB_PATH):
         "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
         "qmcg_profile_sweep": [vp, C.c_int, _dp],
+        "qmcg_mw_evaluate_local_energy": [vp, _dp, _dp, _dp],
+        "qmcg_vmc_sweeps_measure": [vp, C.POINTER(SweepParams), C.c_int, _dp, _dp, C.POINTER(SweepStats)],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqmcg.so")
 
-SOURCES = ["capi.cu", "move_kernels.cu", "recompute_kernels.cu", "sweep_kernel.cu", "flush_kernels.cu", "flush_tc.cu",
+SOURCES = ["capi.cu", "move_kernels.cu", "recompute_kernels.cu", "sweep_kernel.cu", "flush_kernels.cu", "flush_tc.cu", "energy.cu",
            "noalloc.cu"]
 HEADERS = ["common.cuh", "spline.cuh", "launch.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

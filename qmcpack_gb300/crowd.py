@@ -58,6 +58,8 @@ class DeviceSystem:
         d.j1_params, d.j1_cusp = _p(self._j1p), _p(self._j1c)
         d.j2_num_params, d.j2_rcut = self._j2p.shape[1], s.spec.j2_rcut
         d.j2_params, d.j2_cusp = _p(self._j2p), _p(self._j2c)
+        self._q = _d(s.ion_charges) if s.ion_charges is not None else None
+        d.ion_charges = _p(self._q) if self._q is not None else None
         self.handle = C.c_void_p()
         check(L.qmcg_system_create(C.byref(d), C.byref(self.handle)))
 
@@ -170,6 +172,25 @@ class Crowd:
                                      _p(acc, _ip) if acc is not None else None))
         self.last_repaired = st.repaired
         return st.accepted, st.rejected, acc
+
+    def mw_evaluate_local_energy(self):
+        """(E_L, kinetic, potential) per walker; needs all delayed updates completed."""
+        el, ke, vp = np.zeros(self.nw), np.zeros(self.nw), np.zeros(self.nw)
+        check(self.L.qmcg_mw_evaluate_local_energy(self.handle, _p(el), _p(ke), _p(vp)))
+        return el, ke, vp
+
+    def vmc_sweeps_measure(self, nsweeps: int, tau: float, seed: int, rng_mode: int = 1, use_drift: bool = True,
+                           recompute_every: int = 0, staged: bool = False, flush: int = 0):
+        """Sweeps with the local energy of every walker after each: (accepted, rejected, E_L[nsweeps][nw],
+        kinetic[nsweeps][nw])."""
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=rng_mode, seed=seed,
+                        recompute_every=recompute_every, path=1 if staged else 0, flush=flush)
+        st = SweepStats()
+        el = np.zeros((nsweeps, self.nw))
+        ke = np.zeros((nsweeps, self.nw))
+        check(self.L.qmcg_vmc_sweeps_measure(self.handle, C.byref(p), nsweeps, _p(el), _p(ke), C.byref(st)))
+        self.last_repaired = st.repaired
+        return st.accepted, st.rejected, el, ke
 
     def vmc_sweeps_async(self, nsweeps: int):
         check(self.L.qmcg_vmc_sweeps_async(self.handle, nsweeps))

@@ -101,6 +101,13 @@ struct qmcg_system_s
   double j1_rcut = 0, j2_rcut = 0;
   double j1_dri = 0, j2_dri = 0;
   int has_j1 = 0, has_j2 = 0;
+  // Ewald tables for the local energy (precision of the move loop)
+  EwaldHost ewh;
+  int ew_ng = 0;
+  void* ew_gn = nullptr;
+  void* ew_fg = nullptr;
+  void* ew_rho = nullptr;
+  void* ew_q = nullptr;
 };
 
 // BsplineFunctor::reset (BsplineFunctor.h:117-133) in the functor precision T
@@ -167,6 +174,48 @@ static int build_system(const qmcg_system_desc* d, qmcg_system_s* s)
     s->j2c      = dc;
     s->j2_ncoef = d->j2_num_params + 4;
   }
+  // Coulomb: ion charges per species (default: a neutral cell), Ewald tables with
+  // tolerance 1e-7 (FP32) or 1e-12 (FP64)
+  {
+    std::vector<double> q(std::max(d->num_ions, 1), 0.0), pos((size_t)3 * std::max(d->num_ions, 1), 0.0);
+    for (int i = 0; i < d->num_ions; i++)
+    {
+      const int sp = d->ion_species ? d->ion_species[i] : 0;
+      q[i]         = d->ion_charges ? d->ion_charges[sp] : static_cast<double>(s->ne) / d->num_ions;
+      for (int k = 0; k < 3; k++)
+        pos[3 * i + k] = d->ion_pos[3 * i + k];
+    }
+    const double eps = std::is_same<T, float>::value ? 1e-7 : 1e-12;
+    if (ewald_build(s->L, s->ne, d->num_ions, pos.data(), q.data(), eps, s->ewh) != 0)
+      return fail(QMCG_ERR_ARG, "Ewald tables: the cell is too anisotropic for the reciprocal cutoff");
+    const auto& e = s->ewh;
+    s->ew_ng      = static_cast<int>(e.fg.size());
+    const size_t ng = std::max<size_t>(e.fg.size(), 1);
+    std::vector<T> fg(ng, T(0)), rho(2 * ng, T(0)), qt(q.size());
+    for (size_t g = 0; g < e.fg.size(); g++)
+    {
+      fg[g]          = static_cast<T>(e.fg[g]);
+      rho[2 * g]     = static_cast<T>(e.rho_ion[2 * g]);
+      rho[2 * g + 1] = static_cast<T>(e.rho_ion[2 * g + 1]);
+    }
+    for (size_t i = 0; i < q.size(); i++)
+      qt[i] = static_cast<T>(q[i]);
+    char4* dgn;
+    T *dfg, *drho, *dq;
+    CUDA_TRY(s->mem.alloc(&dgn, ng));
+    CUDA_TRY(s->mem.alloc(&dfg, ng));
+    CUDA_TRY(s->mem.alloc(&drho, 2 * ng));
+    CUDA_TRY(s->mem.alloc(&dq, qt.size()));
+    if (!e.gn.empty())
+      CUDA_TRY(cudaMemcpy(dgn, e.gn.data(), e.gn.size() * sizeof(char4), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dfg, fg.data(), ng * sizeof(T), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(drho, rho.data(), 2 * ng * sizeof(T), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(dq, qt.data(), qt.size() * sizeof(T), cudaMemcpyHostToDevice));
+    s->ew_gn  = dgn;
+    s->ew_fg  = dfg;
+    s->ew_rho = drho;
+    s->ew_q   = dq;
+  }
   return QMCG_OK;
 }
 
@@ -196,6 +245,10 @@ extern "C" int qmcg_system_create(const qmcg_system_desc* d, qmcg_system* out)
     for (int i = 0; i < d->num_ions; i++)
       if (d->ion_species[i] < 0 || d->ion_species[i] >= d->num_ion_species)
         return fail(QMCG_ERR_ARG, "ion species index out of range");
+  if (d->ion_charges)
+    for (int sp = 0; sp < d->num_ion_species; sp++)
+      if (!std::isfinite(d->ion_charges[sp]))
+        return fail(QMCG_ERR_ARG, "ion charges must be finite");
   if ((d->j1_num_params > 0 && (!d->j1_params || !(d->j1_rcut > 0))) ||
       (d->j2_num_params > 0 && (!d->j2_params || !(d->j2_rcut > 0))))
     return fail(QMCG_ERR_ARG, "Jastrow parameters or cutoff missing");
@@ -328,6 +381,8 @@ struct qmcg_crowd_s
   virtual int profile_ratio(int niat, double* ms)        = 0;
   virtual int profile_sweep(int n, double* out)          = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
+  virtual int local_energy(double* el, double* ke, double* vp) = 0;
+  virtual int sweeps_measure(const qmcg_sweep_params* p, int n, double* el, double* ke, qmcg_sweep_stats* st) = 0;
 };
 
 template<typename T>
@@ -354,6 +409,10 @@ struct Crowd final : qmcg_crowd_s
   uint64_t graph_seed = 0;
   int sweeps_since_recompute = 0;
   int recompute_every        = 0;
+  EwaldDev<T> ew{};
+  double* e_out  = nullptr; // [3][nw] local energy, kinetic, potential
+  double* e_hist = nullptr; // [e_hist_cap][2][nw] per-sweep local and kinetic energies
+  size_t e_hist_cap = 0;
 
   ~Crowd() override
   {
@@ -363,6 +422,8 @@ struct Crowd final : qmcg_crowd_s
       cudaFreeHost(gauss_h);
     if (unif_h)
       cudaFreeHost(unif_h);
+    if (e_hist)
+      cudaFree(e_hist);
     if (stream)
       cudaStreamDestroy(stream);
   }
@@ -454,6 +515,18 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
     CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size));
+    CUDA_TRY(setup_local_energy<T>());
+    CUDA_TRY(mem.alloc(&e_out, 3 * (size_t)nw));
+    ew.ng      = sys->ew_ng;
+    ew.nmax    = sys->ewh.nmax;
+    ew.gn      = static_cast<const char4*>(sys->ew_gn);
+    ew.fg      = static_cast<const T*>(sys->ew_fg);
+    ew.rho_ion = static_cast<const T*>(sys->ew_rho);
+    ew.ion_q   = static_cast<const T*>(sys->ew_q);
+    ew.alpha   = static_cast<T>(sys->ewh.alpha);
+    ew.e_const = sys->ewh.e_const;
+    if (local_energy_smem(sys->ne, ew.nmax, sizeof(T)) > 200 * 1024)
+      return fail(QMCG_ERR_ARG, "local energy: too many electrons for the shared-memory tables");
     d.gauss     = gauss_d;
     d.uniform   = unif_d;
     d.rng_mode  = 1;
@@ -846,6 +919,61 @@ struct Crowd final : qmcg_crowd_s
 
   int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) override
   {
+    return run_sweeps(p, n, st, acc_log, false);
+  }
+
+  // QMCHamiltonian::mw_evaluate for kinetic + Coulomb after all delayed updates
+  int local_energy(double* el, double* ke, double* vp) override
+  {
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "local energy needs mw_completeUpdates first");
+    CUDA_TRY(launch_local_energy<T>(s, ew, e_out, stream));
+    std::vector<double> h(3 * (size_t)nw);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), e_out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (el)
+      std::copy_n(h.data(), nw, el);
+    if (ke)
+      std::copy_n(h.data() + nw, nw, ke);
+    if (vp)
+      std::copy_n(h.data() + 2 * nw, nw, vp);
+    return QMCG_OK;
+  }
+
+  // sweeps with the local energy measured after each one (into a device history,
+  // read back once at the end)
+  int sweeps_measure(const qmcg_sweep_params* p, int n, double* el, double* ke, qmcg_sweep_stats* st) override
+  {
+    if (n < 0 || !el)
+      return fail(QMCG_ERR_ARG, "bad arguments");
+    const size_t need = (size_t)std::max(n, 1) * 3 * nw;
+    if (need > e_hist_cap)
+    {
+      if (e_hist)
+        CUDA_TRY(cudaFree(e_hist));
+      e_hist = nullptr;
+      CUDA_TRY(cudaMalloc(&e_hist, need * sizeof(double)));
+      e_hist_cap = need;
+    }
+    int rc = run_sweeps(p, n, nullptr, nullptr, true);
+    if (rc)
+      return rc;
+    std::vector<double> h((size_t)n * 3 * nw);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), e_hist, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    rc = sync(st);
+    if (rc)
+      return rc;
+    for (int it = 0; it < n; it++)
+    {
+      std::copy_n(h.data() + (size_t)it * 3 * nw, nw, el + (size_t)it * nw);
+      if (ke)
+        std::copy_n(h.data() + ((size_t)it * 3 + 1) * nw, nw, ke + (size_t)it * nw);
+    }
+    return QMCG_OK;
+  }
+
+  int run_sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log, bool measure)
+  {
     if (!p || n < 0 || !(p->tau > 0) || (p->rng_mode != 0 && p->rng_mode != 1))
       return fail(QMCG_ERR_ARG, "bad sweep parameters");
     if (dc[0] || dc[1])
@@ -885,6 +1013,8 @@ struct Crowd final : qmcg_crowd_s
       }
       else
         CUDA_TRY(cudaGraphLaunch(graph, stream));
+      if (measure)
+        CUDA_TRY(launch_local_energy<T>(s, ew, e_hist + (size_t)it * 3 * nw, stream));
       if (p->rng_mode == 0)
       {
         int used[2];
@@ -901,7 +1031,7 @@ struct Crowd final : qmcg_crowd_s
         sweeps_since_recompute = 0;
       }
     }
-    return sync(st);
+    return measure ? QMCG_OK : sync(st);
   }
 
   int sweep_logged(int* acc_log)
@@ -1208,6 +1338,15 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
   CROWD_CALL(c, sweeps(p, n, st, acc));
 }
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
+extern "C" int qmcg_mw_evaluate_local_energy(qmcg_crowd c, double* el, double* ke, double* vp)
+{
+  CROWD_CALL(c, local_energy(el, ke, vp));
+}
+extern "C" int qmcg_vmc_sweeps_measure(qmcg_crowd c, const qmcg_sweep_params* p, int n, double* el, double* ke,
+                                       qmcg_sweep_stats* st)
+{
+  CROWD_CALL(c, sweeps_measure(p, n, el, ke, st));
+}
 extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }
 extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
 extern "C" int qmcg_profile_sweep(qmcg_crowd c, int n, double* ms) { CROWD_CALL(c, profile_sweep(n, ms)); }

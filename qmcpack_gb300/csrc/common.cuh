@@ -102,6 +102,19 @@ struct DevState
   int use_drift;
 };
 
+// Ewald tables of a system for the local-energy kernel (energy.cu)
+template<typename T>
+struct EwaldDev
+{
+  int ng, nmax;       // half-space G vectors; largest |n| along any axis
+  const char4* gn;    // [ng] (n1, n2, n3): G = 2 pi (n1/Lx, n2/Ly, n3/Lz), sorted
+  const T* fg;        // [ng] 4 pi/V exp(-G^2/4a^2)/G^2
+  const T* rho_ion;   // [ng][2] ion structure factor sum_I Z_I exp(i G.R_I)
+  const T* ion_q;     // [nions] ion charges
+  T alpha;
+  double e_const;     // ion-ion, self-energy and background terms
+};
+
 // Arguments of the delayed-update flush Ainv -= (Ainv U^T - E)(Binv V) over a
 // batch of walkers: row-major per walker, per-walker strides in elements.
 template<typename T>

@@ -1,0 +1,328 @@
+// Local energy of every walker, E_L = T + V, one CTA per walker:
+//
+//   kinetic  T = -1/2 sum_i (|G_i|^2 + L_i) with G_i, L_i the gradient and Laplacian
+//            of log psi from the tracked state (TrialWaveFunction::mw_evaluateGL:
+//            DiracDeterminantBatched.cpp:594-603, TwoBodyJastrow.cpp:774-775,
+//            J1OrbitalSoA.h:119-120; BareKineticEnergy.cpp:110-117)
+//   Coulomb  V = Ewald energy of the electrons (charge -1) and the ions in the
+//            periodic cell (the total of CoulombPBCAA for e-e and i-i and CoulombPBCAB
+//            for e-i; the reference's standalone sum is EwaldRef.cpp:337-398):
+//              V = sum_{i<j} q_i q_j erfc(a r_ij)/r_ij                (minimum image)
+//                + sum_{G in half space, |G| <= G_c} f(G) (|rho_e + rho_I|^2 - |rho_I|^2)
+//                + constant (ion-ion terms, self energy, background)
+//            with f(G) = 4 pi/V exp(-G^2/4a^2)/G^2 and rho_e(G) = -sum_i exp(i G.r_i).
+//
+// The cutoffs follow from a tolerance eps: a L_min/2 = G_c/(2a) = sqrt(-ln eps)
+// (eps = 1e-7 for the FP32 move loop, 1e-12 for FP64).  Sums are FP64; the terms are
+// evaluated in the move-loop precision T.  The structure factor uses per-electron
+// phase tables exp(i n 2 pi x_d / L_d), n = 0..n_max, built in shared memory for a
+// chunk of electrons; each thread owns a set of G vectors (sorted by (n1, n2, n3) so a
+// warp's table reads are mostly broadcasts) and accumulates rho_e(G) in registers.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace qmcg
+{
+
+constexpr int LE_NT  = 256; // threads per walker
+constexpr int LE_CH  = 32;  // electrons per phase-table chunk
+constexpr int LE_GPT = 12;  // G vectors per thread per pass
+
+__device__ __forceinline__ float t_erfc(float x) { return erfcf(x); }
+__device__ __forceinline__ double t_erfc(double x) { return erfc(x); }
+__device__ __forceinline__ void t_sincospi(float x, float* s, float* c) { sincospif(x, s, c); }
+__device__ __forceinline__ void t_sincospi(double x, double* s, double* c) { sincospi(x, s, c); }
+
+size_t local_energy_smem(int ne, int nmax, int tsize)
+{
+  return (size_t)tsize * (3 * (size_t)ne + (size_t)LE_CH * 3 * (nmax + 1) * 2);
+}
+
+template<typename T>
+__global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, EwaldDev<T> ew, double* out)
+{
+  extern __shared__ __align__(16) unsigned char le_smem[];
+  __shared__ double red[3 * 32];
+  const int iw = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ne = s.ne, N = s.norb, lda = s.lda, nm1 = ew.nmax + 1;
+  T* pos = reinterpret_cast<T*>(le_smem); // [3][ne], wrapped into the cell
+  T* tab = pos + 3 * ne;                   // [LE_CH][3][nm1] complex
+  const T Lc[3]   = {T(s.L[0]), T(s.L[1]), T(s.L[2])};
+  const T Li[3]   = {T(1.0 / s.L[0]), T(1.0 / s.L[1]), T(1.0 / s.L[2])};
+
+  for (int i = tid; i < ne; i += LE_NT)
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      double x = s.R[((size_t)iw * 3 + d) * s.ne_pad + i];
+      x -= s.L[d] * floor(x / s.L[d]);
+      pos[d * ne + i] = static_cast<T>(x);
+    }
+  __syncthreads();
+
+  double ke = 0, vr = 0, vk = 0;
+  // ---------------- kinetic energy: a warp per electron
+  for (int i = warp; i < ne; i += LE_NT / 32)
+  {
+    const int sp     = i < s.nup ? 0 : 1;
+    const size_t rb  = ((size_t)sp * s.nw + iw) * N + (i - sp * s.nup);
+    const T* a       = s.Ainv + rb * lda;
+    const T* g       = s.dgrad + rb * 3 * lda;
+    const T* l       = s.dlap + rb * lda;
+    T gx = 0, gy = 0, gz = 0, lp = 0;
+    for (int o = lane; o < N; o += 32)
+    {
+      const T av = a[o];
+      gx += av * g[o];
+      gy += av * g[lda + o];
+      gz += av * g[2 * lda + o];
+      lp += av * l[o];
+    }
+    double G[3] = {warp_sum(static_cast<double>(gx)), warp_sum(static_cast<double>(gy)),
+                   warp_sum(static_cast<double>(gz))};
+    double L    = warp_sum(static_cast<double>(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+    if (lane == 0)
+    {
+      if (s.has_j2)
+      {
+        const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + i;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+          G[d] += static_cast<double>(j2[(1 + d) * s.ne_pad]);
+        L += static_cast<double>(j2[4 * s.ne_pad]);
+      }
+      if (s.has_j1)
+      {
+        const T* j1 = s.J1 + (size_t)iw * 5 * s.ne_pad + i;
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+          G[d] += static_cast<double>(j1[(1 + d) * s.ne_pad]);
+        L -= static_cast<double>(j1[4 * s.ne_pad]);
+      }
+      ke += -0.5 * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + L);
+    }
+  }
+
+  // ---------------- real space: electron pairs enumerated by cyclic separation
+  // m = 1..nsep for every i (j = i + m mod ne), plus m = ne/2 for i < ne/2 when ne is even
+  const T al          = ew.alpha;
+  const int nsep      = (ne - 1) / 2;
+  const long long nfull = (long long)ne * nsep;
+  const long long npair = nfull + ((ne & 1) ? 0 : ne / 2);
+  for (long long p = tid; p < npair; p += LE_NT)
+  {
+    int i, j;
+    if (p < nfull)
+    {
+      i = (int)(p % ne);
+      j = i + 1 + (int)(p / ne);
+      if (j >= ne)
+        j -= ne;
+    }
+    else
+    {
+      i = (int)(p - nfull);
+      j = i + ne / 2;
+    }
+    T r2 = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      T dx = pos[d * ne + j] - pos[d * ne + i];
+      dx -= Lc[d] * rint(dx * Li[d]);
+      r2 += dx * dx;
+    }
+    const T r = sqrt(r2);
+    if (r > T(0))
+      vr += static_cast<double>(t_erfc(al * r) / r);
+  }
+  // electron-ion pairs
+  for (int p = tid; p < ne * s.nions; p += LE_NT)
+  {
+    const int i = p / s.nions, I = p - i * s.nions;
+    T r2 = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      T dx = s.ions[d * s.nions_pad + I] - pos[d * ne + i];
+      dx -= Lc[d] * rint(dx * Li[d]);
+      r2 += dx * dx;
+    }
+    const T r = sqrt(r2);
+    if (r > T(0))
+      vr -= static_cast<double>(ew.ion_q[I] * t_erfc(al * r) / r);
+  }
+
+  // ---------------- reciprocal space
+  for (int g0 = 0; g0 < ew.ng; g0 += LE_NT * LE_GPT)
+  {
+    T re[LE_GPT], im[LE_GPT];
+    int n1[LE_GPT], n2[LE_GPT], n3[LE_GPT];
+#pragma unroll
+    for (int q = 0; q < LE_GPT; q++)
+    {
+      const int g = g0 + tid + q * LE_NT;
+      const char4 c = g < ew.ng ? ew.gn[g] : make_char4(0, 0, 0, 0);
+      n1[q] = c.x;
+      n2[q] = c.y;
+      n3[q] = c.z;
+      re[q] = im[q] = T(0);
+    }
+    for (int c0 = 0; c0 < ne; c0 += LE_CH)
+    {
+      const int cn = min(LE_CH, ne - c0);
+      __syncthreads();
+      for (int e = tid; e < cn * 3 * nm1; e += LE_NT)
+      {
+        const int ci = e / (3 * nm1), rem = e - ci * 3 * nm1, d = rem / nm1, n = rem - d * nm1;
+        const T u    = pos[d * ne + c0 + ci] * Li[d];
+        T sv, cv;
+        t_sincospi(T(2) * T(n) * u, &sv, &cv);
+        tab[2 * e]     = cv;
+        tab[2 * e + 1] = sv;
+      }
+      __syncthreads();
+      for (int ci = 0; ci < cn; ci++)
+      {
+        const T* t = tab + (size_t)ci * 3 * nm1 * 2;
+#pragma unroll
+        for (int q = 0; q < LE_GPT; q++)
+        {
+          const int a2 = n2[q] < 0 ? -n2[q] : n2[q], a3 = n3[q] < 0 ? -n3[q] : n3[q];
+          const T c1 = t[2 * n1[q]], s1 = t[2 * n1[q] + 1];
+          const T c2 = t[2 * (nm1 + a2)], s2 = n2[q] < 0 ? -t[2 * (nm1 + a2) + 1] : t[2 * (nm1 + a2) + 1];
+          const T c3 = t[2 * (2 * nm1 + a3)], s3 = n3[q] < 0 ? -t[2 * (2 * nm1 + a3) + 1] : t[2 * (2 * nm1 + a3) + 1];
+          const T c12 = c1 * c2 - s1 * s2, s12 = s1 * c2 + c1 * s2;
+          re[q] += c12 * c3 - s12 * s3;
+          im[q] += s12 * c3 + c12 * s3;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < LE_GPT; q++)
+    {
+      const int g = g0 + tid + q * LE_NT;
+      if (g < ew.ng)
+      {
+        // rho_e = -(re, im); |rho_e|^2 + 2 Re(conj(rho_I) rho_e)
+        const double er = -static_cast<double>(re[q]), ei = -static_cast<double>(im[q]);
+        const double ir = static_cast<double>(ew.rho_ion[2 * g]), ii = static_cast<double>(ew.rho_ion[2 * g + 1]);
+        vk += static_cast<double>(ew.fg[g]) * (er * er + ei * ei + 2.0 * (ir * er + ii * ei));
+      }
+    }
+  }
+
+  double v[3] = {ke, vr, vk};
+  block_sum<double, 3>(v, red);
+  if (tid == 0)
+  {
+    const double pot     = v[1] + v[2] + ew.e_const;
+    out[iw]              = v[0] + pot;
+    out[s.nw + iw]       = v[0];
+    out[2 * s.nw + iw]   = pot;
+  }
+}
+
+template<typename T>
+cudaError_t setup_local_energy()
+{
+  return cudaFuncSetAttribute(local_energy_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template<typename T>
+cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st)
+{
+  const size_t sm = local_energy_smem(s.ne, ew.nmax, sizeof(T));
+  if (sm > 200 * 1024)
+    return cudaErrorInvalidValue;
+  local_energy_kernel<T><<<s.nw, LE_NT, sm, st>>>(s, ew, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// host: G vectors, ion structure factor and constants
+// ---------------------------------------------------------------------------
+int ewald_build(const double L[3], int ne, int nions, const double* ion_pos, const double* ion_q, double eps,
+                EwaldHost& t)
+{
+  const double vol  = L[0] * L[1] * L[2];
+  const double sq   = std::sqrt(-std::log(eps));
+  const double rcut = 0.5 * std::min(L[0], std::min(L[1], L[2]));
+  const double al   = sq / rcut;
+  const double gc   = 2 * al * sq;
+  int nm[3];
+  for (int d = 0; d < 3; d++)
+    nm[d] = (int)std::floor(gc * L[d] / (2 * M_PI));
+  const int nmax = std::max(nm[0], std::max(nm[1], nm[2]));
+  if (nmax > 127)
+    return -1;
+  t.alpha = al;
+  t.nmax  = nmax;
+  t.gn.clear();
+  t.fg.clear();
+  t.rho_ion.clear();
+  double e_ion_k = 0;
+  for (int a = 0; a <= nm[0]; a++)
+    for (int b = -nm[1]; b <= nm[1]; b++)
+      for (int c = -nm[2]; c <= nm[2]; c++)
+      {
+        if (a == 0 && (b < 0 || (b == 0 && c <= 0)))
+          continue;
+        const double g[3] = {2 * M_PI * a / L[0], 2 * M_PI * b / L[1], 2 * M_PI * c / L[2]};
+        const double g2   = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+        if (g2 > gc * gc)
+          continue;
+        const double f = 4 * M_PI / vol * std::exp(-g2 / (4 * al * al)) / g2;
+        double rr = 0, ri = 0;
+        for (int I = 0; I < nions; I++)
+        {
+          const double ph = g[0] * ion_pos[3 * I] + g[1] * ion_pos[3 * I + 1] + g[2] * ion_pos[3 * I + 2];
+          rr += ion_q[I] * std::cos(ph);
+          ri += ion_q[I] * std::sin(ph);
+        }
+        t.gn.push_back({(signed char)a, (signed char)b, (signed char)c, 0});
+        t.fg.push_back(f);
+        t.rho_ion.push_back(rr);
+        t.rho_ion.push_back(ri);
+        e_ion_k += f * (rr * rr + ri * ri);
+      }
+  // ion-ion real-space part over the neighbouring images
+  double e_ion_r = 0;
+  for (int I = 0; I < nions; I++)
+    for (int J = 0; J < I; J++)
+      for (int x = -1; x <= 1; x++)
+        for (int y = -1; y <= 1; y++)
+          for (int z = -1; z <= 1; z++)
+          {
+            double d[3] = {ion_pos[3 * I] - ion_pos[3 * J], ion_pos[3 * I + 1] - ion_pos[3 * J + 1],
+                           ion_pos[3 * I + 2] - ion_pos[3 * J + 2]};
+            for (int k = 0; k < 3; k++)
+              d[k] -= L[k] * std::round(d[k] / L[k]);
+            d[0] += x * L[0];
+            d[1] += y * L[1];
+            d[2] += z * L[2];
+            const double r = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            e_ion_r += ion_q[I] * ion_q[J] * std::erfc(al * r) / r;
+          }
+  double q2 = ne, qt = -ne;
+  for (int I = 0; I < nions; I++)
+  {
+    q2 += ion_q[I] * ion_q[I];
+    qt += ion_q[I];
+  }
+  // self energy -a/sqrt(pi) sum q^2, background -pi Q^2/(2 a^2 V)
+  t.e_const = e_ion_r + e_ion_k - al / std::sqrt(M_PI) * q2 - M_PI * qt * qt / (2 * al * al * vol);
+  return 0;
+}
+
+template cudaError_t setup_local_energy<float>();
+template cudaError_t setup_local_energy<double>();
+template cudaError_t launch_local_energy<float>(const DevState<float>&, const EwaldDev<float>&, double*, cudaStream_t);
+template cudaError_t launch_local_energy<double>(const DevState<double>&, const EwaldDev<double>&, double*,
+                                                 cudaStream_t);
+
+} // namespace qmcg

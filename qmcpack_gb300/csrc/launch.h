@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <string>
+#include <vector>
 #include "common.cuh"
 
 namespace qmcg
@@ -73,6 +74,23 @@ inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* 
   f.w          = W;
   return f;
 }
+
+// local energy (energy.cu)
+struct EwaldHost
+{
+  double alpha = 0, e_const = 0;
+  int nmax     = 0;
+  std::vector<char4> gn;
+  std::vector<double> fg, rho_ion;
+};
+int ewald_build(const double L[3], int ne, int nions, const double* ion_pos, const double* ion_q, double eps,
+                EwaldHost& t);
+size_t local_energy_smem(int ne, int nmax, int tsize);
+template<typename T>
+cudaError_t setup_local_energy();
+// out: [3][nw] doubles = local energy, kinetic, potential
+template<typename T>
+cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st);
 
 // recompute path (recompute_kernels.cu)
 template<typename T>

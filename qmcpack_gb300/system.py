@@ -75,6 +75,7 @@ class System:
     j1_cusp: np.ndarray          # (n_ion_species,)
     j2_params: np.ndarray        # (2, j2_size): same spin, opposite spin
     j2_cusp: np.ndarray          # (2,)
+    ion_charges: np.ndarray = None  # (n_ion_species,) valence charge; neutral cell by default
 
     @property
     def n_elec(self) -> int:
@@ -134,7 +135,8 @@ def make_system(spec: SystemSpec | str, seed: int = 2024) -> System:
                   ion_species=np.zeros(spec.n_ions, np.int32), n_ion_species=1,
                   grid=np.full(3, g, np.int32), norb=norb, npad=npad, coefs=coefs,
                   j1_params=j1, j1_cusp=np.zeros(1),
-                  j2_params=j2, j2_cusp=np.array([-0.25, -0.5]))
+                  j2_params=j2, j2_cusp=np.array([-0.25, -0.5]),
+                  ion_charges=np.array([float(spec.n_up + spec.n_dn) / spec.n_ions]))
 
 
 def make_walkers(system: System, nw: Optional[int] = None, seed: int = 7) -> np.ndarray:

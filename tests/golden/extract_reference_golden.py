@@ -125,6 +125,28 @@ def main():
         "log_after_accept_1": checks(first, r"std::real\(ddb.get_log_value\(\)\)")[0][1],
     }
 
+    # --- standalone Ewald sums: src/QMCHamiltonians/tests/test_EwaldRef.cpp
+    rel = "src/QMCHamiltonians/tests/test_EwaldRef.cpp"
+    t = read(root, rel)
+    cases = []
+    for sec in re.split(r"SECTION\(", t)[1:]:
+        name = re.match(r'"([^"]+)"', sec).group(1)
+        A = [float(x) for x in re.search(r"A = \{([^}]+)\};", sec).group(1).split(",")]
+        n = int(re.search(r"num_centers = (\d+);", sec).group(1))
+        q0 = float(re.search(r"Q\.resize\(num_centers, (" + NUM + r")\);", sec).group(1))
+        Q = [q0] * n
+        loop = re.search(r"for \(int i = 0; i < (\d+); i\+\+\)\s*Q\[i\] = (" + NUM + r");", sec)
+        if loop:
+            for i in range(int(loop.group(1))):
+                Q[i] = float(loop.group(2))
+        R = [None] * n
+        for i, x, y, z in re.findall(r"R\[(\d+)\]\s*= \{(" + NUM + r"), (" + NUM + r"), (" + NUM + r")\};", sec):
+            R[int(i)] = [float(x), float(y), float(z)]
+        assert all(r is not None for r in R)
+        val = float(re.search(r"CHECK\(Approx\(Vii_ref\) == (" + NUM + r")\);", sec).group(1))
+        cases.append({"name": name, "A": A, "Q": Q, "R": R, "energy": val})
+    g["ewald_ref"] = {"file": rel, "approx_epsilon": 1.1920929e-05, "cases": cases}
+
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.json")
     with open(out, "w") as f:
         json.dump(g, f, indent=1)

