@@ -202,6 +202,48 @@ int qmcg_mw_evaluate_local_energy(qmcg_crowd crowd, double* e_local, double* kin
 int qmcg_vmc_sweeps_measure(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, double* e_local,
                             double* kinetic, qmcg_sweep_stats* stats);
 
+/* ---------------------------------------------------------------- learned MH proposal
+ * No reference counterpart: a new proposal for the same exact Metropolis-Hastings step
+ * (it replaces the drift-diffusion move of VMCBatched::advanceWalkers,
+ * src/QMCDrivers/VMC/VMCBatched.cpp:106-177, and the Green's-function ratio of
+ * QMCDriverNew::computeLogGreensFunction, src/QMCDrivers/QMCDriverNew.h:282-296).
+ * For electron i a per-electron MLP (51 inputs: displacements to the 8 nearest other
+ * electrons and the 8 nearest ions, scaled by 1/2 bohr, and the UNR drift / sqrt(tau);
+ * three tanh layers of width 128; outputs mu, s in R^3) proposes
+ *   r' = r + drift(R) + sqrt(tau) mu + sqrt(tau) exp(s) xi,  xi ~ N(0, 1),
+ * with mu clipped to [-4, 4] and s to [-3, 2], and the move is accepted with
+ * probability min(1, |psi(R')/psi(R)|^2 q(r|R') / q(r'|R)).  Inference runs on the
+ * tensor cores with BF16 weights and FP32 accumulation; training maximises the
+ * expected squared jump distance with hand-written backward and Adam kernels on FP32
+ * master parameters.  With the last layer zero the proposal is drift-diffusion. */
+#define QMCG_PROPOSAL_NUM_PARAMS 43408 /* W1[128][64] b1[128] W2[128][128] b2 W3 b3 W4[16][128] b4[16];
+                                          W1 columns >= 51 and W4/b4 rows >= 6 are kept at zero */
+#define QMCG_PROPOSAL_NUM_INPUTS 64    /* 51 features + 13 zero columns */
+
+/* Allocates the network on the crowd's device and initialises it from `seed`:
+ * hidden layers uniform(-a, a), a = init_scale / sqrt(fan_in); output layer zero. */
+int qmcg_proposal_init(qmcg_crowd crowd, uint64_t seed, double init_scale);
+/* FP32 master parameters, QMCG_PROPOSAL_NUM_PARAMS floats (set resets the optimiser). */
+int qmcg_proposal_get_params(qmcg_crowd crowd, float* params);
+int qmcg_proposal_set_params(qmcg_crowd crowd, const float* params);
+/* The network on caller inputs x [rows][64] (rounded to BF16): out [rows][6] = (mu, s)
+ * before clipping; hidden (may be NULL) [3][rows][128] = the BF16 post-activations. */
+int qmcg_proposal_forward(qmcg_crowd crowd, int rows, const float* x, float* out, float* hidden);
+/* Gradient of sum_r dout[r] . out[r] with respect to the parameters (the training
+ * backward pass on caller inputs): grad [QMCG_PROPOSAL_NUM_PARAMS]. */
+int qmcg_proposal_backward(qmcg_crowd crowd, int rows, const float* x, const float* dout, float* grad);
+/* Features of electron iat for every walker, x [num_walkers][64]: at the current
+ * position (after qmcg_mw_eval_grad) or at the proposed one (at_proposed = 1, after
+ * qmcg_mw_calc_ratio_grad). */
+int qmcg_proposal_features(qmcg_crowd crowd, int iat, int at_proposed, float* x);
+/* Sweeps with the learned proposal (rng_mode must be 1; path is ignored: staged
+ * per-electron kernels in one CUDA graph per sweep).  train != 0 adds one Adam step
+ * (learning rate lr) per electron move over the crowd's walkers.  e_local (may be NULL)
+ * [num_sweeps][num_walkers] as in qmcg_vmc_sweeps_measure; train_stats (may be NULL)
+ * [2] = mean alpha |r' - r|^2 and mean acceptance probability over the training moves. */
+int qmcg_vmc_sweeps_learned(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, int train, double lr,
+                            double* e_local, qmcg_sweep_stats* stats, double* train_stats);
+
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
 

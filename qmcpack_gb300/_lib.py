@@ -20,7 +20,11 @@ EXPORTS = [
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
     "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_ex", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
     "qmcg_profile_sweep", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
+    "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
+    "qmcg_proposal_backward", "qmcg_proposal_features", "qmcg_vmc_sweeps_learned",
 ]
+PROPOSAL_NUM_PARAMS = 43408
+_fp = C.POINTER(C.c_float)
 
 
 class SystemDesc(C.Structure):
@@ -90,6 +94,14 @@ def load(path: str = LIB_PATH):
         "qmcg_profile_sweep": [vp, C.c_int, _dp],
         "qmcg_mw_evaluate_local_energy": [vp, _dp, _dp, _dp],
         "qmcg_vmc_sweeps_measure": [vp, C.POINTER(SweepParams), C.c_int, _dp, _dp, C.POINTER(SweepStats)],
+        "qmcg_proposal_init": [vp, C.c_uint64, C.c_double],
+        "qmcg_proposal_get_params": [vp, _fp],
+        "qmcg_proposal_set_params": [vp, _fp],
+        "qmcg_proposal_forward": [vp, C.c_int, _fp, _fp, _fp],
+        "qmcg_proposal_backward": [vp, C.c_int, _fp, _fp, _fp],
+        "qmcg_proposal_features": [vp, C.c_int, C.c_int, _fp],
+        "qmcg_vmc_sweeps_learned": [vp, C.POINTER(SweepParams), C.c_int, C.c_int, C.c_double, _dp,
+                                    C.POINTER(SweepStats), _dp],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

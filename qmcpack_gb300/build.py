@@ -15,9 +15,9 @@ ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqmcg.so")
 
-SOURCES = ["capi.cu", "move_kernels.cu", "recompute_kernels.cu", "sweep_kernel.cu", "flush_kernels.cu", "flush_tc.cu", "energy.cu",
+SOURCES = ["capi.cu", "move_kernels.cu", "recompute_kernels.cu", "sweep_kernel.cu", "flush_kernels.cu", "flush_tc.cu", "energy.cu", "learned.cu",
            "noalloc.cu"]
-HEADERS = ["common.cuh", "spline.cuh", "launch.h"]
+HEADERS = ["common.cuh", "spline.cuh", "launch.h", "tc.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
          "--expt-relaxed-constexpr", "-I", CSRC, "-I", os.path.join(ROOT, "include")]

@@ -19,6 +19,7 @@ from .system import System
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
+_fp = C.POINTER(C.c_float)
 
 
 def _d(a):
@@ -191,6 +192,54 @@ class Crowd:
         check(self.L.qmcg_vmc_sweeps_measure(self.handle, C.byref(p), nsweeps, _p(el), _p(ke), C.byref(st)))
         self.last_repaired = st.repaired
         return st.accepted, st.rejected, el, ke
+
+    # ---- learned MH proposal
+    def proposal_init(self, seed: int = 1, init_scale: float = 1.0):
+        check(self.L.qmcg_proposal_init(self.handle, seed, init_scale))
+
+    def proposal_params(self) -> np.ndarray:
+        p = np.zeros(_lib.PROPOSAL_NUM_PARAMS, np.float32)
+        check(self.L.qmcg_proposal_get_params(self.handle, _p(p, _fp)))
+        return p
+
+    def set_proposal_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == _lib.PROPOSAL_NUM_PARAMS
+        check(self.L.qmcg_proposal_set_params(self.handle, _p(p, _fp)))
+
+    def proposal_forward(self, x, with_hidden: bool = False):
+        x = np.ascontiguousarray(x, np.float32)
+        rows = x.shape[0]
+        out = np.zeros((rows, 6), np.float32)
+        hid = np.zeros((3, rows, 128), np.float32) if with_hidden else None
+        check(self.L.qmcg_proposal_forward(self.handle, rows, _p(x, _fp), _p(out, _fp),
+                                           _p(hid, _fp) if hid is not None else None))
+        return (out, hid) if with_hidden else out
+
+    def proposal_backward(self, x, dout):
+        x = np.ascontiguousarray(x, np.float32)
+        d = np.ascontiguousarray(dout, np.float32)
+        g = np.zeros(_lib.PROPOSAL_NUM_PARAMS, np.float32)
+        check(self.L.qmcg_proposal_backward(self.handle, x.shape[0], _p(x, _fp), _p(d, _fp), _p(g, _fp)))
+        return g
+
+    def proposal_features(self, iat: int, at_proposed: bool = False):
+        x = np.zeros((self.nw, 64), np.float32)
+        check(self.L.qmcg_proposal_features(self.handle, iat, int(at_proposed), _p(x, _fp)))
+        return x
+
+    def vmc_sweeps_learned(self, nsweeps: int, tau: float, seed: int, train: bool = False, lr: float = 1e-3,
+                           measure: bool = False, use_drift: bool = True, recompute_every: int = 0, flush: int = 0):
+        """(accepted, rejected, E_L[nsweeps][nw] or None, (mean alpha|dr|^2, mean alpha))"""
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
+                        recompute_every=recompute_every, path=1, flush=flush)
+        st = SweepStats()
+        el = np.zeros((nsweeps, self.nw)) if measure else None
+        ts = np.zeros(2)
+        check(self.L.qmcg_vmc_sweeps_learned(self.handle, C.byref(p), nsweeps, int(train), lr,
+                                             _p(el) if el is not None else None, C.byref(st), _p(ts)))
+        self.last_repaired = st.repaired
+        return st.accepted, st.rejected, el, (float(ts[0]), float(ts[1]))
 
     def vmc_sweeps_async(self, nsweeps: int):
         check(self.L.qmcg_vmc_sweeps_async(self.handle, nsweeps))

@@ -82,6 +82,25 @@ struct DeviceArena
   }
 };
 
+// BF16 <-> FP32 on the host: round to nearest even (NaN kept quiet)
+static uint16_t f2bf(float f)
+{
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u)
+    return static_cast<uint16_t>((u >> 16) | 0x40u);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return static_cast<uint16_t>(u >> 16);
+}
+
+static float bf2f(uint16_t h)
+{
+  const uint32_t u = static_cast<uint32_t>(h) << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
 // ---------------------------------------------------------------------------
 // system
 // ---------------------------------------------------------------------------
@@ -382,6 +401,13 @@ struct qmcg_crowd_s
   virtual int profile_sweep(int n, double* out)          = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
   virtual int local_energy(double* el, double* ke, double* vp) = 0;
+  virtual int proposal_init(uint64_t seed, double scale)  = 0;
+  virtual int proposal_params(float* get, const float* set) = 0;
+  virtual int proposal_forward(int rows, const float* x, float* out, float* hidden) = 0;
+  virtual int proposal_backward(int rows, const float* x, const float* dout, float* grad) = 0;
+  virtual int proposal_features(int iat, int at_proposed, float* x) = 0;
+  virtual int sweeps_learned(const qmcg_sweep_params* p, int n, int train, double lr, double* el,
+                             qmcg_sweep_stats* st, double* tstats) = 0;
   virtual int sweeps_measure(const qmcg_sweep_params* p, int n, double* el, double* ke, qmcg_sweep_stats* st) = 0;
 };
 
@@ -409,6 +435,21 @@ struct Crowd final : qmcg_crowd_s
   uint64_t graph_seed = 0;
   int sweeps_since_recompute = 0;
   int recompute_every        = 0;
+  // learned MH proposal
+  struct Learned
+  {
+    bool ready = false;
+    MlpTrain t{};
+    float* out    = nullptr;
+    float* aux    = nullptr;
+    int* err      = nullptr;
+    double* stats = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int g_train = -1, g_drift = -1, g_flush = -1;
+    double g_tau = 0;
+    uint64_t g_seed = 0;
+    float g_lr = 0;
+  } ln;
   EwaldDev<T> ew{};
   double* e_out  = nullptr; // [3][nw] local energy, kinetic, potential
   double* e_hist = nullptr; // [e_hist_cap][2][nw] per-sweep local and kinetic energies
@@ -424,6 +465,8 @@ struct Crowd final : qmcg_crowd_s
       cudaFreeHost(unif_h);
     if (e_hist)
       cudaFree(e_hist);
+    if (ln.graph)
+      cudaGraphExecDestroy(ln.graph);
     if (stream)
       cudaStreamDestroy(stream);
   }
@@ -972,6 +1015,331 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 
+  // ------------------------------------------------------------------ learned proposal
+  int proposal_init(uint64_t seed, double scale) override
+  {
+    const size_t rows = 2 * (size_t)nw;
+    if (!ln.ready)
+    {
+      CUDA_TRY(setup_learned<T>());
+      CUDA_TRY(mem.alloc(&ln.t.params, MP_N));
+      CUDA_TRY(mem.alloc(&ln.t.m, MP_N));
+      CUDA_TRY(mem.alloc(&ln.t.v, MP_N));
+      CUDA_TRY(mem.alloc(&ln.t.grad, MP_N));
+      CUDA_TRY(mem.alloc(&ln.t.wimg, (size_t)ML_WIMG_BYTES));
+      CUDA_TRY(mem.alloc(&ln.t.x, rows * ML_IN));
+      CUDA_TRY(mem.alloc(&ln.t.hid, 3 * rows * ML_H));
+      CUDA_TRY(mem.alloc(&ln.t.g4, rows * 8));
+      CUDA_TRY(mem.alloc(&ln.t.delta, 3 * rows * ML_H));
+      CUDA_TRY(mem.alloc(&ln.t.step, 1));
+      CUDA_TRY(mem.alloc(&ln.out, rows * 8));
+      CUDA_TRY(mem.alloc(&ln.aux, (size_t)nw * ML_AUX));
+      CUDA_TRY(mem.alloc(&ln.err, 1));
+      CUDA_TRY(mem.alloc(&ln.stats, 2));
+    }
+    // uniform(-a, a) with a = scale / sqrt(fan_in) for the hidden layers; the output
+    // layer starts at zero, so the initial proposal is drift-diffusion
+    std::vector<float> h(MP_N, 0.f);
+    std::mt19937_64 g(seed);
+    std::uniform_real_distribution<double> u(-1.0, 1.0);
+    for (int n = 0; n < ML_H; n++)
+      for (int k = 0; k < ML_NIN; k++)
+        h[MP_W1 + n * ML_IN + k] = static_cast<float>(scale / std::sqrt((double)ML_NIN) * u(g));
+    for (int l = 0; l < 2; l++)
+      for (int i = 0; i < ML_H * ML_H; i++)
+        h[(l ? MP_W3 : MP_W2) + i] = static_cast<float>(scale / std::sqrt((double)ML_H) * u(g));
+    ln.ready = true;
+    return proposal_params(nullptr, h.data());
+  }
+
+  int proposal_params(float* get, const float* set) override
+  {
+    if (!ln.ready)
+      return fail(QMCG_ERR_STATE, "proposal not initialised (qmcg_proposal_init)");
+    if (set)
+    {
+      CUDA_TRY(cudaMemcpyAsync(ln.t.params, set, MP_N * sizeof(float), cudaMemcpyHostToDevice, stream));
+      CUDA_TRY(cudaMemsetAsync(ln.t.m, 0, MP_N * sizeof(float), stream));
+      CUDA_TRY(cudaMemsetAsync(ln.t.v, 0, MP_N * sizeof(float), stream));
+      CUDA_TRY(cudaMemsetAsync(ln.t.step, 0, sizeof(int), stream));
+      CUDA_TRY(launch_mlp_pack(ln.t.params, ln.t.wimg, stream));
+    }
+    if (get)
+      CUDA_TRY(cudaMemcpyAsync(get, ln.t.params, MP_N * sizeof(float), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  MlpArgs mlp_args(int rows, const __nv_bfloat16* x, __nv_bfloat16* hid, int hid_rows, int hid_row0, float* out)
+  {
+    MlpArgs a;
+    a.rows     = rows;
+    a.x        = x;
+    a.wimg     = ln.t.wimg;
+    a.params   = ln.t.params;
+    a.hid      = hid;
+    a.hid_rows = hid_rows;
+    a.hid_row0 = hid_row0;
+    a.out      = out;
+    a.aux      = ln.aux;
+    a.err      = ln.err;
+    return a;
+  }
+
+  // the network on caller inputs x [rows][64] (rounded to BF16): out [rows][6] and
+  // optionally the hidden activations [3][rows][128]
+  int proposal_forward(int rows, const float* x, float* out, float* hidden) override
+  {
+    if (!ln.ready)
+      return fail(QMCG_ERR_STATE, "proposal not initialised (qmcg_proposal_init)");
+    if (rows <= 0 || !x || !out)
+      return fail(QMCG_ERR_ARG, "bad arguments");
+    return mlp_host_pass(rows, x, out, hidden, nullptr, nullptr);
+  }
+
+  int proposal_backward(int rows, const float* x, const float* dout, float* grad) override
+  {
+    if (!ln.ready)
+      return fail(QMCG_ERR_STATE, "proposal not initialised (qmcg_proposal_init)");
+    if (rows <= 0 || !x || !dout || !grad)
+      return fail(QMCG_ERR_ARG, "bad arguments");
+    return mlp_host_pass(rows, x, nullptr, nullptr, dout, grad);
+  }
+
+  int mlp_host_pass(int rows, const float* x, float* out, float* hidden, const float* dout, float* grad)
+  {
+    DeviceArena tmp;
+    __nv_bfloat16 *dx, *dh;
+    float *dout_d, *g4, *delta, *dgrad;
+    CUDA_TRY(tmp.alloc(&dx, (size_t)rows * ML_IN));
+    CUDA_TRY(tmp.alloc(&dh, (size_t)3 * rows * ML_H));
+    CUDA_TRY(tmp.alloc(&dout_d, (size_t)rows * 8));
+    std::vector<uint16_t> xb((size_t)rows * ML_IN);
+    for (size_t i = 0; i < xb.size(); i++)
+      xb[i] = f2bf(x[i]);
+    CUDA_TRY(cudaMemcpy(dx, xb.data(), xb.size() * 2, cudaMemcpyHostToDevice));
+    MlpArgs a = mlp_args(rows, dx, dh, rows, 0, dout_d);
+    CUDA_TRY(launch_mlp_forward<T>(a, s, 0, 0, stream));
+    int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, ln.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (err)
+    {
+      CUDA_TRY(cudaMemset(ln.err, 0, sizeof(int)));
+      return fail(QMCG_ERR_CUDA, "proposal network: a tensor-core wait timed out");
+    }
+    if (out)
+    {
+      std::vector<float> o((size_t)rows * 8);
+      CUDA_TRY(cudaMemcpy(o.data(), dout_d, o.size() * 4, cudaMemcpyDeviceToHost));
+      for (int r = 0; r < rows; r++)
+        for (int q = 0; q < ML_NOUT; q++)
+          out[(size_t)r * ML_NOUT + q] = o[(size_t)r * 8 + q];
+    }
+    if (hidden)
+    {
+      std::vector<uint16_t> hb((size_t)3 * rows * ML_H);
+      CUDA_TRY(cudaMemcpy(hb.data(), dh, hb.size() * 2, cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < hb.size(); i++)
+        hidden[i] = bf2f(hb[i]);
+    }
+    if (dout)
+    {
+      CUDA_TRY(tmp.alloc(&g4, (size_t)rows * 8));
+      CUDA_TRY(tmp.alloc(&delta, (size_t)3 * rows * ML_H));
+      CUDA_TRY(tmp.alloc(&dgrad, (size_t)MP_N));
+      std::vector<float> gh((size_t)rows * 8, 0.f);
+      for (int r = 0; r < rows; r++)
+        for (int q = 0; q < ML_NOUT; q++)
+          gh[(size_t)r * 8 + q] = dout[(size_t)r * ML_NOUT + q];
+      CUDA_TRY(cudaMemcpy(g4, gh.data(), gh.size() * 4, cudaMemcpyHostToDevice));
+      MlpTrain t = ln.t;
+      t.x        = dx;
+      t.hid      = dh;
+      t.g4       = g4;
+      t.delta    = delta;
+      t.grad     = dgrad;
+      CUDA_TRY(launch_mlp_backward(t, rows, stream));
+      CUDA_TRY(cudaStreamSynchronize(stream));
+      CUDA_TRY(cudaMemcpy(grad, dgrad, MP_N * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    return QMCG_OK;
+  }
+
+  // features of electron iat for every walker at its current position (after
+  // mw_evalGrad) or at the proposed one (after mw_calcRatioGrad): x [nw][64]
+  int proposal_features(int iat, int at_proposed, float* x) override
+  {
+    if (!ln.ready)
+      return fail(QMCG_ERR_STATE, "proposal not initialised (qmcg_proposal_init)");
+    int rc = check_iat(iat);
+    if (rc)
+      return rc;
+    CUDA_TRY(launch_features<T>(s, iat, at_proposed ? 1 : 0, ln.t.x, stream));
+    std::vector<uint16_t> xb((size_t)nw * ML_IN);
+    CUDA_TRY(cudaMemcpyAsync(xb.data(), ln.t.x, xb.size() * 2, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < xb.size(); i++)
+      x[i] = bf2f(xb[i]);
+    return QMCG_OK;
+  }
+
+  // one sweep with the learned proposal (staged per-electron kernels), optionally
+  // with one training step per electron
+  int enqueue_sweep_learned(bool train, float lr)
+  {
+    int d[2] = {0, 0};
+    const int rows = 2 * nw;
+    __nv_bfloat16* xf = ln.t.x;
+    __nv_bfloat16* xr = ln.t.x + (size_t)nw * ML_IN;
+    const MlpArgs af  = mlp_args(nw, xf, train ? ln.t.hid : nullptr, rows, 0, nullptr);
+    const MlpArgs ar  = mlp_args(nw, xr, train ? ln.t.hid : nullptr, rows, nw, nullptr);
+    for (int iat = 0; iat < sys->ne; iat++)
+    {
+      const int sp = spin_of(iat);
+      CUDA_TRY(launch_propose<T>(s, iat, d[sp], 0, stream));
+      CUDA_TRY(launch_features<T>(s, iat, 0, xf, stream));
+      CUDA_TRY(launch_mlp_forward<T>(af, s, iat, 1, stream));
+      CUDA_TRY(launch_ratio<T>(s, iat, 0, stream));
+      CUDA_TRY(launch_features<T>(s, iat, 1, xr, stream));
+      CUDA_TRY(launch_mlp_forward<T>(ar, s, iat, 2, stream));
+      if (train)
+      {
+        CUDA_TRY(launch_mlp_loss_grad<T>(s, ln.aux, ln.t.g4, ln.stats, stream));
+        CUDA_TRY(launch_mlp_backward(ln.t, rows, stream));
+        CUDA_TRY(launch_mlp_adam(ln.t, lr, stream));
+      }
+      CUDA_TRY(launch_accept<T>(s, iat, d[sp], 1, stream));
+      if (k > 1)
+      {
+        d[sp]++;
+        if (d[sp] == k)
+        {
+          CUDA_TRY(launch_flush_choice(sp, k));
+          d[sp] = 0;
+        }
+      }
+    }
+    for (int sp = 0; sp < 2; sp++)
+      if (k > 1 && d[sp] > 0)
+        CUDA_TRY(launch_flush_choice(sp, d[sp]));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
+    bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
+    CUDA_TRY(cudaGetLastError());
+    return QMCG_OK;
+  }
+
+  int sweeps_learned(const qmcg_sweep_params* p, int n, int train, double lr, double* el, qmcg_sweep_stats* st,
+                     double* tstats) override
+  {
+    if (!ln.ready)
+      return fail(QMCG_ERR_STATE, "proposal not initialised (qmcg_proposal_init)");
+    if (!p || n < 0 || !(p->tau > 0) || p->rng_mode != 1)
+      return fail(QMCG_ERR_ARG, "learned sweeps need tau > 0 and the device random numbers (rng_mode 1)");
+    if (dc[0] || dc[1])
+    {
+      int rc = complete();
+      if (rc)
+        return rc;
+    }
+    const float flr = static_cast<float>(lr);
+    if (!ln.graph || ln.g_train != (train ? 1 : 0) || ln.g_tau != p->tau || ln.g_seed != p->seed ||
+        ln.g_lr != flr || ln.g_flush != p->flush || ln.g_drift != p->use_drift)
+    {
+      if (ln.graph)
+      {
+        cudaGraphExecDestroy(ln.graph);
+        ln.graph = nullptr;
+      }
+      // the sweep graph of the plain path must be rebuilt after this
+      if (graph)
+      {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
+      }
+      s.rng_mode  = 1;
+      s.use_drift = p->use_drift;
+      s.tau       = p->tau;
+      s.seed      = p->seed;
+      flush_kind  = p->flush;
+      cudaGraph_t g;
+      CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      int rc        = enqueue_sweep_learned(train != 0, flr);
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (rc)
+        return rc;
+      if (e != cudaSuccess)
+        return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ln.graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess)
+        return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+      ln.g_train = train ? 1 : 0;
+      ln.g_tau   = p->tau;
+      ln.g_seed  = p->seed;
+      ln.g_lr    = flr;
+      ln.g_flush = p->flush;
+      ln.g_drift = p->use_drift;
+    }
+    if (el)
+    {
+      const size_t need = (size_t)std::max(n, 1) * 3 * nw;
+      if (need > e_hist_cap)
+      {
+        if (e_hist)
+          CUDA_TRY(cudaFree(e_hist));
+        e_hist = nullptr;
+        CUDA_TRY(cudaMalloc(&e_hist, need * sizeof(double)));
+        e_hist_cap = need;
+      }
+    }
+    recompute_every = p->recompute_every;
+    CUDA_TRY(cudaMemsetAsync(s.counters, 0, 3 * sizeof(unsigned long long), stream));
+    CUDA_TRY(cudaMemsetAsync(ln.stats, 0, 2 * sizeof(double), stream));
+    for (int it = 0; it < n; it++)
+    {
+      CUDA_TRY(cudaGraphLaunch(ln.graph, stream));
+      if (el)
+        CUDA_TRY(launch_local_energy<T>(s, ew, e_hist + (size_t)it * 3 * nw, stream));
+      sweeps_since_recompute++;
+      if (p->recompute_every > 0 && sweeps_since_recompute >= p->recompute_every)
+      {
+        int rc = recompute_device();
+        if (rc)
+          return rc;
+        sweeps_since_recompute = 0;
+      }
+    }
+    double hs2[2];
+    int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(hs2, ln.stats, sizeof(hs2), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(&err, ln.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    std::vector<double> h;
+    if (el)
+    {
+      h.resize((size_t)n * 3 * nw);
+      CUDA_TRY(cudaMemcpyAsync(h.data(), e_hist, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    }
+    int rc = sync(st);
+    if (rc)
+      return rc;
+    if (err)
+    {
+      CUDA_TRY(cudaMemset(ln.err, 0, sizeof(int)));
+      return fail(QMCG_ERR_CUDA, "proposal network: a tensor-core wait timed out");
+    }
+    if (el)
+      for (int it = 0; it < n; it++)
+        std::copy_n(h.data() + (size_t)it * 3 * nw, nw, el + (size_t)it * nw);
+    if (tstats)
+    {
+      const double moves = (double)n * sys->ne * nw;
+      tstats[0]          = train ? hs2[0] / moves : 0.0; // mean alpha |r' - r|^2 over training moves
+      tstats[1]          = train ? hs2[1] / moves : 0.0; // mean alpha
+    }
+    return QMCG_OK;
+  }
+
   int run_sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log, bool measure)
   {
     if (!p || n < 0 || !(p->tau > 0) || (p->rng_mode != 0 && p->rng_mode != 1))
@@ -1338,6 +1706,41 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
   CROWD_CALL(c, sweeps(p, n, st, acc));
 }
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
+extern "C" int qmcg_proposal_init(qmcg_crowd c, uint64_t seed, double init_scale)
+{
+  CROWD_CALL(c, proposal_init(seed, init_scale));
+}
+extern "C" int qmcg_proposal_get_params(qmcg_crowd c, float* params)
+{
+  if (!params)
+    return fail(QMCG_ERR_ARG, "null output");
+  CROWD_CALL(c, proposal_params(params, nullptr));
+}
+extern "C" int qmcg_proposal_set_params(qmcg_crowd c, const float* params)
+{
+  if (!params)
+    return fail(QMCG_ERR_ARG, "null input");
+  CROWD_CALL(c, proposal_params(nullptr, params));
+}
+extern "C" int qmcg_proposal_forward(qmcg_crowd c, int rows, const float* x, float* out, float* hidden)
+{
+  CROWD_CALL(c, proposal_forward(rows, x, out, hidden));
+}
+extern "C" int qmcg_proposal_backward(qmcg_crowd c, int rows, const float* x, const float* dout, float* grad)
+{
+  CROWD_CALL(c, proposal_backward(rows, x, dout, grad));
+}
+extern "C" int qmcg_proposal_features(qmcg_crowd c, int iat, int at_proposed, float* x)
+{
+  if (!x)
+    return fail(QMCG_ERR_ARG, "null output");
+  CROWD_CALL(c, proposal_features(iat, at_proposed, x));
+}
+extern "C" int qmcg_vmc_sweeps_learned(qmcg_crowd c, const qmcg_sweep_params* p, int n, int train, double lr,
+                                       double* e_local, qmcg_sweep_stats* st, double* train_stats)
+{
+  CROWD_CALL(c, sweeps_learned(p, n, train, lr, e_local, st, train_stats));
+}
 extern "C" int qmcg_mw_evaluate_local_energy(qmcg_crowd c, double* el, double* ke, double* vp)
 {
   CROWD_CALL(c, local_energy(el, ke, vp));

@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "launch.h"
+#include "tc.cuh"
 
 namespace qmcg
 {
@@ -28,8 +29,6 @@ constexpr int TC_NT    = 128; // 4 warps: warp w owns TMEM lanes 32w..32w+31
 constexpr int TC_KC    = 64;  // K chunk of the first product
 // TMEM columns allocated: T1 in [0, 32), P in [64, 64 + n_pad); a power of two
 __host__ __device__ constexpr int tc_cols(int npad) { return 64 + npad <= 256 ? 256 : 512; }
-constexpr long long TC_WAIT_LIMIT = 1ll << 26;
-
 // byte offset of element (r, k) of an R x KC tile in the K-major core-matrix layout
 __device__ __forceinline__ uint32_t cm_off(int r, int k, int kc)
 {
@@ -51,11 +50,6 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int m, int n)
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
 __device__ __forceinline__ float tf32_hi(float x)
 {
   uint32_t r;
@@ -69,46 +63,6 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
                "l"(a), "l"(b), "r"(idesc), "r"(accum)
                : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar)
-{
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
-               : "memory");
-}
-
-// bounded wait on an mbarrier phase; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
-{
-  for (long long it = 0; it < TC_WAIT_LIMIT; it++)
-  {
-    uint32_t done;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}\n"
-                 : "=r"(done)
-                 : "r"(mbar), "r"(parity)
-                 : "memory");
-    if (done)
-      return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-  uint32_t r[32];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-               "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                 "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                 "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                 "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++)
-    v[i] = __uint_as_float(r[i]);
 }
 
 // shared memory plan (bytes), all tiles 1024-byte aligned

@@ -1,5 +1,6 @@
 // Host-side launch interface between the translation units of the library.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <string>
 #include <vector>
@@ -91,6 +92,57 @@ cudaError_t setup_local_energy();
 // out: [3][nw] doubles = local energy, kinetic, potential
 template<typename T>
 cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st);
+
+// learned MH proposal (learned.cu): MLP 51 -> 128 -> 128 -> 128 -> 6, inputs padded
+// to 64 and outputs to 16 for the tensor cores
+constexpr int ML_IN = 64, ML_NIN = 51, ML_H = 128, ML_OUT = 16, ML_NOUT = 6, ML_M = 128, ML_AUX = 24;
+// FP32 master parameters, flat: W1 [128][64], b1 [128], W2 [128][128], b2, W3, b3, W4 [16][128], b4 [16]
+constexpr int MP_W1 = 0;
+constexpr int MP_B1 = MP_W1 + ML_H * ML_IN;
+constexpr int MP_W2 = MP_B1 + ML_H;
+constexpr int MP_B2 = MP_W2 + ML_H * ML_H;
+constexpr int MP_W3 = MP_B2 + ML_H;
+constexpr int MP_B3 = MP_W3 + ML_H * ML_H;
+constexpr int MP_W4 = MP_B3 + ML_H;
+constexpr int MP_B4 = MP_W4 + ML_OUT * ML_H;
+constexpr int MP_N  = MP_B4 + ML_OUT;
+constexpr int ML_WIMG_BYTES = (ML_H * ML_IN + 2 * ML_H * ML_H + ML_OUT * ML_H) * 2;
+
+struct MlpArgs
+{
+  int rows;
+  const __nv_bfloat16* x;    // [rows][64]
+  const unsigned char* wimg; // packed BF16 weights
+  const float* params;       // FP32 master parameters (biases are read from here)
+  __nv_bfloat16* hid;        // [3][hid_rows][128] post-activations, or null
+  int hid_rows, hid_row0;
+  float* out;                // [rows][8] raw outputs, or null
+  float* aux;                // [nw][ML_AUX] proposal terms kept for training
+  int* err;                  // set when a tensor-core wait times out
+};
+
+struct MlpTrain
+{
+  float *params, *m, *v, *grad;
+  unsigned char* wimg;
+  __nv_bfloat16* x;   // [rows][64]
+  __nv_bfloat16* hid; // [3][rows][128]
+  float* g4;          // [rows][8]
+  float* delta;       // [3][rows][128]
+  int* step;
+};
+
+template<typename T>
+cudaError_t setup_learned();
+cudaError_t launch_mlp_pack(const float* params, unsigned char* img, cudaStream_t st);
+template<typename T>
+cudaError_t launch_features(const DevState<T>& s, int iat, int at_proposed, __nv_bfloat16* X, cudaStream_t st);
+template<typename T>
+cudaError_t launch_mlp_forward(const MlpArgs& a, const DevState<T>& s, int iat, int mode, cudaStream_t st);
+template<typename T>
+cudaError_t launch_mlp_loss_grad(const DevState<T>& s, const float* aux, float* g4, double* stats, cudaStream_t st);
+cudaError_t launch_mlp_backward(const MlpTrain& t, int rows, cudaStream_t st);
+cudaError_t launch_mlp_adam(const MlpTrain& t, float lr, cudaStream_t st);
 
 // recompute path (recompute_kernels.cu)
 template<typename T>
