@@ -169,6 +169,121 @@ def cpu_baseline(workload: str, max_seconds: float = 15.0):
                       f"({'FP32' if spec.precision == 4 else 'FP64'} oracle, OpenMP over walkers), {dt:.1f} s"}
 
 
+def _fp64_twin(system):
+    """The same system in FP64 (the FP32 coefficient values, upcast)."""
+    import dataclasses
+    spec64 = dataclasses.replace(system.spec, precision=8)
+    return dataclasses.replace(system, spec=spec64, coefs=system.coefs.astype(np.float64))
+
+
+def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4):
+    """Per-move ratio error of the FP32 move loop against FP64 on identical positions and
+    coefficients: relative |ratio32 - ratio64| / |ratio64| over nelec electrons x nw walkers."""
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem
+    sys64 = _fp64_twin(system)
+    ds64 = DeviceSystem(sys64)
+    R = make_walkers(system, nw, seed=77)
+    g32, g64 = Crowd(dsys32, nw, k), Crowd(ds64, nw, k)
+    errs = []
+    for g in (g32, g64):
+        g.load_walkers(R)
+        g.mw_evaluateLog()
+    rng = np.random.default_rng(5)
+    for iat in range(nelec):
+        d = rng.normal(size=(nw, 3)) * 0.3
+        out = []
+        for g in (g32, g64):
+            g.mw_evalGrad(iat)
+            g.mw_makeMove(iat, d)
+            r, _ = g.mw_calcRatioGrad(iat)
+            g.mw_accept_rejectMove(iat, np.zeros(nw, np.int32))
+            out.append(r)
+        errs.append(np.abs(out[0] - out[1]) / np.maximum(np.abs(out[1]), 1e-300))
+    e = np.concatenate(errs)
+    del g32, g64, ds64
+    return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(e.max()),
+            "moves": int(e.size), "against": "FP64 move loop, same positions and coefficients"}
+
+
+def effective_samples(args, system, dsys32, seed: int):
+    """Effective independent samples/s = walker-sweeps/s / kappa, kappa the integrated
+    autocorrelation time of the crowd-averaged local energy per sweep (simstats), for
+      plain_fp64:  drift-diffusion, FP64 move loop (walker-resident path, SIMT flush)
+      plain_fp32:  drift-diffusion, FP32 move loop, tcgen05 3xTF32 flush
+      learned_fp32: the learned MH proposal (staged kernels, BF16 network on the tensor cores),
+                    trained on configurations from the FP32 plain run
+    Each run: args.eff_equil untimed sweeps, then args.eff_sweeps timed sweeps with the local
+    energy measured after every sweep (wall clock around the whole call)."""
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem
+    from qmcpack_gb300.stats import energy_statistics
+    spec = system.spec
+    nw, k, tau = spec.walkers, spec.delay, spec.tau
+    n = args.eff_sweeps
+    R0 = make_walkers(system, nw, seed=300)
+    out = {}
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        res = fn()
+        return res, time.perf_counter() - t0
+
+    def summarize(name, el, dt, extra=None):
+        st = energy_statistics(el)
+        wsps = nw * n / dt
+        d = {"energy": st["energy"], "error": st["error"], "variance": st["variance"], "kappa": st["kappa"],
+             "walker_sweeps_per_s": wsps, "effective_samples_per_s": wsps / st["kappa"],
+             "ms_per_sweep": dt / n * 1e3, "sweeps": n}
+        if extra:
+            d.update(extra)
+        out[name] = d
+
+    # FP64 drift-diffusion
+    ds64 = DeviceSystem(_fp64_twin(system))
+    g = Crowd(ds64, nw, k)
+    g.load_walkers(R0)
+    g.mw_evaluateLog()
+    g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=spec.recompute_every)
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=spec.recompute_every))
+    summarize("plain_fp64", el, dt, {"acceptance": a / max(a + r, 1)})
+    del g, ds64
+    # FP32 drift-diffusion
+    g = Crowd(dsys32, nw, k)
+    g.load_walkers(R0)
+    g.mw_evaluateLog()
+    g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=spec.recompute_every, flush=args.flush)
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=spec.recompute_every,
+                                                           flush=args.flush))
+    summarize("plain_fp32", el, dt, {"acceptance": a / max(a + r, 1)})
+    Rplain = g.positions()
+    del g
+    # learned proposal: trained on the plain run's configurations, then frozen
+    g = Crowd(dsys32, nw, k)
+    g.load_walkers(Rplain)
+    g.mw_evaluateLog()
+    g.proposal_init(seed=seed)
+    (_, _, _, tr), t_train = timed(lambda: g.vmc_sweeps_learned(args.train_sweeps, tau, seed + 2, train=True,
+                                                                 lr=args.lr, recompute_every=spec.recompute_every,
+                                                                 flush=args.flush))
+    g.vmc_sweeps_learned(max(args.eff_equil // 2, 2), tau, seed + 3, recompute_every=spec.recompute_every,
+                         flush=args.flush)
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_learned(n, tau, seed + 4, measure=True,
+                                                           recompute_every=spec.recompute_every, flush=args.flush))
+    summarize("learned_fp32", el, dt, {
+        "acceptance": a / max(a + r, 1),
+        "training": {"sweeps": args.train_sweeps, "moves": args.train_sweeps * nw * system.n_elec,
+                     "seconds": t_train, "lr": args.lr, "final_esjd": tr[0], "final_mean_alpha": tr[1],
+                     "data": "configurations of the FP32 drift-diffusion run (continued on-policy)"}})
+    del g
+    p64 = out["plain_fp64"]
+    for name in ("plain_fp32", "learned_fp32"):
+        o = out[name]
+        o["speedup_vs_plain_fp64"] = o["effective_samples_per_s"] / p64["effective_samples_per_s"]
+        o["energy_within_2sigma_of_plain_fp64"] = bool(
+            abs(o["energy"] - p64["energy"]) <= 2 * np.hypot(o["error"], p64["error"]))
+    out["unit"] = "effective samples/s (walker-sweeps/s / kappa)"
+    return out
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
@@ -287,6 +402,11 @@ def run_ours(args, rank: int, world: int):
             dist.destroy_process_group()
         return
     base = cpu_baseline(args.workload) if world == 1 and not args.no_cpu_baseline else None
+    eff = None
+    rerr = None
+    if world == 1 and not args.no_effective and spec.precision == 4:
+        rerr = ratio_error(system, dsys, 64, k)
+        eff = effective_samples(args, system, dsys, seed + 11)
     line = {
         "metric": "walker-moves/s", "value": value, "unit": "walker-moves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -317,6 +437,8 @@ def run_ours(args, rank: int, world: int):
         "walkers_repaired_in_timed_sweeps": repaired,
         "equilibration_sweeps": args.equil,
         "walker_sweeps_per_s": value / system.n_elec,
+        "effective_samples": eff,
+        "ratio_error_fp32": rerr,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -334,6 +456,11 @@ def main():
     ap.add_argument("--equil", type=int, default=20, help="untimed equilibration sweeps before the warm-up")
     ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
                     help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
+    ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
+    ap.add_argument("--eff-sweeps", type=int, default=200, help="timed sweeps per method in the comparison")
+    ap.add_argument("--eff-equil", type=int, default=30)
+    ap.add_argument("--train-sweeps", type=int, default=6)
+    ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
