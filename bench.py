@@ -208,80 +208,98 @@ def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4):
 def effective_samples(args, system, dsys32, seed: int):
     """Effective independent samples/s = walker-sweeps/s / kappa, kappa the integrated
     autocorrelation time of the crowd-averaged local energy per sweep (simstats), for
-      plain_fp64:  drift-diffusion, FP64 move loop (walker-resident path, SIMT flush)
-      plain_fp32:  drift-diffusion, FP32 move loop, tcgen05 3xTF32 flush
-      learned_fp32: the learned MH proposal (staged kernels, BF16 network on the tensor cores),
-                    trained on configurations from the FP32 plain run
-    Each run: args.eff_equil untimed sweeps, then args.eff_sweeps timed sweeps with the local
-    energy measured after every sweep (wall clock around the whole call)."""
+      plain_fp64:   drift-diffusion, FP64 move loop (walker-resident path, SIMT flush)
+      plain_fp32:   drift-diffusion, FP32 move loop, tcgen05 3xTF32 flush
+      learned_fp32: the learned MH proposal, trained on configurations of the FP32 plain run
+                    (staged kernels, BF16 network on the tensor cores, hand-written backward
+                    and Adam), then run frozen on the walker-resident kernel
+    All three start from one configuration equilibrated by args.eff_equil plain FP32 sweeps.
+    FP32 runs: args.eff_sweeps timed sweeps; the FP64 run: args.eff_sweeps_fp64 timed sweeps,
+    and its kappa is the FP32 plain run's (the same drift-diffusion chain up to rounding; a
+    short FP64 series cannot resolve kappa).  Wall clock around each whole call, local
+    energy measured after every sweep."""
     from qmcpack_gb300.crowd import Crowd, DeviceSystem
     from qmcpack_gb300.stats import energy_statistics
     spec = system.spec
     nw, k, tau = spec.walkers, spec.delay, spec.tau
-    n = args.eff_sweeps
-    R0 = make_walkers(system, nw, seed=300)
+    rec = spec.recompute_every
     out = {}
 
     def timed(fn):
+        torch_sync()
         t0 = time.perf_counter()
         res = fn()
         return res, time.perf_counter() - t0
 
-    def summarize(name, el, dt, extra=None):
+    def summarize(name, el, dt, n, extra=None, kappa=None):
         st = energy_statistics(el)
         wsps = nw * n / dt
-        d = {"energy": st["energy"], "error": st["error"], "variance": st["variance"], "kappa": st["kappa"],
-             "walker_sweeps_per_s": wsps, "effective_samples_per_s": wsps / st["kappa"],
-             "ms_per_sweep": dt / n * 1e3, "sweeps": n}
+        kap = st["kappa"] if kappa is None else kappa
+        h = el.mean(axis=1)
+        d = {"energy": st["energy"], "error": st["error"], "variance": st["variance"], "kappa": kap,
+             "kappa_own_series": st["kappa"], "energy_first_half": float(h[: n // 2].mean()),
+             "energy_second_half": float(h[n // 2:].mean()),
+             "walker_sweeps_per_s": wsps, "effective_samples_per_s": wsps / kap, "ms_per_sweep": dt / n * 1e3,
+             "sweeps": n}
         if extra:
             d.update(extra)
         out[name] = d
 
-    # FP64 drift-diffusion
+    g = Crowd(dsys32, nw, k)
+    g.load_walkers(make_walkers(system, nw, seed=300))
+    g.mw_evaluateLog()
+    _, t_eq = timed(lambda: g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=rec,
+                                         flush=args.flush))
+    Req = g.positions()
+    # FP32 drift-diffusion
+    n = args.eff_sweeps
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=rec, flush=args.flush))
+    summarize("plain_fp32", el, dt, n, {"acceptance": a / max(a + r, 1)})
+    del g
+    # FP64 drift-diffusion from the same configurations
     ds64 = DeviceSystem(_fp64_twin(system))
     g = Crowd(ds64, nw, k)
-    g.load_walkers(R0)
+    g.load_walkers(Req)
     g.mw_evaluateLog()
-    g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=spec.recompute_every)
-    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=spec.recompute_every))
-    summarize("plain_fp64", el, dt, {"acceptance": a / max(a + r, 1)})
+    n64 = args.eff_sweeps_fp64
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n64, tau, seed + 1, recompute_every=rec))
+    summarize("plain_fp64", el, dt, n64, {"acceptance": a / max(a + r, 1), "kappa_source": "plain_fp32"},
+              kappa=out["plain_fp32"]["kappa"])
     del g, ds64
-    # FP32 drift-diffusion
-    g = Crowd(dsys32, nw, k)
-    g.load_walkers(R0)
-    g.mw_evaluateLog()
-    g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=spec.recompute_every, flush=args.flush)
-    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=spec.recompute_every,
-                                                           flush=args.flush))
-    summarize("plain_fp32", el, dt, {"acceptance": a / max(a + r, 1)})
-    Rplain = g.positions()
-    del g
     # learned proposal: trained on the plain run's configurations, then frozen
     g = Crowd(dsys32, nw, k)
-    g.load_walkers(Rplain)
+    g.load_walkers(Req)
     g.mw_evaluateLog()
     g.proposal_init(seed=seed)
     (_, _, _, tr), t_train = timed(lambda: g.vmc_sweeps_learned(args.train_sweeps, tau, seed + 2, train=True,
-                                                                 lr=args.lr, recompute_every=spec.recompute_every,
-                                                                 flush=args.flush))
-    g.vmc_sweeps_learned(max(args.eff_equil // 2, 2), tau, seed + 3, recompute_every=spec.recompute_every,
-                         flush=args.flush)
-    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_learned(n, tau, seed + 4, measure=True,
-                                                           recompute_every=spec.recompute_every, flush=args.flush))
-    summarize("learned_fp32", el, dt, {
+                                                                 lr=args.lr, recompute_every=rec, flush=args.flush))
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_learned(n, tau, seed + 4, measure=True, recompute_every=rec,
+                                                           flush=args.flush))
+    summarize("learned_fp32", el, dt, n, {
         "acceptance": a / max(a + r, 1),
         "training": {"sweeps": args.train_sweeps, "moves": args.train_sweeps * nw * system.n_elec,
-                     "seconds": t_train, "lr": args.lr, "final_esjd": tr[0], "final_mean_alpha": tr[1],
-                     "data": "configurations of the FP32 drift-diffusion run (continued on-policy)"}})
+                     "seconds": t_train, "lr": args.lr, "final_mean_alpha_jump2": tr[0],
+                     "final_mean_alpha": tr[1], "final_objective": tr[2],
+                     "data": "configurations of the FP32 drift-diffusion run, continued on-policy"}})
     del g
     p64 = out["plain_fp64"]
     for name in ("plain_fp32", "learned_fp32"):
         o = out[name]
         o["speedup_vs_plain_fp64"] = o["effective_samples_per_s"] / p64["effective_samples_per_s"]
-        o["energy_within_2sigma_of_plain_fp64"] = bool(
-            abs(o["energy"] - p64["energy"]) <= 2 * np.hypot(o["error"], p64["error"]))
+        o["energy_within_2sigma_of_plain_fp32"] = bool(
+            abs(o["energy"] - out["plain_fp32"]["energy"]) <= 2 * np.hypot(o["error"], out["plain_fp32"]["error"]))
     out["unit"] = "effective samples/s (walker-sweeps/s / kappa)"
+    out["equilibration"] = {"sweeps": args.eff_equil, "seconds": t_eq, "method": "plain FP32 drift-diffusion"}
     return out
+
+
+def torch_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except ImportError:
+        pass
 
 
 def run_reference(args, rank: int, world: int):
@@ -457,9 +475,10 @@ def main():
     ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
                     help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
     ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
-    ap.add_argument("--eff-sweeps", type=int, default=200, help="timed sweeps per method in the comparison")
-    ap.add_argument("--eff-equil", type=int, default=30)
-    ap.add_argument("--train-sweeps", type=int, default=6)
+    ap.add_argument("--eff-sweeps", type=int, default=600, help="timed FP32 sweeps per method in the comparison")
+    ap.add_argument("--eff-sweeps-fp64", type=int, default=80, help="timed FP64 sweeps in the comparison")
+    ap.add_argument("--eff-equil", type=int, default=300)
+    ap.add_argument("--train-sweeps", type=int, default=10)
     ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

@@ -236,11 +236,15 @@ int qmcg_proposal_backward(qmcg_crowd crowd, int rows, const float* x, const flo
  * position (after qmcg_mw_eval_grad) or at the proposed one (at_proposed = 1, after
  * qmcg_mw_calc_ratio_grad). */
 int qmcg_proposal_features(qmcg_crowd crowd, int iat, int at_proposed, float* x);
-/* Sweeps with the learned proposal (rng_mode must be 1; path is ignored: staged
- * per-electron kernels in one CUDA graph per sweep).  train != 0 adds one Adam step
- * (learning rate lr) per electron move over the crowd's walkers.  e_local (may be NULL)
+/* Sweeps with the learned proposal (rng_mode must be 1).  Without training and with
+ * params->path 0 they run on the walker-resident sweep kernel (the network evaluated
+ * by each walker's CTA); otherwise on the staged per-electron kernels (the network on
+ * the tensor cores over all walkers), one CUDA graph per sweep.  train != 0 adds one
+ * Adam step (learning rate lr) per electron move over the crowd's walkers.  e_local (may be NULL)
  * [num_sweeps][num_walkers] as in qmcg_vmc_sweeps_measure; train_stats (may be NULL)
- * [2] = mean alpha |r' - r|^2 and mean acceptance probability over the training moves. */
+ * [3] = mean alpha |r' - r|^2, mean acceptance probability and mean training objective
+ * over the training moves.  The objective per move is lambda^4 / j - j with
+ * j = alpha |r' - r|^2 and lambda^2 = 3 tau (Levy, Hoffman and Sohl-Dickstein, ICLR 2018). */
 int qmcg_vmc_sweeps_learned(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, int train, double lr,
                             double* e_local, qmcg_sweep_stats* stats, double* train_stats);
 

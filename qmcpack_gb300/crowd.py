@@ -229,17 +229,19 @@ class Crowd:
         return x
 
     def vmc_sweeps_learned(self, nsweeps: int, tau: float, seed: int, train: bool = False, lr: float = 1e-3,
-                           measure: bool = False, use_drift: bool = True, recompute_every: int = 0, flush: int = 0):
-        """(accepted, rejected, E_L[nsweeps][nw] or None, (mean alpha|dr|^2, mean alpha))"""
+                           measure: bool = False, use_drift: bool = True, recompute_every: int = 0, flush: int = 0,
+                           staged: bool = False):
+        """(accepted, rejected, E_L[nsweeps][nw] or None, (mean alpha|dr|^2, mean alpha, mean objective));
+        inference runs on the walker-resident kernel unless staged (training always uses the staged kernels)."""
         p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
-                        recompute_every=recompute_every, path=1, flush=flush)
+                        recompute_every=recompute_every, path=1 if staged else 0, flush=flush)
         st = SweepStats()
         el = np.zeros((nsweeps, self.nw)) if measure else None
-        ts = np.zeros(2)
+        ts = np.zeros(3)
         check(self.L.qmcg_vmc_sweeps_learned(self.handle, C.byref(p), nsweeps, int(train), lr,
                                              _p(el) if el is not None else None, C.byref(st), _p(ts)))
         self.last_repaired = st.repaired
-        return st.accepted, st.rejected, el, (float(ts[0]), float(ts[1]))
+        return st.accepted, st.rejected, el, (float(ts[0]), float(ts[1]), float(ts[2]))
 
     def vmc_sweeps_async(self, nsweeps: int):
         check(self.L.qmcg_vmc_sweeps_async(self.handle, nsweeps))

@@ -428,6 +428,7 @@ struct Crowd final : qmcg_crowd_s
   cudaGraphExec_t graph = nullptr;
   int graph_rng_mode = -1, graph_use_drift = -1, graph_path = -1;
   int sweep_grid_size = 0;
+  int sweep_grid_learned = 0;
   int flush_kind      = 0;
   int graph_flush     = -1;
   int* tc_err         = nullptr;
@@ -445,7 +446,7 @@ struct Crowd final : qmcg_crowd_s
     int* err      = nullptr;
     double* stats = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int g_train = -1, g_drift = -1, g_flush = -1;
+    int g_train = -1, g_drift = -1, g_flush = -1, g_path = -1;
     double g_tau = 0;
     uint64_t g_seed = 0;
     float g_lr = 0;
@@ -898,8 +899,9 @@ struct Crowd final : qmcg_crowd_s
   // one sweep on the walker-resident path: with delayed updates, one resident
   // launch per segment of up to k electrons of one spin group followed by the
   // batched flush of that spin; with rank-1 updates one launch for the sweep
-  int enqueue_sweep_resident()
+  int enqueue_sweep_resident(bool learned = false)
   {
+    const int grid = learned ? sweep_grid_learned : sweep_grid_size;
     if (k > 1)
     {
       for (int g = 0; g < 2; g++)
@@ -908,15 +910,15 @@ struct Crowd final : qmcg_crowd_s
         for (int i0 = first; i0 < last; i0 += k)
         {
           const int i1 = std::min(i0 + k, last);
-          CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream));
+          CUDA_TRY(launch_sweep_segment<T>(s, grid, i0, i1, stream, learned));
           CUDA_TRY(launch_flush_choice(g, i1 - i0));
         }
       }
     }
     else
     {
-      CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, 0, sys->nup, stream));
-      CUDA_TRY(launch_sweep_segment<T>(s, sweep_grid_size, sys->nup, sys->ne, stream));
+      CUDA_TRY(launch_sweep_segment<T>(s, grid, 0, sys->nup, stream, learned));
+      CUDA_TRY(launch_sweep_segment<T>(s, grid, sys->nup, sys->ne, stream, learned));
     }
     CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
@@ -1027,6 +1029,10 @@ struct Crowd final : qmcg_crowd_s
       CUDA_TRY(mem.alloc(&ln.t.v, MP_N));
       CUDA_TRY(mem.alloc(&ln.t.grad, MP_N));
       CUDA_TRY(mem.alloc(&ln.t.wimg, (size_t)ML_WIMG_BYTES));
+      CUDA_TRY(mem.alloc(&ln.t.wsimt, (size_t)ML_WSIMT_BYTES));
+      s.mlp_simt   = ln.t.wsimt;
+      s.mlp_params = ln.t.params;
+      CUDA_TRY(sweep_grid<T>(s, &sweep_grid_learned, true));
       CUDA_TRY(mem.alloc(&ln.t.x, rows * ML_IN));
       CUDA_TRY(mem.alloc(&ln.t.hid, 3 * rows * ML_H));
       CUDA_TRY(mem.alloc(&ln.t.g4, rows * 8));
@@ -1035,7 +1041,7 @@ struct Crowd final : qmcg_crowd_s
       CUDA_TRY(mem.alloc(&ln.out, rows * 8));
       CUDA_TRY(mem.alloc(&ln.aux, (size_t)nw * ML_AUX));
       CUDA_TRY(mem.alloc(&ln.err, 1));
-      CUDA_TRY(mem.alloc(&ln.stats, 2));
+      CUDA_TRY(mem.alloc(&ln.stats, 3));
     }
     // uniform(-a, a) with a = scale / sqrt(fan_in) for the hidden layers; the output
     // layer starts at zero, so the initial proposal is drift-diffusion
@@ -1062,7 +1068,7 @@ struct Crowd final : qmcg_crowd_s
       CUDA_TRY(cudaMemsetAsync(ln.t.m, 0, MP_N * sizeof(float), stream));
       CUDA_TRY(cudaMemsetAsync(ln.t.v, 0, MP_N * sizeof(float), stream));
       CUDA_TRY(cudaMemsetAsync(ln.t.step, 0, sizeof(int), stream));
-      CUDA_TRY(launch_mlp_pack(ln.t.params, ln.t.wimg, stream));
+      CUDA_TRY(launch_mlp_pack(ln.t.params, ln.t.wimg, ln.t.wsimt, stream));
     }
     if (get)
       CUDA_TRY(cudaMemcpyAsync(get, ln.t.params, MP_N * sizeof(float), cudaMemcpyDeviceToHost, stream));
@@ -1243,8 +1249,9 @@ struct Crowd final : qmcg_crowd_s
         return rc;
     }
     const float flr = static_cast<float>(lr);
+    const int gpath = (!train && p->path == 0) ? 0 : 1; // inference on the walker-resident kernel
     if (!ln.graph || ln.g_train != (train ? 1 : 0) || ln.g_tau != p->tau || ln.g_seed != p->seed ||
-        ln.g_lr != flr || ln.g_flush != p->flush || ln.g_drift != p->use_drift)
+        ln.g_lr != flr || ln.g_flush != p->flush || ln.g_drift != p->use_drift || ln.g_path != gpath)
     {
       if (ln.graph)
       {
@@ -1264,7 +1271,7 @@ struct Crowd final : qmcg_crowd_s
       flush_kind  = p->flush;
       cudaGraph_t g;
       CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-      int rc        = enqueue_sweep_learned(train != 0, flr);
+      int rc        = gpath == 0 ? enqueue_sweep_resident(true) : enqueue_sweep_learned(train != 0, flr);
       cudaError_t e = cudaStreamEndCapture(stream, &g);
       if (rc)
         return rc;
@@ -1280,6 +1287,7 @@ struct Crowd final : qmcg_crowd_s
       ln.g_lr    = flr;
       ln.g_flush = p->flush;
       ln.g_drift = p->use_drift;
+      ln.g_path  = gpath;
     }
     if (el)
     {
@@ -1295,7 +1303,7 @@ struct Crowd final : qmcg_crowd_s
     }
     recompute_every = p->recompute_every;
     CUDA_TRY(cudaMemsetAsync(s.counters, 0, 3 * sizeof(unsigned long long), stream));
-    CUDA_TRY(cudaMemsetAsync(ln.stats, 0, 2 * sizeof(double), stream));
+    CUDA_TRY(cudaMemsetAsync(ln.stats, 0, 3 * sizeof(double), stream));
     for (int it = 0; it < n; it++)
     {
       CUDA_TRY(cudaGraphLaunch(ln.graph, stream));
@@ -1310,7 +1318,7 @@ struct Crowd final : qmcg_crowd_s
         sweeps_since_recompute = 0;
       }
     }
-    double hs2[2];
+    double hs2[3];
     int err = 0;
     CUDA_TRY(cudaMemcpyAsync(hs2, ln.stats, sizeof(hs2), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaMemcpyAsync(&err, ln.err, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -1336,6 +1344,7 @@ struct Crowd final : qmcg_crowd_s
       const double moves = (double)n * sys->ne * nw;
       tstats[0]          = train ? hs2[0] / moves : 0.0; // mean alpha |r' - r|^2 over training moves
       tstats[1]          = train ? hs2[1] / moves : 0.0; // mean alpha
+      tstats[2]          = train ? hs2[2] / moves : 0.0; // mean training objective (lower is better)
     }
     return QMCG_OK;
   }

@@ -100,6 +100,9 @@ struct DevState
   int rng_mode;          // 0: stream from the host, 1: counter-based on the device
   double tau;
   int use_drift;
+  // learned proposal (walker-resident path): SIMT weight image and FP32 master parameters
+  const void* mlp_simt;
+  const float* mlp_params;
 };
 
 // Ewald tables of a system for the local-energy kernel (energy.cu)

@@ -35,9 +35,10 @@ cudaError_t setup_sweep_kernel();
 template<typename T>
 size_t sweep_smem_bytes(const DevState<T>& s);
 template<typename T>
-cudaError_t sweep_grid(const DevState<T>& s, int* grid);
+cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned = false);
 template<typename T>
-cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st);
+cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st,
+                                 bool learned = false);
 // batched, shared-memory-staged flush of one spin for all walkers (flush_kernels.cu);
 // falls back to the two-kernel SIMT flush when the tiles do not fit
 template<typename T>
@@ -107,6 +108,7 @@ constexpr int MP_W4 = MP_B3 + ML_H;
 constexpr int MP_B4 = MP_W4 + ML_OUT * ML_H;
 constexpr int MP_N  = MP_B4 + ML_OUT;
 constexpr int ML_WIMG_BYTES = (ML_H * ML_IN + 2 * ML_H * ML_H + ML_OUT * ML_H) * 2;
+constexpr int ML_WSIMT_BYTES = (ML_IN / 2 + ML_H) * ML_H * 4 + 6 * ML_H * 2;
 
 struct MlpArgs
 {
@@ -124,7 +126,8 @@ struct MlpArgs
 struct MlpTrain
 {
   float *params, *m, *v, *grad;
-  unsigned char* wimg;
+  unsigned char* wimg;  // tensor-core image
+  unsigned char* wsimt; // SIMT image for the walker-resident sweep
   __nv_bfloat16* x;   // [rows][64]
   __nv_bfloat16* hid; // [3][rows][128]
   float* g4;          // [rows][8]
@@ -134,7 +137,7 @@ struct MlpTrain
 
 template<typename T>
 cudaError_t setup_learned();
-cudaError_t launch_mlp_pack(const float* params, unsigned char* img, cudaStream_t st);
+cudaError_t launch_mlp_pack(const float* params, unsigned char* img, unsigned char* simt, cudaStream_t st);
 template<typename T>
 cudaError_t launch_features(const DevState<T>& s, int iat, int at_proposed, __nv_bfloat16* X, cudaStream_t st);
 template<typename T>

@@ -18,14 +18,17 @@
 // Inference: BF16 weights and activations, FP32 accumulation on the tensor cores
 // (tcgen05.mma kind::f16, accumulators in TMEM), 128 walkers per CTA; the proposal or
 // the MH probability is computed in the epilogue of the last layer.
-// Training (hand-written, FP32): the expected squared jump distance E[alpha |r' - r|^2]
-// is maximised by reparameterised gradients through (mu, s) of both evaluations,
+// Training (hand-written, FP32): the expected squared jump j = alpha |r' - r|^2 of every
+// walker's move is pushed up through the objective mean(lambda^4 / j - j) (large jumps
+// rewarded, walkers that do not move penalised), by reparameterised gradients through
+// (mu, s) of both evaluations,
 // backpropagated through the three layers by SIMT kernels, with Adam on FP32 master
 // weights that are re-packed into the BF16 tensor-core image after every step.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "launch.h"
+#include "learned.cuh"
 #include "tc.cuh"
 
 namespace qmcg
@@ -41,7 +44,6 @@ constexpr int ML_A      = ML_WBYTES;               // activation tile 128 x 128 
 constexpr int ML_BIAS   = ML_A + ML_M * ML_H * 2;  // 400 floats
 constexpr int ML_BAR    = ML_BIAS + 400 * 4;
 constexpr int ML_SMEM   = ML_BAR + 64;
-constexpr float ML_MU_MAX = 4.f, ML_S_MIN = -3.f, ML_S_MAX = 2.f, ML_LSCALE = 2.f;
 
 // ---------------------------------------------------------------------------
 // weight packing and parameter layout
@@ -57,7 +59,8 @@ __device__ __forceinline__ bool mp_structural_zero(int i)
   return false;
 }
 
-__global__ void mlp_pack_kernel(const float* __restrict__ p, unsigned char* __restrict__ img)
+__global__ void mlp_pack_kernel(const float* __restrict__ p, unsigned char* __restrict__ img,
+                                unsigned char* __restrict__ simt)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   int base, n, k, K, src;
@@ -82,66 +85,25 @@ __global__ void mlp_pack_kernel(const float* __restrict__ p, unsigned char* __re
   }
   else
     return;
-  *reinterpret_cast<__nv_bfloat16*>(img + base + cm_off_b(n, k, K, 2)) = __float2bfloat16_rn(p[src]);
+  const __nv_bfloat16 v = __float2bfloat16_rn(p[src]);
+  *reinterpret_cast<__nv_bfloat16*>(img + base + cm_off_b(n, k, K, 2)) = v;
+  // SIMT image: W1..W3 as pairs along k, W4 rows 0..5 row-major
+  __nv_bfloat16* sp = reinterpret_cast<__nv_bfloat16*>(simt);
+  if (base == ML_W4)
+  {
+    if (n < ML_NOUT)
+      sp[2 * MS_NPAIRS + n * ML_H + k] = v;
+  }
+  else
+  {
+    const int off = base == ML_W1 ? MS_P1 : base == ML_W2 ? MS_P2 : MS_P3;
+    sp[2 * (off + (k >> 1) * ML_H + n) + (k & 1)] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // features: one warp per walker
 // ---------------------------------------------------------------------------
-// sorted insertion into a register list of the 8 smallest (d2, index)
-__device__ __forceinline__ void top8_insert(float (&bd)[8], int (&bj)[8], float v, int id)
-{
-#pragma unroll
-  for (int q = 0; q < 8; q++)
-    if (v < bd[q])
-    {
-      const float tv = bd[q];
-      const int ti   = bj[q];
-      bd[q]          = v;
-      bj[q]          = id;
-      v              = tv;
-      id             = ti;
-    }
-}
-
-// 8 rounds of warp argmin over the lanes' list heads; lane q gets the q-th nearest index
-__device__ __forceinline__ int top8_merge(float (&bd)[8], int (&bj)[8], int lane)
-{
-  int mine = -1;
-#pragma unroll
-  for (int q = 0; q < 8; q++)
-  {
-    float v = bd[0];
-    int who = lane;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-      const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
-      const int w2   = __shfl_xor_sync(0xffffffffu, who, o);
-      if (v2 < v || (v2 == v && w2 < who))
-      {
-        v   = v2;
-        who = w2;
-      }
-    }
-    const int j = __shfl_sync(0xffffffffu, bj[0], who);
-    if (lane == q)
-      mine = (v < 3.0e38f) ? j : -1;
-    if (lane == who)
-    {
-#pragma unroll
-      for (int t = 0; t < 7; t++)
-      {
-        bd[t] = bd[t + 1];
-        bj[t] = bj[t + 1];
-      }
-      bd[7] = 3.4e38f;
-      bj[7] = -1;
-    }
-  }
-  return mine;
-}
-
 template<typename T>
 __global__ void features_kernel(DevState<T> s, int iat, int at_proposed, __nv_bfloat16* __restrict__ X)
 {
@@ -234,8 +196,6 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n)
 {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
-
-__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 
 // MODE 0: raw outputs; 1: proposal at the current position; 2: MH probability at the proposed one
 template<typename T, int MODE>
@@ -415,7 +375,9 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(MlpArgs a, DevState<T>
 // training: loss gradient, backward, Adam
 // ---------------------------------------------------------------------------
 // dL/d(raw outputs) of the forward row iw and the reverse row nw + iw for
-// L = -(1/nw) sum_w alpha_w |r'_w - r_w|^2, alpha = min(1, e^Delta) (0 when p < eps)
+// L = (1/nw) sum_w (lambda^4 / j_w - j_w), j_w = alpha_w |r'_w - r_w|^2 the expected
+// squared jump of walker w's move, alpha = min(1, e^Delta) (0 when p < eps); the
+// objective of Levy, Hoffman, Sohl-Dickstein (ICLR 2018) for learned MCMC kernels
 template<typename T>
 __global__ void mlp_loss_grad_kernel(DevState<T> s, const float* __restrict__ aux, float* __restrict__ g4,
                                      double* __restrict__ stats)
@@ -435,7 +397,12 @@ __global__ void mlp_loss_grad_kernel(DevState<T> s, const float* __restrict__ au
     dr[d] = s.disp[iw * 3 + d];
     j2 += dr[d] * dr[d];
   }
-  const double inv_n = 1.0 / s.nw;
+  // per-walker weight of the jump objective L_w = lambda^4 / j_w - j_w, j_w = alpha |dr|^2,
+  // lambda^2 = 3 tau (the jump of drift-diffusion): dL/dtheta = -(lambda^4 / j^2 + 1) dj/dtheta.
+  // The first term keeps every walker moving instead of favouring rare long jumps.
+  const double lam2  = 3.0 * s.tau;
+  const double jw    = fmax(alpha * j2, 0.01 * lam2);
+  const double inv_n = (lam2 * lam2 / (jw * jw) + 1.0) / s.nw;
   float* gf = g4 + (size_t)iw * 8;
   float* gr = g4 + (size_t)(s.nw + iw) * 8;
 #pragma unroll
@@ -466,6 +433,7 @@ __global__ void mlp_loss_grad_kernel(DevState<T> s, const float* __restrict__ au
   gf[6] = gf[7] = gr[6] = gr[7] = 0.f;
   atomicAdd(stats, alpha * j2);
   atomicAdd(stats + 1, alpha);
+  atomicAdd(stats + 2, lam2 * lam2 / jw - alpha * j2);
 }
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 x) { return __bfloat162float(x); }
@@ -572,10 +540,10 @@ cudaError_t setup_learned()
   return e;
 }
 
-cudaError_t launch_mlp_pack(const float* params, unsigned char* img, cudaStream_t st)
+cudaError_t launch_mlp_pack(const float* params, unsigned char* img, unsigned char* simt, cudaStream_t st)
 {
   const int n = ML_H * ML_IN + 2 * ML_H * ML_H + ML_OUT * ML_H;
-  mlp_pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(params, img);
+  mlp_pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(params, img, simt);
   return cudaGetLastError();
 }
 
@@ -634,7 +602,7 @@ cudaError_t launch_mlp_adam(const MlpTrain& t, float lr, cudaStream_t st)
 {
   mlp_adam_kernel<<<(MP_N + 255) / 256, 256, 0, st>>>(t.params, t.m, t.v, t.grad, t.step, lr);
   mlp_step_kernel<<<1, 1, 0, st>>>(t.step);
-  return launch_mlp_pack(t.params, t.wimg, st);
+  return launch_mlp_pack(t.params, t.wimg, t.wsimt, st);
 }
 
 template cudaError_t setup_learned<float>();

@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "launch.h"
+#include "learned.cuh"
 #include "spline.cuh"
 
 namespace qmcg
@@ -109,7 +110,23 @@ __device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const
   }
 }
 
-template<typename T, int NT, int MINB>
+// shared scratch of the learned proposal (empty for the drift-diffusion kernel)
+template<typename T, bool LEARNED>
+struct LearnedSmem
+{
+};
+template<typename T>
+struct LearnedSmem<T, true>
+{
+  float x[ML_IN];
+  float h[2 * ML_H];
+  float red[ML_NOUT * 4];
+  float out[8];
+  T g[3];
+  T p;
+};
+
+template<typename T, int NT, int MINB, bool LEARNED>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -133,6 +150,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
   __shared__ int s_acc;
   __shared__ T s_det;
   __shared__ T s_cur[10];
+  __shared__ LearnedSmem<T, LEARNED> lsm;
+  const __nv_bfloat162* ml_pairs = reinterpret_cast<const __nv_bfloat162*>(s.mlp_simt);
+  const __nv_bfloat16* ml_w4 = reinterpret_cast<const __nv_bfloat16*>(ml_pairs + MS_NPAIRS);
 
   const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
@@ -220,6 +240,50 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
           g[3] += x * pv0[j];
         }
         block_sum<T, 4>(g, red);
+        if constexpr (LEARNED)
+        {
+          // the network at the current position: (mu, s) of the proposal
+          if (threadIdx.x == 0)
+          {
+            if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
+              atomicOr(s.status + w, ST_ILLCOND);
+            for (int d = 0; d < 3; d++)
+            {
+              T gs = g[d];
+              if (s.has_j1)
+                gs += s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat];
+              if (s.has_j2)
+                gs += J2s[(1 + d) * s.ne_pad + iat];
+              lsm.g[d] = gs;
+            }
+          }
+          __syncthreads();
+          const T pc[3] = {Rs[iat], Rs[s.ne_pad + iat], Rs[2 * s.ne_pad + iat]};
+          features_cta(s, Rs, iat, pc, lsm.g, lsm.x);
+          __syncthreads();
+          mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, lsm.x, lsm.h, lsm.red, lsm.out);
+          if (threadIdx.x == 0)
+          {
+            const T st = sqrt(tau);
+            T drift[3];
+            unr_drift_t(tau, lsm.g, drift);
+            T sum_s = 0, x2 = 0;
+            for (int d = 0; d < 3; d++)
+            {
+              const T mu = T(clampf(lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
+              const T sd = T(clampf(lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+              sum_s += sd;
+              x2 += s_gauss[d] * s_gauss[d];
+              const T dd = drift[d] + st * mu + st * exp(sd) * s_gauss[d];
+              s_disp[d]  = dd;
+              s_pos[d]   = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(dd);
+            }
+            s_loggf = -sum_s - T(0.5) * x2;
+          }
+          __syncthreads();
+        }
+        else
+        {
         if (threadIdx.x == 0)
         {
           if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
@@ -257,6 +321,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
               : T(0);
         }
         __syncthreads();
+        }
       }
       // ------------------------------------------------ evaluation at the proposed position
       const double pos[3] = {s_pos[0], s_pos[1], s_pos[2]};
@@ -346,6 +411,25 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         const T p = detr * detr * exp(T(2) * logj);
         if (!isfinite(p) || (p != T(0) && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
           atomicOr(s.status + w, ST_NONFINITE);
+        s_det    = detr;
+        s_cur[0] = acc[10];
+        s_cur[1] = acc[11];
+        s_cur[2] = acc[12];
+        s_cur[3] = acc[13];
+        s_cur[4] = acc[4];
+        s_cur[5] = acc[5];
+        s_cur[6] = acc[6];
+        s_cur[7] = acc[7];
+        s_cur[8] = acc[8];
+        s_cur[9] = -acc[9];
+        if constexpr (LEARNED)
+        {
+          lsm.p = p;
+          for (int d = 0; d < 3; d++)
+            lsm.g[d] = g[d];
+        }
+        else
+        {
         T log_gb = T(0);
         if (s.use_drift)
         {
@@ -372,20 +456,55 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         }
         else
           n_rej++;
-        s_acc    = a;
-        s_det    = detr;
-        s_cur[0] = acc[10];
-        s_cur[1] = acc[11];
-        s_cur[2] = acc[12];
-        s_cur[3] = acc[13];
-        s_cur[4] = acc[4];
-        s_cur[5] = acc[5];
-        s_cur[6] = acc[6];
-        s_cur[7] = acc[7];
-        s_cur[8] = acc[8];
-        s_cur[9] = -acc[9];
+        s_acc = a;
+        }
       }
       __syncthreads();
+      if constexpr (LEARNED)
+      {
+        // the network at the proposed position: the reverse density q(r | R')
+        const T pn[3] = {T(s_pos[0]), T(s_pos[1]), T(s_pos[2])};
+        features_cta(s, Rs, iat, pn, lsm.g, lsm.x);
+        __syncthreads();
+        mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, lsm.x, lsm.h, lsm.red, lsm.out);
+        if (threadIdx.x == 0)
+        {
+          const T st = sqrt(tau);
+          T drift[3];
+          unr_drift_t(tau, lsm.g, drift);
+          T sum_s = 0, z2 = 0;
+          for (int d = 0; d < 3; d++)
+          {
+            const T mu = T(clampf(lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
+            const T sd = T(clampf(lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+            sum_s += sd;
+            const T z = (-s_disp[d] - drift[d] - st * mu) / (st * exp(sd));
+            z2 += z * z;
+          }
+          const T log_gb = -sum_s - T(0.5) * z2;
+          const T p      = lsm.p;
+          const T detr   = s_det;
+          int a          = 0;
+          if (p >= Eps<T>::v)
+          {
+            const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
+            a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - s_loggf) ? 1 : 0;
+          }
+          if (a)
+          {
+            n_acc++;
+            int ex;
+            det_mant = frexp(det_mant * fabs(static_cast<double>(detr)), &ex);
+            det_exp += ex;
+            if (detr < T(0))
+              det_neg ^= 1;
+          }
+          else
+            n_rej++;
+          s_acc = a;
+        }
+        __syncthreads();
+      }
       // ------------------------------------------------ accept / reject
       const bool accd = s_acc != 0;
       if (K > 1)
@@ -567,7 +686,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
 template<typename T>
 cudaError_t setup_sweep_kernel()
 {
-  return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
+  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
 }
 
@@ -580,17 +703,24 @@ size_t sweep_smem_bytes(const DevState<T>& s)
 // electrons [i0, i1) of every walker, inside one spin group; with delayed updates
 // i1 - i0 <= k and the host flushes after the launch
 template<typename T>
-cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st)
+cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st, bool learned)
 {
   if (i0 < 0 || i1 > s.ne || i1 <= i0 || (i0 < s.nup) != (i1 - 1 < s.nup) || (s.k > 1 && i1 - i0 > s.k))
     return cudaErrorInvalidValue;
   constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-  sweep_kernel<T, NT, MINB><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+  if (learned)
+  {
+    if (!s.mlp_simt || !s.mlp_params)
+      return cudaErrorInvalidValue;
+    sweep_kernel<T, NT, MINB, true><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+  }
+  else
+    sweep_kernel<T, NT, MINB, false><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
   return cudaGetLastError();
 }
 
 template<typename T>
-cudaError_t sweep_grid(const DevState<T>& s, int* grid)
+cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned)
 {
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -600,7 +730,10 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid)
   if (e != cudaSuccess)
     return e;
   constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB>, NT, sweep_smem_bytes(s));
+  e = learned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, true>, NT,
+                                                              sweep_smem_bytes(s))
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, false>, NT,
+                                                              sweep_smem_bytes(s));
   if (e != cudaSuccess)
     return e;
   if (per_sm < 1)
@@ -613,9 +746,9 @@ template cudaError_t setup_sweep_kernel<float>();
 template cudaError_t setup_sweep_kernel<double>();
 template size_t sweep_smem_bytes<float>(const DevState<float>&);
 template size_t sweep_smem_bytes<double>(const DevState<double>&);
-template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t);
-template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t);
-template cudaError_t sweep_grid<float>(const DevState<float>&, int*);
-template cudaError_t sweep_grid<double>(const DevState<double>&, int*);
+template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t, bool);
+template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t, bool);
+template cudaError_t sweep_grid<float>(const DevState<float>&, int*, bool);
+template cudaError_t sweep_grid<double>(const DevState<double>&, int*, bool);
 
 } // namespace qmcg

@@ -118,7 +118,7 @@ def test_zero_output_layer_is_drift_diffusion():
         g.mw_evaluateLog()
         if learned:
             g.proposal_init(seed=4)
-            a, r, _, _ = g.vmc_sweeps_learned(2, 0.3, 21)
+            a, r, _, _ = g.vmc_sweeps_learned(2, 0.3, 21, staged=True)
         else:
             a, r, _ = g.vmc_sweeps(2, 0.3, 21, rng_mode=1, staged=True)
         out.append((a, r, g.positions()))
@@ -144,15 +144,15 @@ def test_learned_sampling_is_unbiased():
         else:
             g.proposal_init(seed=7)
             g.set_proposal_params(_params(np.random.default_rng(8), w4_scale=0.5))
-            g.vmc_sweeps_learned(30, 0.3, 5)
-            _, _, el, _ = g.vmc_sweeps_learned(150, 0.3, 6, measure=True)
+            g.vmc_sweeps_learned(30, 0.3, 5, staged=True)
+            _, _, el, _ = g.vmc_sweeps_learned(150, 0.3, 6, measure=True, staged=True)
         res[mode] = energy_statistics(el)
     a, b = res["plain"], res["learned"]
     print("plain", a, "learned", b)
     assert abs(a["energy"] - b["energy"]) < 4 * np.hypot(a["error"], b["error"])
 
 
-def test_training_increases_jump_distance():
+def test_training_lowers_the_objective():
     Crowd, DeviceSystem = _gpu()
     s = _small(prec=8, n=8, nw=128, delay=4, seed=25)
     ds = DeviceSystem(s)
@@ -162,9 +162,57 @@ def test_training_increases_jump_distance():
     g.proposal_init(seed=1)
     g.vmc_sweeps(10, 0.3, 1, rng_mode=1)
     # lr = 0: the statistics of the untrained (drift-diffusion) proposal
-    _, _, _, (esjd0, acc0) = g.vmc_sweeps_learned(4, 0.3, 2, train=True, lr=0.0)
-    g.vmc_sweeps_learned(20, 0.3, 3, train=True, lr=2e-3)
-    _, _, _, (esjd1, acc1) = g.vmc_sweeps_learned(4, 0.3, 4, train=True, lr=0.0)
-    print("expected squared jump distance per move: before", esjd0, "after", esjd1,
-          "acceptance", acc0, "->", acc1)
-    assert np.isfinite(esjd1) and esjd1 > esjd0
+    _, _, _, (esjd0, acc0, obj0) = g.vmc_sweeps_learned(12, 0.3, 2, train=True, lr=0.0)
+    g.vmc_sweeps_learned(60, 0.3, 3, train=True, lr=2e-3)
+    _, _, _, (esjd1, acc1, obj1) = g.vmc_sweeps_learned(12, 0.3, 4, train=True, lr=0.0)
+    print("training objective per move: before", obj0, "after", obj1, "; expected squared jump", esjd0, "->",
+          esjd1, "; acceptance", acc0, "->", acc1)
+    assert np.isfinite(obj1) and obj1 < obj0
+
+
+def test_resident_zero_output_layer_is_drift_diffusion():
+    """Walker-resident inference with a zero output layer reproduces the resident
+    drift-diffusion sweep (FP64)."""
+    Crowd, DeviceSystem = _gpu()
+    s = _small(nw=8)
+    ds = DeviceSystem(s)
+    R = make_walkers(s, 8, seed=19)
+    out = []
+    for learned in (False, True):
+        g = Crowd(ds, 8, 4)
+        g.load_walkers(R)
+        g.mw_evaluateLog()
+        if learned:
+            g.proposal_init(seed=4)
+            a, r, _, _ = g.vmc_sweeps_learned(2, 0.3, 23)
+        else:
+            a, r, _ = g.vmc_sweeps(2, 0.3, 23, rng_mode=1)
+        out.append((a, r, g.positions()))
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    np.testing.assert_allclose(out[0][2], out[1][2], rtol=0, atol=1e-10)
+
+
+def test_resident_learned_sampling_is_unbiased():
+    """Walker-resident inference with a random network samples |psi|^2 (FP32 and FP64)."""
+    Crowd, DeviceSystem = _gpu()
+    for prec in (8, 4):
+        s = _small(prec=prec, n=8, nw=256, delay=4, seed=35)
+        ds = DeviceSystem(s)
+        R = make_walkers(s, 256, seed=36)
+        res = {}
+        for mode in ("plain", "learned"):
+            g = Crowd(ds, 256, 4)
+            g.load_walkers(R)
+            g.mw_evaluateLog()
+            if mode == "plain":
+                g.vmc_sweeps(30, 0.3, 5, rng_mode=1)
+                _, _, el, _ = g.vmc_sweeps_measure(200, 0.3, 6)
+            else:
+                g.proposal_init(seed=7)
+                g.set_proposal_params(_params(np.random.default_rng(9), w4_scale=0.5))
+                g.vmc_sweeps_learned(30, 0.3, 5)
+                _, _, el, _ = g.vmc_sweeps_learned(200, 0.3, 6, measure=True)
+            res[mode] = energy_statistics(el)
+        a, b = res["plain"], res["learned"]
+        print("precision", prec, "plain", a, "learned (resident)", b)
+        assert abs(a["energy"] - b["energy"]) < 4 * np.hypot(a["error"], b["error"])
