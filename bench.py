@@ -422,7 +422,7 @@ def run_ours(args, rank: int, world: int):
     base = cpu_baseline(args.workload) if world == 1 and not args.no_cpu_baseline else None
     eff = None
     rerr = None
-    if world == 1 and not args.no_effective and spec.precision == 4:
+    if world == 1 and not args.no_effective and args.workload == "c1_384e":
         rerr = ratio_error(system, dsys, 64, k)
         eff = effective_samples(args, system, dsys, seed + 11)
     line = {

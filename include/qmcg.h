@@ -90,7 +90,7 @@ typedef struct
                           sweep), else the staged per-electron kernels; 1: always the staged kernels */
   int flush;           /* delayed-update flush of the walker-resident path: 0 = SIMT (FP32 or FP64),
                           1 = tensor cores TF32, 3 = tensor cores 3xTF32 split precision (FP32 move loop,
-                          delay rank <= 32; otherwise the SIMT flush is used) */
+                          delay rank <= 64; otherwise the SIMT flush is used) */
 } qmcg_sweep_params;
 
 typedef struct
@@ -268,8 +268,10 @@ int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int d
 
 /* qmcg_mw_update_inv_mat with a choice of method: 0 = SIMT, 1 = tcgen05 tensor cores
  * in TF32, 3 = tcgen05 tensor cores in 3xTF32 split precision.  Methods 1 and 3 need
- * precision 4, delay_rank <= 32 and n, lda multiples of 4; other cases return
- * QMCG_ERR_ARG.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
+ * precision 4, delay_rank <= 64 and n, lda multiples of 4; other cases return
+ * QMCG_ERR_ARG.  Shapes whose whole product fits in tensor memory (delay_rank <= 32,
+ * n + 64 <= 512 columns) run in one pass; others run the second product over tiles of
+ * 128 inverse columns.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
 int qmcg_mw_update_inv_mat_ex(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                               void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                               int method, void* stream);

@@ -1837,7 +1837,7 @@ extern "C" int qmcg_mw_update_inv_mat_ex(int precision, int nw, int n, int lda, 
   if (rc)
     return rc;
   if (precision != 4 || !flush_tc_supported(n, k, lda))
-    return fail(QMCG_ERR_ARG, "tensor-core flush needs precision 4, delay_rank <= 32, n and lda multiples of 4");
+    return fail(QMCG_ERR_ARG, "tensor-core flush needs precision 4, delay_rank <= 64, n and lda multiples of 4");
   if (nw == 0 || dc == 0)
     return QMCG_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -377,31 +377,307 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(cols) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// N-tiled variant for large determinants and delay ranks up to 64: the second
+// product runs over column tiles of TT_TN inverse columns, W = Binv V is formed
+// per tile from global V, so neither N nor k is bounded by TMEM or by a full V in
+// shared memory.  TMEM: T1 in columns [0, 64), the product tile in [64, 64 + TT_TN).
+// ---------------------------------------------------------------------------
+constexpr int TT_KC = 32;  // K chunk of the first product
+constexpr int TT_TN = 128; // inverse columns per tile of the second product
+constexpr int TT_KMAX = 64;
+
+struct TtPlan
+{
+  int k1;                    // delay rank padded to 16
+  uint32_t a_hi, a_lo, u_hi, u_lo; // first product: 128 x KC and k1 x KC
+  uint32_t a2_hi, a2_lo, w_hi, w_lo; // second product: 128 x k1 and TN x k1
+  uint32_t binv, dl, bar, total;
+};
+
+__host__ __device__ inline TtPlan tt_plan(int k)
+{
+  TtPlan p;
+  p.k1    = ((k + 15) / 16) * 16;
+  auto al = [](uint32_t x) { return (x + 1023u) & ~1023u; };
+  uint32_t o = 0;
+  p.a_hi  = o; o = al(o + TC_M * TT_KC * 4);
+  p.a_lo  = o; o = al(o + TC_M * TT_KC * 4);
+  p.u_hi  = o; o = al(o + p.k1 * TT_KC * 4);
+  p.u_lo  = o; o = al(o + p.k1 * TT_KC * 4);
+  uint32_t o2 = 0;
+  p.a2_hi = o2; o2 = al(o2 + TC_M * p.k1 * 4);
+  p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
+  p.w_hi  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
+  p.w_lo  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
+  o = o > o2 ? o : o2;
+  p.binv  = o; o = al(o + k * k * 4);
+  p.dl    = o; o = al(o + k * 4);
+  p.bar   = o; o += 16;
+  p.total = al(o);
+  return p;
+}
+
+template<int TERMS>
+__global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<float> f, int* err)
+{
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+  const TtPlan P = tt_plan(f.k);
+  const int n = f.n, k = f.k, dc = f.dc, lda = f.lda, k1 = P.k1;
+  const int iw = blockIdx.x, r0 = blockIdx.y * TC_M;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float* A         = f.ainv + (size_t)iw * f.sA;
+  const float* U   = f.u + (size_t)iw * f.sU;
+  const float* V   = f.v + (size_t)iw * f.sU;
+  const float* Bi  = f.binv + (size_t)iw * f.sB;
+  const int* dlist = f.delay_list + (size_t)iw * f.sD;
+  float* Bs        = reinterpret_cast<float*>(sm + P.binv);
+  int* dls         = reinterpret_cast<int*>(sm + P.dl);
+  const uint32_t bar = smem_u32(sm + P.bar);
+  if (tid == 0)
+  {
+    s_fail = 0;
+    mbar_init(bar);
+  }
+  if (warp == 0)
+    tmem_alloc(smem_u32(&s_tmem), 256);
+  for (int e = tid; e < dc * dc; e += TC_NT)
+    Bs[e] = Bi[(size_t)(e / dc) * k + (e % dc)];
+  for (int e = tid; e < dc; e += TC_NT)
+    dls[e] = dlist[e];
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t d1 = tmem, d2 = tmem + 64;
+  uint32_t phase = 0;
+  auto split_store = [&](float4 x, uint32_t hi_base, uint32_t lo_base, uint32_t off) {
+    const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
+    *reinterpret_cast<float4*>(sm + hi_base + off) = h;
+    if (TERMS > 1)
+      *reinterpret_cast<float4*>(sm + lo_base + off) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
+  };
+  auto wait_mma = [&]() {
+    if (!mbar_wait(bar, phase))
+      atomicExch(&s_fail, 1);
+    phase ^= 1;
+    tc_fence_after();
+    __syncthreads();
+    return s_fail == 0;
+  };
+  // slot e of a (rows x KC) chunk: 8 consecutive slots fill one core matrix
+  auto slot_row = [](int e) { return (e / (8 * (TT_KC / 4))) * 8 + (e & 7); };
+  auto slot_col = [](int e) { return ((e >> 3) % (TT_KC / 4)) * 4; };
+  bool ok = true;
+
+  // ---------------- T1 = Ainv[rows] U^T over K = n in chunks of KC
+  constexpr int AV = TC_M * (TT_KC / 4) / TC_NT; // 8 float4 per thread
+  const int ub = k1 * (TT_KC / 4);
+  for (int k0 = 0; k0 < n && ok; k0 += TT_KC)
+  {
+#pragma unroll
+    for (int q = 0; q < AV; q++)
+    {
+      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e);
+      const int gr = r0 + r, gc = k0 + c4;
+      const float4 x = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
+                                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      split_store(x, P.a_hi, P.a_lo, cm_off(r, c4, TT_KC));
+    }
+    for (int e = tid; e < ub; e += TC_NT)
+    {
+      const int r = slot_row(e), c4 = slot_col(e), gc = k0 + c4;
+      const float4 x = (r < dc && gc < n) ? *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc)
+                                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      split_store(x, P.u_hi, P.u_lo, cm_off(r, c4, TT_KC));
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0)
+    {
+      tc_fence_after();
+      const uint32_t id = idesc_tf32(TC_M, k1);
+      const uint32_t ah = smem_u32(sm + P.a_hi), al = smem_u32(sm + P.a_lo);
+      const uint32_t bh = smem_u32(sm + P.u_hi), bl = smem_u32(sm + P.u_lo);
+      for (int ks = 0; ks < TT_KC / 8; ks++)
+      {
+        const uint32_t adv = ks * 256;
+        mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, (k0 == 0 && ks == 0) ? 0 : 1);
+        if (TERMS > 1)
+        {
+          mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bl + adv, TT_KC), id, 1);
+          mma_tf32(d1, smem_desc(al + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, 1);
+        }
+      }
+      mma_commit(bar);
+    }
+    ok = wait_mma();
+  }
+
+  // ---------------- (T1 - E) from TMEM into the second product's A operand
+  if (ok)
+  {
+    const int r = warp * 32 + lane;
+    for (int c0 = 0; c0 < k1; c0 += 32)
+    {
+      float t[32];
+      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        if (c0 + q < k1)
+        {
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+          {
+            const int c = c0 + q + u;
+            float x     = t[q + u];
+            if (c >= dc)
+              x = 0.f;
+            else if (dls[c] == r0 + r)
+              x -= 1.f;
+            v[u] = x;
+          }
+          split_store(make_float4(v[0], v[1], v[2], v[3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
+        }
+    }
+  }
+  // ---------------- column tiles: W_tile = Binv V[:, tile], P_tile = (T1 - E) W_tile^T, Ainv -= P
+  for (int t0 = 0; t0 < n && ok; t0 += TT_TN)
+  {
+    {
+      // thread i owns column t0 + i of the tile
+      const int i = tid;
+      const int col = t0 + i;
+      float vcol[TT_KMAX];
+#pragma unroll
+      for (int l = 0; l < TT_KMAX; l++)
+        vcol[l] = (l < dc && col < n) ? V[(size_t)l * lda + col] : 0.f;
+      for (int c4 = 0; c4 < k1; c4 += 4)
+      {
+        float w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+        {
+          const int c = c4 + q;
+          float a     = 0.f;
+          if (c < dc)
+#pragma unroll
+            for (int l = 0; l < TT_KMAX; l++)
+              if (l < dc)
+                a += Bs[c * dc + l] * vcol[l];
+          w[q] = a;
+        }
+        split_store(make_float4(w[0], w[1], w[2], w[3]), P.w_hi, P.w_lo, cm_off(i, c4, k1));
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0)
+    {
+      tc_fence_after();
+      const uint32_t id = idesc_tf32(TC_M, TT_TN);
+      const uint32_t ah = smem_u32(sm + P.a2_hi), al = smem_u32(sm + P.a2_lo);
+      const uint32_t bh = smem_u32(sm + P.w_hi), bl = smem_u32(sm + P.w_lo);
+      for (int ks = 0; ks < k1 / 8; ks++)
+      {
+        const uint32_t adv = ks * 256;
+        mma_tf32(d2, smem_desc(ah + adv, k1), smem_desc(bh + adv, k1), id, ks ? 1 : 0);
+        if (TERMS > 1)
+        {
+          mma_tf32(d2, smem_desc(ah + adv, k1), smem_desc(bl + adv, k1), id, 1);
+          mma_tf32(d2, smem_desc(al + adv, k1), smem_desc(bh + adv, k1), id, 1);
+        }
+      }
+      mma_commit(bar);
+    }
+    ok = wait_mma();
+    if (!ok)
+      break;
+    // epilogue: each thread one inverse row, 32 columns at a time
+    const int r  = warp * 32 + lane;
+    const int gr = r0 + r;
+    float* row   = A + (size_t)(gr < n ? gr : 0) * lda + t0;
+    for (int c0 = 0; c0 < TT_TN; c0 += 32)
+    {
+      float p[32];
+      tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
+      if (gr < n)
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          if (t0 + c0 + 4 * q < n)
+          {
+            float4 a = *reinterpret_cast<const float4*>(row + c0 + 4 * q);
+            a.x -= p[4 * q];
+            a.y -= p[4 * q + 1];
+            a.z -= p[4 * q + 2];
+            a.w -= p[4 * q + 3];
+            *reinterpret_cast<float4*>(row + c0 + 4 * q) = a;
+          }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok && tid == 0)
+    atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    tmem_dealloc(tmem, 256);
+}
+
+// the compact kernel: whole product in TMEM, k <= 32
+static bool flush_tc_compact_ok(int n, int k)
+{
+  const TcPlan p = tc_plan(n, k);
+  return k <= 32 && 64 + p.npad <= 512 && p.total <= 200 * 1024;
+}
+
 bool flush_tc_supported(int n, int k, int lda)
 {
-  // 64 + n_pad TMEM columns, one 128-row block per CTA, 16-byte aligned rows
-  const TcPlan p = tc_plan(n, k);
-  return k <= 32 && 64 + p.npad <= 512 && (lda % 4) == 0 && (n % 4) == 0 && p.total <= 200 * 1024;
+  // 16-byte aligned rows; delay rank up to 64 (the tiled kernel covers any N)
+  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k).total <= 200 * 1024;
 }
 
 cudaError_t setup_flush_tc()
 {
   cudaError_t e = cudaFuncSetAttribute(flush_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  if (e != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(flush_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(flush_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(flush_tc_tiled_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(flush_tc_tiled_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  return e;
 }
 
 cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cudaStream_t st)
 {
   if (f.dc <= 0 || f.nw <= 0)
     return cudaSuccess;
-  const TcPlan p = tc_plan(f.n, f.k);
   dim3 grid(f.nw, (f.n + TC_M - 1) / TC_M);
-  if (terms == 1)
-    flush_tc_kernel<1><<<grid, TC_NT, p.total, st>>>(f, err);
+  if (flush_tc_compact_ok(f.n, f.k))
+  {
+    const TcPlan p = tc_plan(f.n, f.k);
+    if (terms == 1)
+      flush_tc_kernel<1><<<grid, TC_NT, p.total, st>>>(f, err);
+    else
+      flush_tc_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
+  }
   else
-    flush_tc_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
+  {
+    if (f.k > TT_KMAX)
+      return cudaErrorInvalidValue;
+    const TtPlan p = tt_plan(f.k);
+    if (terms == 1)
+      flush_tc_tiled_kernel<1><<<grid, TC_NT, p.total, st>>>(f, err);
+    else
+      flush_tc_tiled_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
+  }
   return cudaGetLastError();
 }
 

@@ -3,7 +3,8 @@
 Checked against the NumPy FP64 restatement of DelayedUpdate::updateInvMat
 (src/QMCWaveFunctions/Fermion/DelayedUpdate.h:145-215) used in
 tests/test_gpu_det_engine.py.  Tolerances (max error over the largest element):
-3xTF32 1e-5, TF32 5e-3 (TF32 keeps 10 mantissa bits, unit roundoff 2^-11).
+3xTF32 1e-5, TF32 5e-3 (TF32 keeps 10 mantissa bits, unit roundoff 2^-11).  The C2 shape
+(n = 768, k = 64) reports both errors against FP64.
 """
 import numpy as np
 import pytest
@@ -33,7 +34,10 @@ def call_ex(method, arrays, dc):
 
 @pytest.mark.parametrize("method,tol", [(3, 1e-5), (1, 5e-3)])
 @pytest.mark.parametrize("nw,n,lda,k,dc", [(3, 20, 32, 4, 4), (2, 64, 64, 16, 9), (4, 192, 192, 32, 32),
-                                           (2, 200, 208, 32, 17)])
+                                           (2, 200, 208, 32, 17),
+                                           # N-tiled kernel: k > 32 or n + 64 > 512 tensor-memory columns
+                                           (3, 192, 192, 64, 37), (2, 300, 304, 48, 41), (2, 520, 528, 16, 9),
+                                           (2, 768, 768, 64, 64)])
 def test_tensor_core_flush(method, tol, nw, n, lda, k, dc):
     arrays = flush_case(nw, n, lda, k, dc, seed=7 * n + dc)
     rc, got, L = call_ex(method, arrays, dc)
