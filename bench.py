@@ -342,7 +342,8 @@ def run_ours(args, rank: int, world: int):
     R = make_walkers(system, nw, seed=100 + rank)
     crowd.load_walkers(R)
     crowd.mw_evaluateLog()
-    seed = 2024 + 7919 * rank
+    from qmcpack_gb300.replicas import aggregate_timing, replica_seed
+    seed = replica_seed(2024, rank)
     recompute_every = spec.recompute_every
     # equilibration from the uniform start (untimed), then warm-up (also captures the sweep graph)
     if args.equil > 0:
@@ -366,11 +367,7 @@ def run_ours(args, rank: int, world: int):
     ms = e0.elapsed_time(e1)
     acc, rej = crowd.sync()
     repaired = crowd.last_repaired
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    moves = args.steps * nw * system.n_elec * world
+    moves, ms = aggregate_timing(args.steps * nw * system.n_elec, ms)
     value = moves / (ms / 1e3)
     sweeps_done = args.equil + args.warmup
     recomputes = 0
@@ -391,10 +388,7 @@ def run_ours(args, rank: int, world: int):
         lp, _, _ = crowd.get_log()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    _, e2e_s = aggregate_timing(0.0, e2e_s)
     e2e_value = moves / e2e_s
     h2d = Rnp.nbytes
     d2h = Rnp.nbytes + lp.nbytes
