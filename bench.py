@@ -38,6 +38,9 @@ DESCRIPTIONS = {
                "every 100 sweeps",
     "c0_32e": "32 electrons, 16 orbitals on a 32^3 grid, 8 ions, a=10 bohr, 64 walkers, rank-1 updates, FP64",
     "c2_1536e": "1536 electrons, 768 orbitals on a 60^3 grid, 128 ions, a=25 bohr, 256 walkers, delay rank 64, FP32",
+    "c3_mixed": "uneven crowd of 1024 walkers: 410 on the 32-electron system, 410 on the 384-electron system, "
+                "204 on a 768-electron system (384 orbitals, 40^3 grid, 64 ions, a=20 bohr), FP32, one persistent "
+                "launch per stage, delay rank autotuned per system",
 }
 
 
@@ -302,8 +305,121 @@ def torch_sync():
         pass
 
 
+def c3_systems():
+    from qmcpack_gb300.system import scaled_spec
+    return [make_system(scaled_spec("c0_32e", precision=4, walkers=410)),
+            make_system(scaled_spec("c1_384e", walkers=410)),
+            make_system(scaled_spec("c3_768e", walkers=204))]
+
+
+def run_c3(args, rank: int, world: int):
+    """Uneven crowd: the three systems swept together by qmcg_group_sweeps (one persistent
+    launch per stage), against sweeping the crowds one after the other."""
+    import torch
+    from qmcpack_gb300.autotune import tune
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem, Group
+    from qmcpack_gb300.replicas import aggregate_timing, replica_seed
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seed = replica_seed(2024, rank)
+    systems = c3_systems()
+    dss = [DeviceSystem(s) for s in systems]
+    tuned = [tune(s, s.spec.walkers, dsys=ds, flush=args.flush) for s, ds in zip(systems, dss)]
+    crowds = []
+    for i, (s, ds, t) in enumerate(zip(systems, dss, tuned)):
+        g = Crowd(ds, s.spec.walkers, t["delay"])
+        g.load_walkers(make_walkers(s, s.spec.walkers, seed=50 + i + 100 * rank))
+        g.mw_evaluateLog()
+        g.vmc_sweeps(max(args.equil // 2, 1), 0.3, seed + i, rng_mode=1, flush=args.flush)
+        crowds.append(g)
+    moves_per_sweep = sum(s.spec.walkers * s.n_elec for s in systems)
+    # one after the other: each crowd's own sweep graph
+    for g in crowds:
+        g.vmc_sweeps(args.warmup, 0.3, seed, rng_mode=1, flush=args.flush)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g in crowds:
+        g.vmc_sweeps_async(args.steps)
+    for g in crowds:
+        g.sync()
+    seq_s = time.perf_counter() - t0
+    grp = Group(crowds)
+    grp.sweeps(args.warmup, 0.3, seed, flush=args.flush)
+    stream = torch.cuda.ExternalStream(crowds[0].stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    stats = grp.sweeps(args.steps, 0.3, seed + 1, flush=args.flush)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    moves, ms = aggregate_timing(args.steps * moves_per_sweep, ms)
+    value = moves / (ms / 1e3)
+    # end to end through the C ABI with host buffers (positions in and out of every crowd)
+    hosts = [g.positions() for g in crowds]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for g, h in zip(crowds, hosts):
+            g.load_walkers(h)
+        grp.sweeps(1, 0.3, seed + 2, flush=args.flush)
+        for i, g in enumerate(crowds):
+            hosts[i] = g.positions()
+    e2e_s = time.perf_counter() - t0
+    _, e2e_s = aggregate_timing(0.0, e2e_s)
+    h2d = sum(h.nbytes for h in hosts)
+    algo = sum(bytes_per_walker_move(s, t["delay"]) * s.spec.walkers * s.n_elec for s, t in zip(systems, tuned))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs") or 6800.0
+    achieved = algo / (ms / args.steps / 1e3) / 1e9
+    info = grp.info()
+    if rank != 0:
+        return
+    acc = sum(x[0] for x in stats)
+    rej = sum(x[1] for x in stats)
+    line = {
+        "metric": "walker-moves/s", "value": value, "unit": "walker-moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"c3_mixed: {DESCRIPTIONS['c3_mixed']}",
+                   "step": "one VMC sweep of every crowd (group graph: one persistent launch per stage + flushes)",
+                   "crowds": [{"electrons": s.n_elec, "orbitals": s.norb, "walkers": s.spec.walkers,
+                               "delay_rank": t["delay"], "autotune_ms_per_sweep": t["table"]}
+                              for s, t in zip(systems, tuned)],
+                   "group": info, "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "whole group sweep (sweep_multi_kernel stages + flushes + repair)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs")
+                     else "fallback 6.8 TB/s", "traffic": None, "algorithmic_bytes_per_sweep": algo},
+        "cpu_baseline": None,
+        "e2e": {"value": moves / e2e_s, "unit": "walker-moves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": h2d},
+        "gpu_launches": (2 * info["stages"] + 6) * args.steps,
+        "clocks": clk,
+        "acceptance": acc / max(acc + rej, 1),
+        "sequential_crowds": {"value": args.steps * moves_per_sweep / seq_s, "unit": "walker-moves/s",
+                              "what": "the same crowds swept one after the other, each from its own graph"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
+        return
+    if args.workload not in SPECS:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement is timed on single-system "
+                          "workloads only (c0_32e, c1_384e, c2_1536e, c3_768e)"}), flush=True)
         return
     spec = SPECS[args.workload]
     base = cpu_baseline(args.workload, max_seconds=max(5.0, 60.0 / max(args.steps, 1)))
@@ -463,7 +579,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS))
+    ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS) + ["c3_mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--equil", type=int, default=20, help="untimed equilibration sweeps before the warm-up")
     ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
@@ -481,6 +597,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "c3_mixed":
+        run_c3(args, rank, world)
     else:
         run_ours(args, rank, world)
 

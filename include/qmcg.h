@@ -34,6 +34,7 @@ extern "C" {
 
 typedef struct qmcg_system_s* qmcg_system;
 typedef struct qmcg_crowd_s* qmcg_crowd;
+typedef struct qmcg_group_s* qmcg_group;
 
 /* A Slater-Jastrow system: what QMCPACK reads from its XML input for this path.
  *   cell       orthorhombic, periodic in x, y, z (DTD_BConds<T,3,PPPO>,
@@ -248,6 +249,22 @@ int qmcg_proposal_features(qmcg_crowd crowd, int iat, int at_proposed, float* x)
 int qmcg_vmc_sweeps_learned(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, int train, double lr,
                             double* e_local, qmcg_sweep_stats* stats, double* train_stats);
 
+/* ---------------------------------------------------------------- uneven crowds
+ * No single reference counterpart: QMCPACK runs one crowd per thread, each with its
+ * own launches.  A group sweeps crowds of different systems (up to 8, one precision,
+ * the crowds keep their state and ownership) together: per stage, ONE persistent
+ * launch of the walker-resident kernel covers the stage's segment of every crowd
+ * (work items (crowd, walker) handed out through a device counter, most expensive
+ * crowd first), followed by each crowd's delayed-update flush; one CUDA graph per
+ * sweep on the first crowd's stream.  Every crowd gets its own counter-based stream
+ * (params->seed mixed with the crowd's index). */
+int qmcg_group_create(const qmcg_crowd* crowds, int num_crowds, qmcg_group* out);
+int qmcg_group_destroy(qmcg_group group);
+/* rng_mode must be 1; stats (may be NULL) [num_crowds]. */
+int qmcg_group_sweeps(qmcg_group group, const qmcg_sweep_params* params, int num_sweeps, qmcg_sweep_stats* stats);
+/* out[3]: stages per sweep, CTAs of the persistent launch, shared memory bytes per CTA. */
+int qmcg_group_info(qmcg_group group, int* out);
+
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);
 
@@ -269,9 +286,9 @@ int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int d
 /* qmcg_mw_update_inv_mat with a choice of method: 0 = SIMT, 1 = tcgen05 tensor cores
  * in TF32, 3 = tcgen05 tensor cores in 3xTF32 split precision.  Methods 1 and 3 need
  * precision 4, delay_rank <= 64 and n, lda multiples of 4; other cases return
- * QMCG_ERR_ARG.  Shapes whose whole product fits in tensor memory (delay_rank <= 32,
- * n + 64 <= 512 columns) run in one pass; others run the second product over tiles of
- * 128 inverse columns.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
+ * QMCG_ERR_ARG.  Shapes whose second product is one MMA (delay_rank <= 32, n padded to
+ * 16 <= 256) run in one pass; others run the second product over tiles of 128 inverse
+ * columns.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
 int qmcg_mw_update_inv_mat_ex(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                               void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                               int method, void* stream);

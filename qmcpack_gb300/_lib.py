@@ -22,6 +22,7 @@ EXPORTS = [
     "qmcg_profile_sweep", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
     "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
     "qmcg_proposal_backward", "qmcg_proposal_features", "qmcg_vmc_sweeps_learned",
+    "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info",
 ]
 PROPOSAL_NUM_PARAMS = 43408
 _fp = C.POINTER(C.c_float)
@@ -102,6 +103,10 @@ def load(path: str = LIB_PATH):
         "qmcg_proposal_features": [vp, C.c_int, C.c_int, _fp],
         "qmcg_vmc_sweeps_learned": [vp, C.POINTER(SweepParams), C.c_int, C.c_int, C.c_double, _dp,
                                     C.POINTER(SweepStats), _dp],
+        "qmcg_group_create": [C.POINTER(vp), C.c_int, C.POINTER(vp)],
+        "qmcg_group_destroy": [vp],
+        "qmcg_group_sweeps": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats)],
+        "qmcg_group_info": [vp, _ip],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

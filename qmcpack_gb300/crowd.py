@@ -267,3 +267,41 @@ class Crowd:
         p = C.c_void_p()
         check(self.L.qmcg_crowd_stream(self.handle, C.byref(p)))
         return p.value or 0
+
+
+def group_seed(seed: int, index: int) -> int:
+    """The counter-based stream seed a group gives its index-th crowd."""
+    return (seed ^ ((0x9E3779B97F4A7C15 * (index + 1)) & 0xFFFFFFFFFFFFFFFF)) & 0xFFFFFFFFFFFFFFFF
+
+
+class Group:
+    """Crowds of different systems swept together, one persistent launch per stage."""
+
+    def __init__(self, crowds):
+        self.L = _lib.load()
+        self.crowds = list(crowds)
+        arr = (C.c_void_p * len(self.crowds))(*[c.handle.value for c in self.crowds])
+        self.handle = C.c_void_p()
+        check(self.L.qmcg_group_create(arr, len(self.crowds), C.byref(self.handle)))
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            self.L.qmcg_group_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def sweeps(self, nsweeps: int, tau: float, seed: int, use_drift: bool = True, recompute_every: int = 0,
+               flush: int = 0):
+        """[(accepted, rejected, repaired) per crowd]"""
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
+                        recompute_every=recompute_every, path=0, flush=flush)
+        st = (SweepStats * len(self.crowds))()
+        check(self.L.qmcg_group_sweeps(self.handle, C.byref(p), nsweeps, st))
+        return [(x.accepted, x.rejected, x.repaired) for x in st]
+
+    def info(self):
+        out = np.zeros(3, np.int32)
+        check(self.L.qmcg_group_info(self.handle, _p(out, _ip)))
+        return {"stages": int(out[0]), "ctas": int(out[1]), "smem_bytes": int(out[2])}

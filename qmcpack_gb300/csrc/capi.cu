@@ -888,12 +888,30 @@ struct Crowd final : qmcg_crowd_s
   bool resident(const qmcg_sweep_params* p) const { return p->rng_mode == 1 && p->path == 0; }
 
   // the flush of one spin after a resident segment: tensor cores when asked for and possible
-  cudaError_t launch_flush_choice(int spin, int dc)
+  cudaError_t launch_flush_choice(int spin, int dc, cudaStream_t st = nullptr)
   {
+    if (!st)
+      st = stream;
     if constexpr (std::is_same<T, float>::value)
       if ((flush_kind == 1 || flush_kind == 3) && flush_tc_supported(sys->norb, k, sys->lda))
-        return launch_flush_tc(crowd_flush_args<float>(s, spin, dc, W), flush_kind, tc_err, stream);
-    return launch_flush_fused<T>(crowd_flush_args<T>(s, spin, dc, W), stream);
+        return launch_flush_tc(crowd_flush_args<float>(s, spin, dc, W), flush_kind, tc_err, st);
+    return launch_flush_fused<T>(crowd_flush_args<T>(s, spin, dc, W), st);
+  }
+
+  // the segments [i0, i1) of one sweep on the walker-resident path, in launch order
+  std::vector<std::pair<int, int>> segments() const
+  {
+    std::vector<std::pair<int, int>> out;
+    for (int g = 0; g < 2; g++)
+    {
+      const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
+      if (k > 1)
+        for (int i0 = first; i0 < last; i0 += k)
+          out.push_back({i0, std::min(i0 + k, last)});
+      else
+        out.push_back({first, last});
+    }
+    return out;
   }
 
   // one sweep on the walker-resident path: with delayed updates, one resident
@@ -1625,6 +1643,244 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 };
+
+// ---------------------------------------------------------------------------
+// crowds of different systems swept together: one persistent launch per stage
+// ---------------------------------------------------------------------------
+struct qmcg_group_s
+{
+  virtual ~qmcg_group_s() = default;
+  virtual int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st) = 0;
+  virtual int info(int* out) = 0;
+};
+
+template<typename T>
+struct Group final : qmcg_group_s
+{
+  std::vector<Crowd<T>*> cs;
+  cudaStream_t stream = nullptr; // the first crowd's stream
+  DeviceArena mem;
+  DevState<T>* table = nullptr;
+  int* work          = nullptr; // one dynamic work counter per stage
+  std::vector<MultiStage> stages;
+  size_t smem = 0;
+  int grid    = 0;
+  cudaGraphExec_t graph = nullptr;
+  double g_tau = 0;
+  uint64_t g_seed = 0;
+  int g_drift = -1, g_flush = -1;
+  std::vector<int> since_recompute;
+
+  ~Group() override
+  {
+    if (graph)
+      cudaGraphExecDestroy(graph);
+  }
+
+  int init(const std::vector<Crowd<T>*>& crowds)
+  {
+    cs     = crowds;
+    stream = cs[0]->stream;
+    since_recompute.assign(cs.size(), 0);
+    for (auto* c : cs)
+      smem = std::max(smem, sweep_smem_bytes<T>(c->s));
+    if (smem > 220 * 1024)
+      return fail(QMCG_ERR_ARG, "group: a crowd's walker state does not fit in shared memory");
+    CUDA_TRY(sweep_multi_grid<T>(smem, &grid));
+    CUDA_TRY(mem.alloc(&table, cs.size()));
+    // stages: the j-th segment of every crowd; crowds ordered by cost per walker (largest first)
+    std::vector<int> order(cs.size());
+    for (size_t c = 0; c < cs.size(); c++)
+      order[c] = (int)c;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+      const double ca = (double)cs[a]->sys->ne * cs[a]->sys->lda, cb = (double)cs[b]->sys->ne * cs[b]->sys->lda;
+      return ca > cb;
+    });
+    size_t nst = 0;
+    for (auto* c : cs)
+      nst = std::max(nst, c->segments().size());
+    for (size_t j = 0; j < nst; j++)
+    {
+      MultiStage st{};
+      st.nactive = 0;
+      st.begin[0] = 0;
+      for (int c : order)
+      {
+        const auto seg = cs[c]->segments();
+        if (j >= seg.size())
+          continue;
+        const int a = st.nactive++;
+        st.crowd[a]     = c;
+        st.i0[a]        = seg[j].first;
+        st.i1[a]        = seg[j].second;
+        st.begin[a + 1] = st.begin[a] + cs[c]->nw;
+      }
+      stages.push_back(st);
+    }
+    CUDA_TRY(mem.alloc(&work, stages.size()));
+    return QMCG_OK;
+  }
+
+  int build(const qmcg_sweep_params* p)
+  {
+    if (graph && g_tau == p->tau && g_seed == p->seed && g_drift == p->use_drift && g_flush == p->flush)
+      return QMCG_OK;
+    if (graph)
+    {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    std::vector<DevState<T>> h(cs.size());
+    for (size_t c = 0; c < cs.size(); c++)
+    {
+      Crowd<T>* x = cs[c];
+      if (x->graph)
+      {
+        cudaGraphExecDestroy(x->graph);
+        x->graph = nullptr;
+      }
+      x->s.rng_mode  = 1;
+      x->s.use_drift = p->use_drift;
+      x->s.tau       = p->tau;
+      // independent counter-based streams per crowd
+      x->s.seed   = p->seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(c + 1));
+      x->flush_kind = p->flush;
+      h[c]        = x->s;
+    }
+    CUDA_TRY(cudaMemcpy(table, h.data(), h.size() * sizeof(DevState<T>), cudaMemcpyHostToDevice));
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue();
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (rc)
+      return rc;
+    if (e != cudaSuccess)
+      return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    g_tau   = p->tau;
+    g_seed  = p->seed;
+    g_drift = p->use_drift;
+    g_flush = p->flush;
+    return QMCG_OK;
+  }
+
+  int enqueue()
+  {
+    CUDA_TRY(cudaMemsetAsync(work, 0, stages.size() * sizeof(int), stream));
+    for (size_t j = 0; j < stages.size(); j++)
+    {
+      const MultiStage& st = stages[j];
+      CUDA_TRY(launch_sweep_multi<T>(table, st, smem, grid, work + j, stream));
+      for (int a = 0; a < st.nactive; a++)
+      {
+        Crowd<T>* x = cs[st.crowd[a]];
+        if (x->k > 1)
+          CUDA_TRY(x->launch_flush_choice(st.i0[a] >= x->sys->nup ? 1 : 0, st.i1[a] - st.i0[a], stream));
+      }
+    }
+    for (auto* x : cs)
+    {
+      CUDA_TRY(launch_recompute<T>(x->s, x->Mt, 1, stream));
+      bump_counter_kernel<<<1, 1, 0, stream>>>(x->s.sweep_counter);
+      CUDA_TRY(cudaGetLastError());
+    }
+    return QMCG_OK;
+  }
+
+  int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st) override
+  {
+    if (!p || n < 0 || !(p->tau > 0) || p->rng_mode != 1)
+      return fail(QMCG_ERR_ARG, "group sweeps need tau > 0 and the device random numbers (rng_mode 1)");
+    for (auto* x : cs)
+      if (x->dc[0] || x->dc[1])
+      {
+        int rc = x->complete();
+        if (rc)
+          return rc;
+      }
+    // every crowd's pending work is ordered before the group's stream
+    for (auto* x : cs)
+      CUDA_TRY(cudaStreamSynchronize(x->stream));
+    int rc = build(p);
+    if (rc)
+      return rc;
+    for (auto* x : cs)
+      CUDA_TRY(cudaMemsetAsync(x->s.counters, 0, 3 * sizeof(unsigned long long), stream));
+    for (int it = 0; it < n; it++)
+    {
+      CUDA_TRY(cudaGraphLaunch(graph, stream));
+      for (size_t c = 0; c < cs.size(); c++)
+        if (p->recompute_every > 0 && ++since_recompute[c] >= p->recompute_every)
+        {
+          CUDA_TRY(launch_recompute<T>(cs[c]->s, cs[c]->Mt, 0, stream));
+          since_recompute[c] = 0;
+        }
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    for (size_t c = 0; c < cs.size(); c++)
+    {
+      rc = cs[c]->sync(st ? st + c : nullptr);
+      if (rc)
+        return rc;
+    }
+    return QMCG_OK;
+  }
+
+  // out: [0] stages per sweep, [1] CTAs of the persistent launch, [2] shared memory bytes per CTA
+  int info(int* out) override
+  {
+    out[0] = (int)stages.size();
+    out[1] = grid;
+    out[2] = (int)smem;
+    return QMCG_OK;
+  }
+};
+
+extern "C" int qmcg_group_create(const qmcg_crowd* crowds, int n, qmcg_group* out)
+{
+  if (!crowds || !out || n < 1 || n > MULTI_MAX)
+    return fail(QMCG_ERR_ARG, "need 1..8 crowds");
+  *out = nullptr;
+  for (int c = 0; c < n; c++)
+    if (!crowds[c] || crowds[c]->sys->prec != crowds[0]->sys->prec)
+      return fail(QMCG_ERR_ARG, "group crowds must exist and share one precision");
+  auto make = [&](auto tag) -> int {
+    using TT = decltype(tag);
+    std::vector<Crowd<TT>*> v;
+    for (int c = 0; c < n; c++)
+      v.push_back(static_cast<Crowd<TT>*>(crowds[c]));
+    auto g = std::make_unique<Group<TT>>();
+    int rc = g->init(v);
+    if (rc)
+      return rc;
+    *out = g.release();
+    return QMCG_OK;
+  };
+  return crowds[0]->sys->prec == 8 ? make(double{}) : make(float{});
+}
+
+extern "C" int qmcg_group_destroy(qmcg_group g)
+{
+  delete g;
+  return QMCG_OK;
+}
+
+extern "C" int qmcg_group_sweeps(qmcg_group g, const qmcg_sweep_params* p, int n, qmcg_sweep_stats* stats)
+{
+  if (!g)
+    return fail(QMCG_ERR_ARG, "null group");
+  return g->sweeps(p, n, stats);
+}
+
+extern "C" int qmcg_group_info(qmcg_group g, int* out)
+{
+  if (!g || !out)
+    return fail(QMCG_ERR_ARG, "null argument");
+  return g->info(out);
+}
 
 extern "C" int qmcg_crowd_create(qmcg_system sys, int nw, int k, qmcg_crowd* out)
 {

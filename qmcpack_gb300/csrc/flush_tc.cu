@@ -630,11 +630,12 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
     tmem_dealloc(tmem, 256);
 }
 
-// the compact kernel: whole product in TMEM, k <= 32
+// the compact kernel: whole product in TMEM, k <= 32, and the second product is one
+// MMA whose N = n_pad must not exceed 256 (the largest N of tcgen05.mma with M = 128)
 static bool flush_tc_compact_ok(int n, int k)
 {
   const TcPlan p = tc_plan(n, k);
-  return k <= 32 && 64 + p.npad <= 512 && p.total <= 200 * 1024;
+  return k <= 32 && p.npad <= 256 && p.total <= 200 * 1024;
 }
 
 bool flush_tc_supported(int n, int k, int lda)

@@ -39,6 +39,20 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned = false);
 template<typename T>
 cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st,
                                  bool learned = false);
+// uneven crowds: one launch per stage over (crowd, walker) work items
+constexpr int MULTI_MAX = 8;
+struct MultiStage
+{
+  int nactive;                 // crowds with a segment in this stage
+  int crowd[MULTI_MAX];        // their indices in the state table, most expensive first
+  int i0[MULTI_MAX], i1[MULTI_MAX];
+  int begin[MULTI_MAX + 1];    // prefix of walker counts: items [begin[a], begin[a+1]) belong to crowd[a]
+};
+template<typename T>
+cudaError_t launch_sweep_multi(const DevState<T>* table, const MultiStage& st, size_t smem, int grid, int* work,
+                               cudaStream_t stm);
+template<typename T>
+cudaError_t sweep_multi_grid(size_t smem, int* grid);
 // batched, shared-memory-staged flush of one spin for all walkers (flush_kernels.cu);
 // falls back to the two-kernel SIMT flush when the tiles do not fit
 template<typename T>

@@ -126,10 +126,26 @@ struct LearnedSmem<T, true>
   T p;
 };
 
-template<typename T, int NT, int MINB, bool LEARNED>
-__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
+// per-CTA scalars of the resident sweep in shared memory
+template<typename T, bool LEARNED>
+struct SweepShared
 {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double pos[3];
+  T disp[3];
+  T gauss[3];
+  T loggf;
+  int acc;
+  T det;
+  T cur[10];
+  LearnedSmem<T, LEARNED> lsm;
+};
+
+// The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.
+template<typename T, int NT, bool LEARNED>
+__device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i1, int w, unsigned char* smem_raw,
+                                             SweepShared<T, LEARNED>& sh, unsigned long long& n_acc,
+                                             unsigned long long& n_rej)
+{
   const int lda = s.lda, n = s.norb, K = s.k;
   T* part   = reinterpret_cast<T*>(smem_raw); // 28 x lda
   T* pre    = part + 28 * lda;                // 2 x 5 x lda prefetch buffers
@@ -143,20 +159,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
   T* tv     = pv + K;                         // K
   T* yv     = tv + K;                         // K
   T* red    = yv + K;                         // 16 x 32
-  __shared__ double s_pos[3];
-  __shared__ T s_disp[3];
-  __shared__ T s_gauss[3];
-  __shared__ T s_loggf;
-  __shared__ int s_acc;
-  __shared__ T s_det;
-  __shared__ T s_cur[10];
-  __shared__ LearnedSmem<T, LEARNED> lsm;
   const __nv_bfloat162* ml_pairs = reinterpret_cast<const __nv_bfloat162*>(s.mlp_simt);
   const __nv_bfloat16* ml_w4 = reinterpret_cast<const __nv_bfloat16*>(ml_pairs + MS_NPAIRS);
 
   const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
-  unsigned long long n_acc = 0, n_rej = 0;
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
   const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
   const T tau       = T(s.tau);
@@ -164,8 +171,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
   const int first   = spin ? s.nup : 0;
   const int lane    = threadIdx.x & 31, wid = threadIdx.x >> 5;
   (void)spare;
+  (void)ml_w4;
 
-  for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
   {
     const size_t slot = (size_t)spin * s.nw + w;
     for (int e = threadIdx.x; e < 3 * s.ne_pad; e += NT)
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
       const T* dg   = arow + lda;
       const T* pv0  = arow + 4 * lda;
       if (threadIdx.x == 32)
-        gaussians<T>((uint32_t)w, (uint32_t)iat, sweep, k0, k1, s_gauss);
+        gaussians<T>((uint32_t)w, (uint32_t)iat, sweep, k0, k1, sh.gauss);
       async_wait_all();
       __syncthreads();
       // ------------------------------------------------ up-to-date inverse row
@@ -254,31 +261,31 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
                 gs += s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat];
               if (s.has_j2)
                 gs += J2s[(1 + d) * s.ne_pad + iat];
-              lsm.g[d] = gs;
+              sh.lsm.g[d] = gs;
             }
           }
           __syncthreads();
           const T pc[3] = {Rs[iat], Rs[s.ne_pad + iat], Rs[2 * s.ne_pad + iat]};
-          features_cta(s, Rs, iat, pc, lsm.g, lsm.x);
+          features_cta(s, Rs, iat, pc, sh.lsm.g, sh.lsm.x);
           __syncthreads();
-          mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, lsm.x, lsm.h, lsm.red, lsm.out);
+          mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, sh.lsm.x, sh.lsm.h, sh.lsm.red, sh.lsm.out);
           if (threadIdx.x == 0)
           {
             const T st = sqrt(tau);
             T drift[3];
-            unr_drift_t(tau, lsm.g, drift);
+            unr_drift_t(tau, sh.lsm.g, drift);
             T sum_s = 0, x2 = 0;
             for (int d = 0; d < 3; d++)
             {
-              const T mu = T(clampf(lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
-              const T sd = T(clampf(lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+              const T mu = T(clampf(sh.lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
+              const T sd = T(clampf(sh.lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
               sum_s += sd;
-              x2 += s_gauss[d] * s_gauss[d];
-              const T dd = drift[d] + st * mu + st * exp(sd) * s_gauss[d];
-              s_disp[d]  = dd;
-              s_pos[d]   = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(dd);
+              x2 += sh.gauss[d] * sh.gauss[d];
+              const T dd = drift[d] + st * mu + st * exp(sd) * sh.gauss[d];
+              sh.disp[d]  = dd;
+              sh.pos[d]   = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(dd);
             }
-            s_loggf = -sum_s - T(0.5) * x2;
+            sh.loggf = -sum_s - T(0.5) * x2;
           }
           __syncthreads();
         }
@@ -301,7 +308,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
           const T sqrttau = sqrt(tau);
           T delta[3], drift[3];
           for (int d = 0; d < 3; d++)
-            delta[d] = s_gauss[d] * sqrttau;
+            delta[d] = sh.gauss[d] * sqrttau;
           if (s.use_drift)
           {
             unr_drift_t(tau, gn, drift);
@@ -313,10 +320,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
               drift[d] = delta[d];
           for (int d = 0; d < 3; d++)
           {
-            s_disp[d] = drift[d];
-            s_pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
+            sh.disp[d] = drift[d];
+            sh.pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
           }
-          s_loggf = s.use_drift
+          sh.loggf = s.use_drift
               ? -(T(0.5) / tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
               : T(0);
         }
@@ -324,7 +331,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         }
       }
       // ------------------------------------------------ evaluation at the proposed position
-      const double pos[3] = {s_pos[0], s_pos[1], s_pos[2]};
+      const double pos[3] = {sh.pos[0], sh.pos[1], sh.pos[2]};
       spline_partials(s, pos, part);
       T acc[14];
 #pragma unroll
@@ -411,22 +418,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         const T p = detr * detr * exp(T(2) * logj);
         if (!isfinite(p) || (p != T(0) && (!isfinite(g[0]) || !isfinite(g[1]) || !isfinite(g[2]))))
           atomicOr(s.status + w, ST_NONFINITE);
-        s_det    = detr;
-        s_cur[0] = acc[10];
-        s_cur[1] = acc[11];
-        s_cur[2] = acc[12];
-        s_cur[3] = acc[13];
-        s_cur[4] = acc[4];
-        s_cur[5] = acc[5];
-        s_cur[6] = acc[6];
-        s_cur[7] = acc[7];
-        s_cur[8] = acc[8];
-        s_cur[9] = -acc[9];
+        sh.det    = detr;
+        sh.cur[0] = acc[10];
+        sh.cur[1] = acc[11];
+        sh.cur[2] = acc[12];
+        sh.cur[3] = acc[13];
+        sh.cur[4] = acc[4];
+        sh.cur[5] = acc[5];
+        sh.cur[6] = acc[6];
+        sh.cur[7] = acc[7];
+        sh.cur[8] = acc[8];
+        sh.cur[9] = -acc[9];
         if constexpr (LEARNED)
         {
-          lsm.p = p;
+          sh.lsm.p = p;
           for (int d = 0; d < 3; d++)
-            lsm.g[d] = g[d];
+            sh.lsm.g[d] = g[d];
         }
         else
         {
@@ -436,14 +443,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
           T dr[3];
           unr_drift_t(tau, g, dr);
           for (int d = 0; d < 3; d++)
-            dr[d] += s_disp[d];
+            dr[d] += sh.disp[d];
           log_gb = -(T(0.5) / tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
         }
         int a = 0;
         if (p >= Eps<T>::v)
         {
           const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
-          a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - s_loggf) ? 1 : 0;
+          a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - sh.loggf) ? 1 : 0;
         }
         if (a)
         {
@@ -456,39 +463,39 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         }
         else
           n_rej++;
-        s_acc = a;
+        sh.acc = a;
         }
       }
       __syncthreads();
       if constexpr (LEARNED)
       {
         // the network at the proposed position: the reverse density q(r | R')
-        const T pn[3] = {T(s_pos[0]), T(s_pos[1]), T(s_pos[2])};
-        features_cta(s, Rs, iat, pn, lsm.g, lsm.x);
+        const T pn[3] = {T(sh.pos[0]), T(sh.pos[1]), T(sh.pos[2])};
+        features_cta(s, Rs, iat, pn, sh.lsm.g, sh.lsm.x);
         __syncthreads();
-        mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, lsm.x, lsm.h, lsm.red, lsm.out);
+        mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, sh.lsm.x, sh.lsm.h, sh.lsm.red, sh.lsm.out);
         if (threadIdx.x == 0)
         {
           const T st = sqrt(tau);
           T drift[3];
-          unr_drift_t(tau, lsm.g, drift);
+          unr_drift_t(tau, sh.lsm.g, drift);
           T sum_s = 0, z2 = 0;
           for (int d = 0; d < 3; d++)
           {
-            const T mu = T(clampf(lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
-            const T sd = T(clampf(lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+            const T mu = T(clampf(sh.lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
+            const T sd = T(clampf(sh.lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
             sum_s += sd;
-            const T z = (-s_disp[d] - drift[d] - st * mu) / (st * exp(sd));
+            const T z = (-sh.disp[d] - drift[d] - st * mu) / (st * exp(sd));
             z2 += z * z;
           }
           const T log_gb = -sum_s - T(0.5) * z2;
-          const T p      = lsm.p;
-          const T detr   = s_det;
+          const T p      = sh.lsm.p;
+          const T detr   = sh.det;
           int a          = 0;
           if (p >= Eps<T>::v)
           {
             const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
-            a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - s_loggf) ? 1 : 0;
+            a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - sh.loggf) ? 1 : 0;
           }
           if (a)
           {
@@ -501,12 +508,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
           }
           else
             n_rej++;
-          s_acc = a;
+          sh.acc = a;
         }
         __syncthreads();
       }
       // ------------------------------------------------ accept / reject
-      const bool accd = s_acc != 0;
+      const bool accd = sh.acc != 0;
       if (K > 1)
       {
         T* U       = s.U + slot * K * lda;
@@ -516,7 +523,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
           V[(size_t)dc * lda + j] = arow[j];
         if (accd)
         {
-          const T sigma = T(1) / s_det;
+          const T sigma = T(1) / sh.det;
           rows_dot<T, NT>(V, lda, dc, phi, n, pv, T(-1));
           __syncthreads();
           for (int i = threadIdx.x; i < dc; i += NT)
@@ -574,7 +581,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
             tmp[j] = (j == row) ? a - T(1) : a;
         }
         __syncthreads();
-        const T c = T(-1) / s_det;
+        const T c = T(-1) / sh.det;
         for (int e = threadIdx.x; e < n * n; e += NT)
         {
           const int j = e / n, i = e % n;
@@ -641,14 +648,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
         {
           if (s.has_j2)
             for (int q = 0; q < 5; q++)
-              J2s[q * s.ne_pad + iat] = s_cur[5 + q];
+              J2s[q * s.ne_pad + iat] = sh.cur[5 + q];
           if (s.has_j1)
             for (int q = 0; q < 5; q++)
-              s.J1[((size_t)w * 5 + q) * s.ne_pad + iat] = s_cur[q];
+              s.J1[((size_t)w * 5 + q) * s.ne_pad + iat] = sh.cur[q];
           for (int d = 0; d < 3; d++)
           {
-            s.R[((size_t)w * 3 + d) * s.ne_pad + iat] = s_pos[d];
-            Rs[d * s.ne_pad + iat]                    = static_cast<T>(s_pos[d]);
+            s.R[((size_t)w * 3 + d) * s.ne_pad + iat] = sh.pos[d];
+            Rs[d * s.ne_pad + iat]                    = static_cast<T>(sh.pos[d]);
           }
         }
       }
@@ -676,11 +683,109 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
       s.J2[(size_t)w * 5 * s.ne_pad + e] = J2s[e];
     __syncthreads();
   }
+}
+
+template<typename T, int NT, int MINB, bool LEARNED>
+__global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ SweepShared<T, LEARNED> sh;
+  unsigned long long n_acc = 0, n_rej = 0;
+  for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
+    sweep_walker<T, NT, LEARNED>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
   if (threadIdx.x == 0)
   {
     atomicAdd(s.counters + 0, n_acc);
     atomicAdd(s.counters + 1, n_rej);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Uneven crowds: one persistent launch covers one stage (the st-th segment of every
+// crowd that has one).  Work items are (crowd, walker) pairs, ordered with the most
+// expensive crowd first and handed out dynamically through a global counter, so CTAs
+// that finish cheap walkers pick up the next item; each CTA loads a crowd's state
+// descriptor into shared memory when it switches crowds.
+// ---------------------------------------------------------------------------
+template<typename T, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep_multi_kernel(const DevState<T>* __restrict__ table, MultiStage st,
+                                                               int* __restrict__ work)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ SweepShared<T, false> sh;
+  __shared__ __align__(16) DevState<T> ds;
+  __shared__ int s_item;
+  unsigned long long n_acc = 0, n_rej = 0;
+  int cur = -1;
+  const int total = st.begin[st.nactive];
+  for (;;)
+  {
+    if (threadIdx.x == 0)
+      s_item = atomicAdd(work, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total)
+      break;
+    int a = 0;
+    while (a + 1 < st.nactive && item >= st.begin[a + 1])
+      a++;
+    const int c = st.crowd[a];
+    if (c != cur)
+    {
+      if (cur >= 0 && threadIdx.x == 0)
+      {
+        atomicAdd(ds.counters + 0, n_acc);
+        atomicAdd(ds.counters + 1, n_rej);
+      }
+      n_acc = n_rej = 0;
+      __syncthreads();
+      const int* src = reinterpret_cast<const int*>(table + c);
+      int* dst       = reinterpret_cast<int*>(&ds);
+      for (int e = threadIdx.x; e < (int)(sizeof(DevState<T>) / sizeof(int)); e += NT)
+        dst[e] = src[e];
+      __syncthreads();
+      cur = c;
+    }
+    sweep_walker<T, NT, false>(ds, st.i0[a], st.i1[a], item - st.begin[a], smem_raw, sh, n_acc, n_rej);
+    __syncthreads();
+  }
+  if (cur >= 0 && threadIdx.x == 0)
+  {
+    atomicAdd(ds.counters + 0, n_acc);
+    atomicAdd(ds.counters + 1, n_rej);
+  }
+}
+
+template<typename T>
+cudaError_t launch_sweep_multi(const DevState<T>* table, const MultiStage& st, size_t smem, int grid, int* work,
+                               cudaStream_t stm)
+{
+  if (st.nactive <= 0)
+    return cudaSuccess;
+  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
+  sweep_multi_kernel<T, NT, MINB><<<grid, NT, smem, stm>>>(table, st, work);
+  return cudaGetLastError();
+}
+
+template<typename T>
+cudaError_t sweep_multi_grid(size_t smem, int* grid)
+{
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(sweep_multi_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_multi_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
+                                                      SweepCfg<T>::NT, smem);
+  if (e != cudaSuccess)
+    return e;
+  if (per_sm < 1)
+    return cudaErrorInvalidConfiguration;
+  *grid = per_sm * sms;
+  return cudaSuccess;
 }
 
 template<typename T>
@@ -750,5 +855,12 @@ template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, in
 template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t, bool);
 template cudaError_t sweep_grid<float>(const DevState<float>&, int*, bool);
 template cudaError_t sweep_grid<double>(const DevState<double>&, int*, bool);
+
+template cudaError_t launch_sweep_multi<float>(const DevState<float>*, const MultiStage&, size_t, int, int*,
+                                               cudaStream_t);
+template cudaError_t launch_sweep_multi<double>(const DevState<double>*, const MultiStage&, size_t, int, int*,
+                                                cudaStream_t);
+template cudaError_t sweep_multi_grid<float>(size_t, int*);
+template cudaError_t sweep_multi_grid<double>(size_t, int*);
 
 } // namespace qmcg

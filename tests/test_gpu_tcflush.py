@@ -35,8 +35,9 @@ def call_ex(method, arrays, dc):
 @pytest.mark.parametrize("method,tol", [(3, 1e-5), (1, 5e-3)])
 @pytest.mark.parametrize("nw,n,lda,k,dc", [(3, 20, 32, 4, 4), (2, 64, 64, 16, 9), (4, 192, 192, 32, 32),
                                            (2, 200, 208, 32, 17),
-                                           # N-tiled kernel: k > 32 or n + 64 > 512 tensor-memory columns
+                                           # N-tiled kernel: k > 32 or n_pad > 256 (one MMA's largest N)
                                            (3, 192, 192, 64, 37), (2, 300, 304, 48, 41), (2, 520, 528, 16, 9),
+                                           (2, 384, 384, 32, 32),
                                            (2, 768, 768, 64, 64)])
 def test_tensor_core_flush(method, tol, nw, n, lda, k, dc):
     arrays = flush_case(nw, n, lda, k, dc, seed=7 * n + dc)
