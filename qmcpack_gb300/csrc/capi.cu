@@ -1696,6 +1696,8 @@ struct Group final : qmcg_group_s
       const double ca = (double)cs[a]->sys->ne * cs[a]->sys->lda, cb = (double)cs[b]->sys->ne * cs[b]->sys->lda;
       return ca > cb;
     });
+    // a crowd with m segments places segment j in stage floor(j * S / m), S the largest m,
+    // so every crowd progresses through its sweep at the same pace
     size_t nst = 0;
     for (auto* c : cs)
       nst = std::max(nst, c->segments().size());
@@ -1707,15 +1709,21 @@ struct Group final : qmcg_group_s
       for (int c : order)
       {
         const auto seg = cs[c]->segments();
-        if (j >= seg.size())
+        const size_t m = seg.size();
+        int hit        = -1;
+        for (size_t q = 0; q < m; q++)
+          if ((q * nst) / m == j)
+            hit = (int)q;
+        if (hit < 0)
           continue;
         const int a = st.nactive++;
         st.crowd[a]     = c;
-        st.i0[a]        = seg[j].first;
-        st.i1[a]        = seg[j].second;
+        st.i0[a]        = seg[hit].first;
+        st.i1[a]        = seg[hit].second;
         st.begin[a + 1] = st.begin[a] + cs[c]->nw;
       }
-      stages.push_back(st);
+      if (st.nactive > 0)
+        stages.push_back(st);
     }
     CUDA_TRY(mem.alloc(&work, stages.size()));
     return QMCG_OK;
