@@ -283,6 +283,26 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T* scratch)
   __syncthreads();
 }
 
+// sum NV values over the block; results valid in warp 0 only (no trailing barrier:
+// the caller must synchronise before scratch is written again)
+template<typename T, int NV>
+__device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++)
+    v[q] = warp_sum(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++)
+      scratch[q * 32 + wid] = v[q];
+  __syncthreads();
+  if (wid == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++)
+      v[q] = warp_sum(lane < nwarp ? scratch[q * 32 + lane] : T(0));
+}
+
 // Umrigar drift scaling (DriftModifierUNR::getDrift, a = 1)
 __device__ __forceinline__ void unr_drift(double tau, const double g[3], double d[3])
 {

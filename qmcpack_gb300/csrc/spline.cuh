@@ -42,8 +42,11 @@ struct Vec<double>
 // its x-plane with 128-bit loads that are contiguous over orbitals, and writes
 // 7 partial sums (v, gx, gy, gz, hxx, hyy, hzz) to part[i][7][lda].
 // ---------------------------------------------------------------------------
+// Units [u_lo, u_hi) are handed to threads t, t + nt, ... (t = the caller's rank).
 template<typename T>
-__device__ __forceinline__ void spline_partials(const DevState<T>& s, const double pos[3], T* part)
+__device__ __forceinline__ void spline_partials(const DevState<T>& s, const double pos[3], T* part,
+                                                int t = threadIdx.x, int nt = blockDim.x, int u_lo = 0,
+                                                int u_hi = 1 << 30)
 {
   constexpr int W = Vec<T>::W;
   T ru[3];
@@ -68,7 +71,8 @@ __device__ __forceinline__ void spline_partials(const DevState<T>& s, const doub
   bspline_weights(tz, c, dc, d2c);
   const int ncol  = s.lda / W;
   const T* origin = s.coefs + ix * s.xs + iy * s.ys + iz * s.zs;
-  for (int unit = threadIdx.x; unit < 4 * ncol; unit += blockDim.x)
+  const int u_end = min(4 * ncol, u_hi);
+  for (int unit = u_lo + t; unit < u_end; unit += nt)
   {
     const int col = unit % ncol;
     const int i   = unit / ncol;

@@ -195,8 +195,10 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         gaussians<T>((uint32_t)w, (uint32_t)iat, sweep, k0, k1, sh.gauss);
       async_wait_all();
       __syncthreads();
-      // ------------------------------------------------ up-to-date inverse row
+      // ------------------------------------------------ up-to-date inverse row, fused with
+      // the gradient and self-ratio sums of the same elements
       const T* inv = arow;
+      T g[4]       = {0, 0, 0, 0};
       if (K > 1 && dc > 0)
       {
         const T* U = s.U + slot * K * lda;
@@ -212,6 +214,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           Bs[dc * K + i] = -a;
         }
         __syncthreads();
+        // the next electron's rows arrive while this one is evaluated
+        if (iat + 1 < i1)
+          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
         for (int j = threadIdx.x; j < n; j += NT)
         {
           T a[4] = {0, 0, 0, 0};
@@ -227,25 +232,30 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           }
           for (; c < dc; c++)
             a[0] += V[(size_t)c * lda + j] * tv[c];
-          invrow[j] = arow[j] + ((a[0] + a[1]) + (a[2] + a[3]));
-        }
-        __syncthreads();
-        inv = invrow;
-      }
-      // the next electron's rows arrive while this one is evaluated
-      if (iat + 1 < i1)
-        prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
-      // ------------------------------------------------ gradient, health check, proposal
-      {
-        T g[4] = {0, 0, 0, 0};
-        for (int j = threadIdx.x; j < n; j += NT)
-        {
-          const T x = inv[j];
+          const T x = arow[j] + ((a[0] + a[1]) + (a[2] + a[3]));
+          invrow[j] = x;
           g[0] += x * dg[j];
           g[1] += x * dg[lda + j];
           g[2] += x * dg[2 * lda + j];
           g[3] += x * pv0[j];
         }
+        inv = invrow;
+      }
+      else
+      {
+        if (iat + 1 < i1)
+          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
+        for (int j = threadIdx.x; j < n; j += NT)
+        {
+          const T x = arow[j];
+          g[0] += x * dg[j];
+          g[1] += x * dg[lda + j];
+          g[2] += x * dg[2 * lda + j];
+          g[3] += x * pv0[j];
+        }
+      }
+      // ------------------------------------------------ gradient, health check, proposal
+      {
         block_sum<T, 4>(g, red);
         if constexpr (LEARNED)
         {
@@ -332,54 +342,58 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
       // ------------------------------------------------ evaluation at the proposed position
       const double pos[3] = {sh.pos[0], sh.pos[1], sh.pos[2]};
-      spline_partials(s, pos, part);
       T acc[14];
 #pragma unroll
       for (int q = 0; q < 14; q++)
         acc[q] = T(0);
       const T x0 = static_cast<T>(pos[0]), y0 = static_cast<T>(pos[1]), z0 = static_cast<T>(pos[2]);
-      if (s.has_j2)
-        for (int j = threadIdx.x; j < s.ne; j += NT)
-        {
-          if (j == iat)
-            continue;
-          const T dx = min_image(Rs[j] - x0, L0, Li0);
-          const T dy = min_image(Rs[s.ne_pad + j] - y0, L1, Li1);
-          const T dz = min_image(Rs[2 * s.ne_pad + j] - z0, L2, Li2);
-          const T r  = sqrt(dx * dx + dy * dy + dz * dz);
-          if (r < s.j2_rcut)
+      // Jastrow rows against the positions in shared memory, threads t0, t0 + stride, ...
+      auto jastrow_rows = [&](int t0, int stride) {
+        if (s.has_j2)
+          for (int j = t0; j < s.ne; j += stride)
           {
-            const int same = (j < s.nup) == (iat < s.nup);
-            T du, d2u;
-            const T u = functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
-            du *= T(1) / r;
-            acc[5] += u;
-            acc[6] += du * dx;
-            acc[7] += du * dy;
-            acc[8] += du * dz;
-            acc[9] += d2u + T(2) * du;
+            if (j == iat)
+              continue;
+            const T dx = min_image(Rs[j] - x0, L0, Li0);
+            const T dy = min_image(Rs[s.ne_pad + j] - y0, L1, Li1);
+            const T dz = min_image(Rs[2 * s.ne_pad + j] - z0, L2, Li2);
+            const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r < s.j2_rcut)
+            {
+              const int same = (j < s.nup) == (iat < s.nup);
+              T du, d2u;
+              const T u = functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
+              du *= T(1) / r;
+              acc[5] += u;
+              acc[6] += du * dx;
+              acc[7] += du * dy;
+              acc[8] += du * dz;
+              acc[9] += d2u + T(2) * du;
+            }
           }
-        }
-      if (s.has_j1)
-        for (int j = threadIdx.x; j < s.nions; j += NT)
-        {
-          const T dx = min_image(s.ions[j] - x0, L0, Li0);
-          const T dy = min_image(s.ions[s.nions_pad + j] - y0, L1, Li1);
-          const T dz = min_image(s.ions[2 * s.nions_pad + j] - z0, L2, Li2);
-          const T r  = sqrt(dx * dx + dy * dy + dz * dz);
-          if (r < s.j1_rcut)
+        if (s.has_j1)
+          for (int j = t0; j < s.nions; j += stride)
           {
-            T du, d2u;
-            const T u =
-                functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
-            du *= T(1) / r;
-            acc[10] += u;
-            acc[11] += du * dx;
-            acc[12] += du * dy;
-            acc[13] += du * dz;
-            acc[4] += d2u + T(2) * du;
+            const T dx = min_image(s.ions[j] - x0, L0, Li0);
+            const T dy = min_image(s.ions[s.nions_pad + j] - y0, L1, Li1);
+            const T dz = min_image(s.ions[2 * s.nions_pad + j] - z0, L2, Li2);
+            const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r < s.j1_rcut)
+            {
+              T du, d2u;
+              const T u =
+                  functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
+              du *= T(1) / r;
+              acc[10] += u;
+              acc[11] += du * dx;
+              acc[12] += du * dy;
+              acc[13] += du * dz;
+              acc[4] += d2u + T(2) * du;
+            }
           }
-        }
+      };
+      spline_partials(s, pos, part);
+      jastrow_rows(threadIdx.x, NT);
       __syncthreads();
       for (int o = threadIdx.x; o < n; o += NT)
       {
@@ -394,7 +408,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         acc[2] += x * vgl[2];
         acc[3] += x * vgl[3];
       }
-      block_sum<T, 14>(acc, red);
+      block_sum_to0<T, 14>(acc, red);
       if (threadIdx.x == 0)
       {
         const T detr = acc[0];
