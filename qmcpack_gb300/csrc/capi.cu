@@ -568,8 +568,9 @@ struct Crowd final : qmcg_crowd_s
     ew.rho_ion = static_cast<const T*>(sys->ew_rho);
     ew.ion_q   = static_cast<const T*>(sys->ew_q);
     ew.alpha   = static_cast<T>(sys->ewh.alpha);
+    ew.rcut    = static_cast<T>(0.5 * std::min(sys->L[0], std::min(sys->L[1], sys->L[2])));
     ew.e_const = sys->ewh.e_const;
-    if (local_energy_smem(sys->ne, ew.nmax, sizeof(T)) > 200 * 1024)
+    if (local_energy_smem(sys->ne, ew.nmax, sizeof(T)) > 200 * 1024 || sys->ne > 46340)
       return fail(QMCG_ERR_ARG, "local energy: too many electrons for the shared-memory tables");
     d.gauss     = gauss_d;
     d.uniform   = unif_d;

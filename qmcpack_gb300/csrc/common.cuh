@@ -115,6 +115,7 @@ struct EwaldDev
   const T* rho_ion;   // [ng][2] ion structure factor sum_I Z_I exp(i G.R_I)
   const T* ion_q;     // [nions] ion charges
   T alpha;
+  T rcut;             // pairs beyond rcut (half the shortest cell side) contribute below the tolerance
   double e_const;     // ion-ion, self-energy and background terms
 };
 

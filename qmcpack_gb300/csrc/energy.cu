@@ -7,7 +7,7 @@
 //   Coulomb  V = Ewald energy of the electrons (charge -1) and the ions in the
 //            periodic cell (the total of CoulombPBCAA for e-e and i-i and CoulombPBCAB
 //            for e-i; the reference's standalone sum is EwaldRef.cpp:337-398):
-//              V = sum_{i<j} q_i q_j erfc(a r_ij)/r_ij                (minimum image)
+//              V = sum_{i<j} q_i q_j erfc(a r_ij)/r_ij   (minimum image, r_ij < L_min/2)
 //                + sum_{G in half space, |G| <= G_c} f(G) (|rho_e + rho_I|^2 - |rho_I|^2)
 //                + constant (ion-ion terms, self energy, background)
 //            with f(G) = 4 pi/V exp(-G^2/4a^2)/G^2 and rho_e(G) = -sum_i exp(i G.r_i).
@@ -111,21 +111,22 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
   // m = 1..nsep for every i (j = i + m mod ne), plus m = ne/2 for i < ne/2 when ne is even
   const T al          = ew.alpha;
   const int nsep      = (ne - 1) / 2;
-  const long long nfull = (long long)ne * nsep;
-  const long long npair = nfull + ((ne & 1) ? 0 : ne / 2);
-  for (long long p = tid; p < npair; p += LE_NT)
+  const int nfull = ne * nsep; // ne <= 46340 keeps the pair count in 32 bits
+  const int npair = nfull + ((ne & 1) ? 0 : ne / 2);
+  for (int p = tid; p < npair; p += LE_NT)
   {
     int i, j;
     if (p < nfull)
     {
-      i = (int)(p % ne);
-      j = i + 1 + (int)(p / ne);
+      const int m = p / ne;
+      i = p - m * ne;
+      j = i + 1 + m;
       if (j >= ne)
         j -= ne;
     }
     else
     {
-      i = (int)(p - nfull);
+      i = p - nfull;
       j = i + ne / 2;
     }
     T r2 = 0;
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
       r2 += dx * dx;
     }
     const T r = sqrt(r2);
-    if (r > T(0))
+    if (r > T(0) && r < ew.rcut)
       vr += static_cast<double>(t_erfc(al * r) / r);
   }
   // electron-ion pairs
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
       r2 += dx * dx;
     }
     const T r = sqrt(r2);
-    if (r > T(0))
+    if (r > T(0) && r < ew.rcut)
       vr -= static_cast<double>(ew.ion_q[I] * t_erfc(al * r) / r);
   }
 
