@@ -100,6 +100,7 @@ struct DevState
   int rng_mode;          // 0: stream from the host, 1: counter-based on the device
   double tau;
   int use_drift;
+  double* gj_scratch;  // [2 nw][3 N + 8] pivot broadcast of the cluster Gauss-Jordan repair
   // learned proposal (walker-resident path): SIMT weight image and FP32 master parameters
   const void* mlp_simt;
   const float* mlp_params;

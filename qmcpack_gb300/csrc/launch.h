@@ -162,6 +162,7 @@ cudaError_t launch_mlp_backward(const MlpTrain& t, int rows, cudaStream_t st);
 cudaError_t launch_mlp_adam(const MlpTrain& t, float lr, cudaStream_t st);
 
 // recompute path (recompute_kernels.cu)
+__host__ __device__ size_t gj_scratch_doubles(int n);
 template<typename T>
 cudaError_t launch_recompute(const DevState<T>& s, double* mscratch, int masked, cudaStream_t st);
 } // namespace qmcg

@@ -219,6 +219,187 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same FP64 Gauss-Jordan inverse spread over a cluster of GJ_CL CTAs per matrix
+// (one SM each), for the masked repair of a few walkers where one SM's FP64 rate is
+// the latency: CTA r owns a contiguous block of columns.  Per pivot step the owner of
+// column k finds the pivot and publishes (pivot row, pivot value, column k with rows k
+// and p exchanged) in a double-buffered global scratch; one cluster barrier
+// (release/acquire) later every CTA swaps, scales and eliminates its own columns.
+// ---------------------------------------------------------------------------
+constexpr int GJ_CL = 8;
+constexpr int GJ_NT = 256;
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+
+__host__ __device__ size_t gj_scratch_doubles(int n) { return 3 * (size_t)n + 8; }
+
+template<typename T>
+__global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double* Mt, int masked)
+{
+  const int slot = blockIdx.x / GJ_CL;
+  if (skip_walker(s, slot % s.nw, masked)) // uniform over the cluster
+    return;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const int n = s.norb, r = (int)cluster_rank();
+  const int cw = (n + GJ_CL - 1) / GJ_CL, c0 = r * cw, c1 = min(n, c0 + cw), ncw = max(0, c1 - c0);
+  double* prow = reinterpret_cast<double*>(gsm);  // cw
+  int* cmap    = reinterpret_cast<int*>(prow + cw); // n
+  __shared__ double bval[GJ_NT / 32];
+  __shared__ int bidx[GJ_NT / 32];
+  double* a   = Mt + (size_t)slot * n * n;
+  double* scr = s.gj_scratch + (size_t)slot * gj_scratch_doubles(n);
+  double* pdv = scr + 2 * (size_t)n;                  // [2][2] pivot row, pivot value
+  int* perm   = reinterpret_cast<int*>(scr + 2 * (size_t)n + 4);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  double logabs = 0.0;
+  int sgn = 1, bad = 0;
+  for (int k = 0; k < n; k++)
+  {
+    const int b     = k & 1;
+    double* pc      = scr + (size_t)b * n;
+    if (k / cw == r)
+    {
+      double bv = -1.0;
+      int bi    = n;
+      for (int i = k + tid; i < n; i += GJ_NT)
+      {
+        const double v = fabs(a[(size_t)i * n + k]);
+        if (v > bv || (v == bv && i < bi))
+        {
+          bv = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi    = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi))
+        {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0)
+      {
+        bval[wid] = bv;
+        bidx[wid] = bi;
+      }
+      __syncthreads();
+      double pb = bval[0];
+      int p     = bidx[0];
+      for (int w = 1; w < GJ_NT / 32; w++)
+        if (bval[w] > pb || (bval[w] == pb && bidx[w] < p))
+        {
+          pb = bval[w];
+          p  = bidx[w];
+        }
+      if (!(pb > 0.0))
+        p = k;
+      for (int i = tid; i < n; i += GJ_NT)
+      {
+        const int src = (i == p) ? k : i;
+        pc[i]         = (i == k) ? 0.0 : a[(size_t)src * n + k];
+      }
+      if (tid == 0)
+      {
+        pdv[2 * b]     = (double)p;
+        pdv[2 * b + 1] = pb > 0.0 ? a[(size_t)p * n + k] : 0.0;
+        perm[k]        = p;
+      }
+    }
+    cluster_sync_all();
+    const int p    = (int)__ldcg(pdv + 2 * b);
+    const double d = __ldcg(pdv + 2 * b + 1);
+    if (!(fabs(d) > 0.0))
+    {
+      bad = 1;
+      break;
+    }
+    logabs += log(fabs(d));
+    if (d < 0.0)
+      sgn = -sgn;
+    if (p != k)
+      sgn = -sgn;
+    if (p != k)
+      for (int j = c0 + tid; j < c1; j += GJ_NT)
+      {
+        const double t        = a[(size_t)k * n + j];
+        a[(size_t)k * n + j]  = a[(size_t)p * n + j];
+        a[(size_t)p * n + j]  = t;
+      }
+    __syncthreads();
+    for (int jj = tid; jj < ncw; jj += GJ_NT)
+    {
+      const int j = c0 + jj;
+      const double v = (j == k ? 1.0 : a[(size_t)k * n + j]) / d;
+      prow[jj]             = v;
+      a[(size_t)k * n + j] = v;
+    }
+    __syncthreads();
+    for (int i = wid; i < n; i += GJ_NT / 32)
+    {
+      if (i == k)
+        continue;
+      const double f = __ldcg(pc + i);
+      double* ai     = a + (size_t)i * n + c0;
+      for (int jj = lane; jj < ncw; jj += 32)
+      {
+        const double base = (c0 + jj == k) ? 0.0 : ai[jj];
+        ai[jj]            = base - f * prow[jj];
+      }
+    }
+    __syncthreads();
+  }
+  cluster_sync_all();
+  if (bad)
+  {
+    if (r == 0 && tid == 0)
+    {
+      atomicOr(s.status + (slot % s.nw), ST_SINGULAR);
+      s.log_abs[slot] = -INFINITY;
+      s.sign[slot]    = 0;
+    }
+    return;
+  }
+  // the row interchanges become column interchanges applied in reverse order:
+  // output column j holds working column cmap[j]
+  if (tid == 0)
+  {
+    for (int j = 0; j < n; j++)
+      cmap[j] = j;
+    for (int k = n - 1; k >= 0; k--)
+    {
+      const int p = __ldcg(perm + k);
+      const int t = cmap[k];
+      cmap[k]     = cmap[p];
+      cmap[p]     = t;
+    }
+  }
+  __syncthreads();
+  T* A = s.Ainv + (size_t)slot * n * s.lda;
+  for (int i = wid; i < n; i += GJ_NT / 32)
+    for (int jj = lane; jj < ncw; jj += 32)
+      A[(size_t)i * s.lda + c0 + jj] = static_cast<T>(__ldcg(a + (size_t)i * n + cmap[c0 + jj]));
+  if (r == 0 && tid == 0)
+  {
+    s.log_abs[slot] = logabs;
+    s.sign[slot]    = sgn;
+  }
+}
+
 // grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
 // Vat, Grad, Lap over the ions.
 template<typename T, int NT>
@@ -316,10 +497,31 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
-  constexpr int NTG = 512;
-  const size_t smg  = (size_t)s.norb * (2 * sizeof(double) + sizeof(int));
-  gj_inverse_kernel<T, NTG><<<2 * s.nw, NTG, smg, st>>>(s, Mt, masked);
-  e = cudaGetLastError();
+  if (masked && s.gj_scratch)
+  {
+    // the few flagged matrices: a cluster of GJ_CL SMs each
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = dim3(2 * s.nw * GJ_CL);
+    cfg.blockDim           = dim3(GJ_NT);
+    const int cw           = (s.norb + GJ_CL - 1) / GJ_CL;
+    cfg.dynamicSmemBytes   = (size_t)cw * sizeof(double) + (size_t)s.norb * sizeof(int);
+    cfg.stream             = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id               = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = GJ_CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs                = attr;
+    cfg.numAttrs             = 1;
+    e = cudaLaunchKernelEx(&cfg, gj_cluster_kernel<T>, s, Mt, masked);
+  }
+  else
+  {
+    constexpr int NTG = 512;
+    const size_t smg  = (size_t)s.norb * (2 * sizeof(double) + sizeof(int));
+    gj_inverse_kernel<T, NTG><<<2 * s.nw, NTG, smg, st>>>(s, Mt, masked);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess)
     return e;
   dim3 grid(s.nw, (s.ne + 127) / 128);
