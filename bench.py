@@ -331,6 +331,7 @@ def run_c3(args, rank: int, world: int):
     crowds = []
     for i, (s, ds, t) in enumerate(zip(systems, dss, tuned)):
         g = Crowd(ds, s.spec.walkers, t["delay"])
+        g.set_threads(t["threads_per_walker"])
         g.load_walkers(make_walkers(s, s.spec.walkers, seed=50 + i + 100 * rank))
         g.mw_evaluateLog()
         g.vmc_sweeps(max(args.equil // 2, 1), 0.3, seed + i, rng_mode=1, flush=args.flush)
@@ -395,7 +396,8 @@ def run_c3(args, rank: int, world: int):
         "config": {"workload": f"c3_mixed: {DESCRIPTIONS['c3_mixed']}",
                    "step": "one VMC sweep of every crowd (group graph: one persistent launch per stage + flushes)",
                    "crowds": [{"electrons": s.n_elec, "orbitals": s.norb, "walkers": s.spec.walkers,
-                               "delay_rank": t["delay"], "autotune_ms_per_sweep": t["table"]}
+                               "delay_rank": t["delay"], "threads_per_walker": t["threads_per_walker"],
+                               "autotune_ms_per_sweep": t["table"]}
                               for s, t in zip(systems, tuned)],
                    "group": info, "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": "whole group sweep (sweep_multi_kernel stages + flushes + repair)",

@@ -262,8 +262,15 @@ int qmcg_group_create(const qmcg_crowd* crowds, int num_crowds, qmcg_group* out)
 int qmcg_group_destroy(qmcg_group group);
 /* rng_mode must be 1; stats (may be NULL) [num_crowds]. */
 int qmcg_group_sweeps(qmcg_group group, const qmcg_sweep_params* params, int num_sweeps, qmcg_sweep_stats* stats);
-/* out[3]: stages per sweep, CTAs of the persistent launch, shared memory bytes per CTA. */
+/* out[4]: stages per sweep, CTAs of the persistent launch, shared memory bytes per CTA,
+ * threads per CTA (256 when any crowd runs more than 128 threads per walker alone). */
 int qmcg_group_info(qmcg_group group, int* out);
+
+/* Threads per walker (CTA size) of the walker-resident drift-diffusion kernel: 128,
+ * 256 or 512 (512 for FP32 only); 0 restores the default, which grows with the
+ * walker's shared-memory footprint so that an SM keeps enough warps when it holds only
+ * one or two walkers.  The learned proposal always runs 128 threads per walker. */
+int qmcg_crowd_set_threads(qmcg_crowd crowd, int threads);
 
 /* Waits for the crowd's stream, then reports and clears the walker status bits. */
 int qmcg_crowd_sync(qmcg_crowd crowd, qmcg_sweep_stats* stats);

@@ -22,7 +22,7 @@ EXPORTS = [
     "qmcg_profile_sweep", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
     "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
     "qmcg_proposal_backward", "qmcg_proposal_features", "qmcg_vmc_sweeps_learned",
-    "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info",
+    "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info", "qmcg_crowd_set_threads",
 ]
 PROPOSAL_NUM_PARAMS = 43408
 _fp = C.POINTER(C.c_float)
@@ -107,6 +107,7 @@ def load(path: str = LIB_PATH):
         "qmcg_group_destroy": [vp],
         "qmcg_group_sweeps": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats)],
         "qmcg_group_info": [vp, _ip],
+        "qmcg_crowd_set_threads": [vp, C.c_int],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

@@ -2,10 +2,11 @@
 
 For a system and a walker count, every candidate delay rank k (the delayed-update
 window, which sets how many electrons one resident launch moves and how often the
-batched flush runs) is timed over a few device-RNG sweeps of a fresh crowd, and the
-fastest is kept.  The walker-resident design fixes one walker per CTA of 128 threads
+batched flush runs) and CTA size is timed over a few device-RNG sweeps of a fresh crowd,
+and the fastest is kept.  The walker-resident design fixes one walker per CTA
 and the spline work unit (one coefficient column x one x-plane: 16 rows of orbitals),
-so those are reported, not searched.  Results are cached in a JSON file keyed by the
+so those are reported, not searched; the threads per walker (128, 256, 512) are searched
+with the delay rank.  Results are cached in a JSON file keyed by the
 system shape, the walker count, the precision and the GPU name.
 """
 from __future__ import annotations
@@ -39,7 +40,7 @@ def candidate_ranks(system: System):
 
 def tune(system: System, nw: int, dsys=None, flush: int = 3, sweeps: int = 3, candidates=None,
          use_cache: bool = True) -> dict:
-    """{'delay': k, 'threads_per_walker': 128, 'walkers_per_block': 1, 'ms_per_sweep': t, 'table': {k: t}}"""
+    """{'delay': k, 'threads_per_walker': t, 'walkers_per_block': 1, 'ms_per_sweep': ms, 'table': {...}}"""
     from .crowd import Crowd, DeviceSystem
     path = _cache_path()
     key = _key(system, nw, flush)
@@ -54,21 +55,25 @@ def tune(system: System, nw: int, dsys=None, flush: int = 3, sweeps: int = 3, ca
     dsys = dsys or DeviceSystem(system)
     R = make_walkers(system, nw, seed=5)
     table = {}
+    threads = (128, 256, 512) if system.spec.precision == 4 else (128, 256)
     for k in candidates or candidate_ranks(system):
         g = Crowd(dsys, nw, k)
         g.load_walkers(R)
         g.mw_evaluateLog()
-        g.vmc_sweeps(2, system.spec.tau, 1, rng_mode=1, flush=flush)  # warm-up, builds the graph
-        g.sync()
-        t0 = time.perf_counter()
-        g.vmc_sweeps_async(sweeps)
-        g.sync()
-        table[k] = (time.perf_counter() - t0) / sweeps * 1e3
+        for nt in threads:
+            g.set_threads(nt)
+            g.vmc_sweeps(2, system.spec.tau, 1, rng_mode=1, flush=flush)  # warm-up, builds the graph
+            g.sync()
+            t0 = time.perf_counter()
+            g.vmc_sweeps_async(sweeps)
+            g.sync()
+            table[(k, nt)] = (time.perf_counter() - t0) / sweeps * 1e3
         del g
     best = min(table, key=table.get)
-    res = {"delay": int(best), "threads_per_walker": 128, "walkers_per_block": 1,
+    res = {"delay": int(best[0]), "threads_per_walker": int(best[1]), "walkers_per_block": 1,
            "spline_unit": "one coefficient column x one x-plane (16 rows of orbitals)",
-           "ms_per_sweep": float(table[best]), "table": {str(k): float(v) for k, v in table.items()}}
+           "ms_per_sweep": float(table[best]),
+           "table": {f"k{k}/t{nt}": float(v) for (k, nt), v in table.items()}}
     if use_cache:
         cache[key] = res
         os.makedirs(os.path.dirname(path), exist_ok=True)

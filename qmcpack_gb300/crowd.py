@@ -193,6 +193,10 @@ class Crowd:
         self.last_repaired = st.repaired
         return st.accepted, st.rejected, el, ke
 
+    def set_threads(self, threads: int = 0):
+        """Threads per walker of the resident drift-diffusion kernel (128/256/512; 0 = default)."""
+        check(self.L.qmcg_crowd_set_threads(self.handle, threads))
+
     # ---- learned MH proposal
     def proposal_init(self, seed: int = 1, init_scale: float = 1.0):
         check(self.L.qmcg_proposal_init(self.handle, seed, init_scale))
@@ -302,6 +306,6 @@ class Group:
         return [(x.accepted, x.rejected, x.repaired) for x in st]
 
     def info(self):
-        out = np.zeros(3, np.int32)
+        out = np.zeros(4, np.int32)
         check(self.L.qmcg_group_info(self.handle, _p(out, _ip)))
-        return {"stages": int(out[0]), "ctas": int(out[1]), "smem_bytes": int(out[2])}
+        return {"stages": int(out[0]), "ctas": int(out[1]), "smem_bytes": int(out[2]), "threads": int(out[3])}

@@ -401,6 +401,7 @@ struct qmcg_crowd_s
   virtual int profile_sweep(int n, double* out)          = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
   virtual int local_energy(double* el, double* ke, double* vp) = 0;
+  virtual int set_threads(int nt)                        = 0;
   virtual int proposal_init(uint64_t seed, double scale)  = 0;
   virtual int proposal_params(float* get, const float* set) = 0;
   virtual int proposal_forward(int rows, const float* x, float* out, float* hidden) = 0;
@@ -429,6 +430,8 @@ struct Crowd final : qmcg_crowd_s
   int graph_rng_mode = -1, graph_use_drift = -1, graph_path = -1;
   int sweep_grid_size = 0;
   int sweep_grid_learned = 0;
+  int sweep_nt           = 128; // threads per walker of the drift-diffusion resident kernel
+  int graph_nt           = -1;
   int flush_kind      = 0;
   int graph_flush     = -1;
   int* tc_err         = nullptr;
@@ -559,7 +562,8 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&unif_d, nu));
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
-    CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size));
+    sweep_nt = sweep_default_threads<T>(d);
+    CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size, false, sweep_nt));
     CUDA_TRY(setup_local_energy<T>());
     CUDA_TRY(mem.alloc(&e_out, 3 * (size_t)nw));
     ew.ng      = sys->ew_ng;
@@ -930,15 +934,15 @@ struct Crowd final : qmcg_crowd_s
         for (int i0 = first; i0 < last; i0 += k)
         {
           const int i1 = std::min(i0 + k, last);
-          CUDA_TRY(launch_sweep_segment<T>(s, grid, i0, i1, stream, learned));
+          CUDA_TRY(launch_sweep_segment<T>(s, grid, i0, i1, stream, learned, sweep_nt));
           CUDA_TRY(launch_flush_choice(g, i1 - i0));
         }
       }
     }
     else
     {
-      CUDA_TRY(launch_sweep_segment<T>(s, grid, 0, sys->nup, stream, learned));
-      CUDA_TRY(launch_sweep_segment<T>(s, grid, sys->nup, sys->ne, stream, learned));
+      CUDA_TRY(launch_sweep_segment<T>(s, grid, 0, sys->nup, stream, learned, sweep_nt));
+      CUDA_TRY(launch_sweep_segment<T>(s, grid, sys->nup, sys->ne, stream, learned, sweep_nt));
     }
     CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
     bump_counter_kernel<<<1, 1, 0, stream>>>(s.sweep_counter);
@@ -949,7 +953,8 @@ struct Crowd final : qmcg_crowd_s
   int build_graph(const qmcg_sweep_params* p)
   {
     if (graph && graph_rng_mode == p->rng_mode && graph_use_drift == p->use_drift && graph_tau == p->tau &&
-        graph_seed == p->seed && graph_path == (resident(p) ? 0 : 1) && graph_flush == p->flush)
+        graph_seed == p->seed && graph_path == (resident(p) ? 0 : 1) && graph_flush == p->flush &&
+        graph_nt == sweep_nt)
       return QMCG_OK;
     if (graph)
     {
@@ -979,6 +984,7 @@ struct Crowd final : qmcg_crowd_s
     graph_seed      = p->seed;
     graph_path      = resident(p) ? 0 : 1;
     graph_flush     = p->flush;
+    graph_nt        = sweep_nt;
     return QMCG_OK;
   }
 
@@ -1034,6 +1040,19 @@ struct Crowd final : qmcg_crowd_s
       if (ke)
         std::copy_n(h.data() + ((size_t)it * 3 + 1) * nw, nw, ke + (size_t)it * nw);
     }
+    return QMCG_OK;
+  }
+
+  int set_threads(int nt) override
+  {
+    if (nt == 0)
+      nt = sweep_default_threads<T>(s);
+    if (!sweep_threads_ok(nt, sizeof(T)))
+      return fail(QMCG_ERR_ARG, "threads per walker must be 128, 256 or 512 (FP32 only)");
+    int grid = 0;
+    CUDA_TRY(sweep_grid<T>(s, &grid, false, nt));
+    sweep_nt        = nt;
+    sweep_grid_size = grid;
     return QMCG_OK;
   }
 
@@ -1520,7 +1539,8 @@ struct Crowd final : qmcg_crowd_s
           for (int i0 = first; i0 < last; i0 += k)
           {
             const int i1 = std::min(i0 + k, last);
-            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream); });
+            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream, false,
+                                                                  sweep_nt); });
             if (rc)
               return rc;
             rc = timed(1, [&] { return launch_flush_choice(g, i1 - i0); });
@@ -1539,7 +1559,8 @@ struct Crowd final : qmcg_crowd_s
         for (int g = 0; g < 2; g++)
         {
           const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
-          int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, first, last, stream); });
+          int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, first, last, stream, false,
+                                                                sweep_nt); });
           if (rc)
             return rc;
           if (it == 0)
@@ -1667,6 +1688,7 @@ struct Group final : qmcg_group_s
   std::vector<MultiStage> stages;
   size_t smem = 0;
   int grid    = 0;
+  int nt      = 128; // threads per walker of the group launch
   cudaGraphExec_t graph = nullptr;
   double g_tau = 0;
   uint64_t g_seed = 0;
@@ -1688,7 +1710,12 @@ struct Group final : qmcg_group_s
       smem = std::max(smem, sweep_smem_bytes<T>(c->s));
     if (smem > 220 * 1024)
       return fail(QMCG_ERR_ARG, "group: a crowd's walker state does not fit in shared memory");
-    CUDA_TRY(sweep_multi_grid<T>(smem, &grid));
+    // one CTA size for the launch: 256 threads per walker when any crowd runs more than 128 alone
+    nt = 128;
+    for (auto* c : cs)
+      if (c->sweep_nt > 128)
+        nt = 256;
+    CUDA_TRY(sweep_multi_grid<T>(smem, &grid, nt));
     CUDA_TRY(mem.alloc(&table, cs.size()));
     // stages: the j-th segment of every crowd; crowds ordered by cost per walker (largest first)
     std::vector<int> order(cs.size());
@@ -1783,7 +1810,7 @@ struct Group final : qmcg_group_s
     for (size_t j = 0; j < stages.size(); j++)
     {
       const MultiStage& st = stages[j];
-      CUDA_TRY(launch_sweep_multi<T>(table, st, smem, grid, work + j, stream));
+      CUDA_TRY(launch_sweep_multi<T>(table, st, smem, grid, work + j, stream, nt));
       for (int a = 0; a < st.nactive; a++)
       {
         Crowd<T>* x = cs[st.crowd[a]];
@@ -1839,12 +1866,14 @@ struct Group final : qmcg_group_s
     return QMCG_OK;
   }
 
-  // out: [0] stages per sweep, [1] CTAs of the persistent launch, [2] shared memory bytes per CTA
+  // out: [0] stages per sweep, [1] CTAs of the persistent launch, [2] shared memory bytes per CTA,
+  // [3] threads per CTA
   int info(int* out) override
   {
     out[0] = (int)stages.size();
     out[1] = grid;
     out[2] = (int)smem;
+    out[3] = nt;
     return QMCG_OK;
   }
 };
@@ -2016,6 +2045,7 @@ extern "C" int qmcg_vmc_sweeps_learned(qmcg_crowd c, const qmcg_sweep_params* p,
 {
   CROWD_CALL(c, sweeps_learned(p, n, train, lr, e_local, st, train_stats));
 }
+extern "C" int qmcg_crowd_set_threads(qmcg_crowd c, int threads) { CROWD_CALL(c, set_threads(threads)); }
 extern "C" int qmcg_mw_evaluate_local_energy(qmcg_crowd c, double* el, double* ke, double* vp)
 {
   CROWD_CALL(c, local_energy(el, ke, vp));

@@ -35,10 +35,13 @@ cudaError_t setup_sweep_kernel();
 template<typename T>
 size_t sweep_smem_bytes(const DevState<T>& s);
 template<typename T>
-cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned = false);
+cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned = false, int threads = 128);
+template<typename T>
+int sweep_default_threads(const DevState<T>& s);
+bool sweep_threads_ok(int threads, int tsize);
 template<typename T>
 cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st,
-                                 bool learned = false);
+                                 bool learned = false, int threads = 128);
 // uneven crowds: one launch per stage over (crowd, walker) work items
 constexpr int MULTI_MAX = 8;
 struct MultiStage
@@ -50,9 +53,9 @@ struct MultiStage
 };
 template<typename T>
 cudaError_t launch_sweep_multi(const DevState<T>* table, const MultiStage& st, size_t smem, int grid, int* work,
-                               cudaStream_t stm);
+                               cudaStream_t stm, int threads);
 template<typename T>
-cudaError_t sweep_multi_grid(size_t smem, int* grid);
+cudaError_t sweep_multi_grid(size_t smem, int* grid, int threads);
 // batched, shared-memory-staged flush of one spin for all walkers (flush_kernels.cu);
 // falls back to the two-kernel SIMT flush when the tiles do not fit
 template<typename T>

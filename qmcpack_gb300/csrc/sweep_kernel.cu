@@ -19,6 +19,7 @@
 // Gaussians, drift, Green's functions) runs in the move-loop precision, as the
 // reference's mixed-precision build does in RealType.
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "launch.h"
@@ -770,30 +771,36 @@ __global__ void __launch_bounds__(NT, MINB) sweep_multi_kernel(const DevState<T>
   }
 }
 
+// threads per walker of the group launch: 128 or 256
 template<typename T>
 cudaError_t launch_sweep_multi(const DevState<T>* table, const MultiStage& st, size_t smem, int grid, int* work,
-                               cudaStream_t stm)
+                               cudaStream_t stm, int nt)
 {
   if (st.nactive <= 0)
     return cudaSuccess;
-  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-  sweep_multi_kernel<T, NT, MINB><<<grid, NT, smem, stm>>>(table, st, work);
+  if (nt == 256)
+    sweep_multi_kernel<T, 256, sizeof(T) == 4 ? 2 : 1><<<grid, 256, smem, stm>>>(table, st, work);
+  else
+    sweep_multi_kernel<T, 128, sizeof(T) == 4 ? 4 : 2><<<grid, 128, smem, stm>>>(table, st, work);
   return cudaGetLastError();
 }
 
 template<typename T>
-cudaError_t sweep_multi_grid(size_t smem, int* grid)
+cudaError_t sweep_multi_grid(size_t smem, int* grid, int nt)
 {
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess)
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  auto occ = [&](auto kern, int threads) {
+    cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    if (r == cudaSuccess)
+      r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    return r;
+  };
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(sweep_multi_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_multi_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB>,
-                                                      SweepCfg<T>::NT, smem);
+    e = nt == 256 ? occ(sweep_multi_kernel<T, 256, sizeof(T) == 4 ? 2 : 1>, 256)
+                  : occ(sweep_multi_kernel<T, 128, sizeof(T) == 4 ? 4 : 2>, 128);
   if (e != cudaSuccess)
     return e;
   if (per_sm < 1)
@@ -802,15 +809,42 @@ cudaError_t sweep_multi_grid(size_t smem, int* grid)
   return cudaSuccess;
 }
 
+// threads per walker of the drift-diffusion kernel: 128, 256 or 512 (FP64: up to 256);
+// the registers per thread stay at 128 (255 for FP64) whatever the CTA size
+template<typename T, int NT>
+struct SweepMinb
+{
+  static constexpr int v = sizeof(T) == 4 ? (NT == 128 ? 4 : NT == 256 ? 2 : 1) : (NT == 128 ? 2 : 1);
+};
+
+bool sweep_threads_ok(int nt, int tsize) { return nt == 128 || nt == 256 || (nt == 512 && tsize == 4); }
+
+template<typename T, typename F>
+static cudaError_t with_threads(int nt, F&& f)
+{
+  if (nt == 128)
+    return f(std::integral_constant<int, 128>{});
+  if (nt == 256)
+    return f(std::integral_constant<int, 256>{});
+  if constexpr (sizeof(T) == 4)
+    if (nt == 512)
+      return f(std::integral_constant<int, 512>{});
+  return cudaErrorInvalidValue;
+}
+
 template<typename T>
 cudaError_t setup_sweep_kernel()
 {
-  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, false>,
+  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  if (e != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  for (int nt : {128, 256, 512})
+    if (e == cudaSuccess && sweep_threads_ok(nt, sizeof(T)))
+      e = with_threads<T>(nt, [](auto c) {
+        constexpr int NT = decltype(c)::value;
+        return cudaFuncSetAttribute(sweep_kernel<T, NT, SweepMinb<T, NT>::v, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      });
+  return e;
 }
 
 template<typename T>
@@ -820,26 +854,31 @@ size_t sweep_smem_bytes(const DevState<T>& s)
 }
 
 // electrons [i0, i1) of every walker, inside one spin group; with delayed updates
-// i1 - i0 <= k and the host flushes after the launch
+// i1 - i0 <= k and the host flushes after the launch.  The learned proposal needs 128
+// threads (one per hidden neuron).
 template<typename T>
-cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st, bool learned)
+cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1, cudaStream_t st, bool learned,
+                                 int nt)
 {
   if (i0 < 0 || i1 > s.ne || i1 <= i0 || (i0 < s.nup) != (i1 - 1 < s.nup) || (s.k > 1 && i1 - i0 > s.k))
     return cudaErrorInvalidValue;
-  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
   if (learned)
   {
+    constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
     if (!s.mlp_simt || !s.mlp_params)
       return cudaErrorInvalidValue;
     sweep_kernel<T, NT, MINB, true><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+    return cudaGetLastError();
   }
-  else
-    sweep_kernel<T, NT, MINB, false><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
-  return cudaGetLastError();
+  return with_threads<T>(nt, [&](auto c) {
+    constexpr int NT = decltype(c)::value;
+    sweep_kernel<T, NT, SweepMinb<T, NT>::v, false><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+    return cudaGetLastError();
+  });
 }
 
 template<typename T>
-cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned)
+cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
 {
   int dev = 0, sms = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -848,11 +887,18 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned)
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess)
     return e;
-  constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-  e = learned ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, true>, NT,
-                                                              sweep_smem_bytes(s))
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, false>, NT,
-                                                              sweep_smem_bytes(s));
+  if (learned)
+  {
+    constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, true>, NT,
+                                                      sweep_smem_bytes(s));
+  }
+  else
+    e = with_threads<T>(nt, [&](auto c) {
+      constexpr int NT = decltype(c)::value;
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, SweepMinb<T, NT>::v, false>,
+                                                           NT, sweep_smem_bytes(s));
+    });
   if (e != cudaSuccess)
     return e;
   if (per_sm < 1)
@@ -861,20 +907,34 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned)
   return cudaSuccess;
 }
 
+// default threads per walker: enough warps per SM when shared memory allows few CTAs
+template<typename T>
+int sweep_default_threads(const DevState<T>& s)
+{
+  const size_t sm = sweep_smem_bytes(s);
+  if (sm > 114 * 1024)
+    return sizeof(T) == 4 ? 512 : 256;
+  if (sm > 76 * 1024)
+    return 256;
+  return 128;
+}
+
 template cudaError_t setup_sweep_kernel<float>();
 template cudaError_t setup_sweep_kernel<double>();
 template size_t sweep_smem_bytes<float>(const DevState<float>&);
 template size_t sweep_smem_bytes<double>(const DevState<double>&);
-template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t, bool);
-template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t, bool);
-template cudaError_t sweep_grid<float>(const DevState<float>&, int*, bool);
-template cudaError_t sweep_grid<double>(const DevState<double>&, int*, bool);
+template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t, bool, int);
+template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t, bool, int);
+template cudaError_t sweep_grid<float>(const DevState<float>&, int*, bool, int);
+template cudaError_t sweep_grid<double>(const DevState<double>&, int*, bool, int);
+template int sweep_default_threads<float>(const DevState<float>&);
+template int sweep_default_threads<double>(const DevState<double>&);
 
 template cudaError_t launch_sweep_multi<float>(const DevState<float>*, const MultiStage&, size_t, int, int*,
-                                               cudaStream_t);
+                                               cudaStream_t, int);
 template cudaError_t launch_sweep_multi<double>(const DevState<double>*, const MultiStage&, size_t, int, int*,
-                                                cudaStream_t);
-template cudaError_t sweep_multi_grid<float>(size_t, int*);
-template cudaError_t sweep_multi_grid<double>(size_t, int*);
+                                                cudaStream_t, int);
+template cudaError_t sweep_multi_grid<float>(size_t, int*, int);
+template cudaError_t sweep_multi_grid<double>(size_t, int*, int);
 
 } // namespace qmcg
