@@ -1,0 +1,22 @@
+#!/bin/sh
+# Builds oracle/_ref/libref.so: the reference's header-only tricubic spline evaluator
+# compiled in place from REFERENCE_ROOT (default /root/reference), with a minimal
+# config.h shim.  Test infrastructure only; skipped when the reference is absent.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-/root/reference}
+[ -d "$REF/src/spline2" ] || { echo "reference sources not found at $REF; skipping oracle/_ref"; exit 0; }
+mkdir -p "$HERE/_ref"
+${CXX:-g++} -O2 -std=c++17 -fPIC -shared -Drestrict=__restrict__ \
+  -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/src/einspline" -I "$REF/src/Platforms" \
+  "$HERE/ref_spline.cpp" -o "$HERE/_ref/libref.so"
+# the reference's CPU delayed-update engine, its BLAS calls forwarded to scipy's OpenBLAS
+BLASDIR=$(${PYTHON:-python3} -c "import scipy, os; print(os.path.realpath(os.path.join(os.path.dirname(scipy.__file__), '..', 'scipy.libs')))" 2>/dev/null || true)
+BLAS=$(ls "$BLASDIR"/libscipy_openblas*.so 2>/dev/null | head -1)
+if [ -n "$BLAS" ]; then
+  ${CXX:-g++} -O2 -std=c++17 -fPIC -shared -fopenmp -Drestrict=__restrict__ \
+    -I "$HERE/ref_shim" -I "$REF/src" -I "$REF/src/Platforms" -I "$REF/src/Containers" -I "$REF/src/einspline" \
+    -I "$REF/src/Utilities" -I "$REF/src/Concurrency" \
+    "$HERE/ref_delayed.cpp" -o "$HERE/_ref/libref_delayed.so" "$BLAS" -Wl,-rpath,"$BLASDIR" -Wl,--no-undefined
+fi
+echo "built $HERE/_ref"
