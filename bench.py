@@ -179,13 +179,15 @@ def _fp64_twin(system):
     return dataclasses.replace(system, spec=spec64, coefs=system.coefs.astype(np.float64))
 
 
-def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4):
+def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4, R=None):
     """Per-move ratio error of the FP32 move loop against FP64 on identical positions and
-    coefficients: relative |ratio32 - ratio64| / |ratio64| over nelec electrons x nw walkers."""
+    coefficients: relative |ratio32 - ratio64| / |ratio64| over nelec electrons x nw walkers,
+    both crowds freshly recomputed from the positions R (uniform random if None)."""
     from qmcpack_gb300.crowd import Crowd, DeviceSystem
     sys64 = _fp64_twin(system)
     ds64 = DeviceSystem(sys64)
-    R = make_walkers(system, nw, seed=77)
+    label = "uniform random" if R is None else "equilibrated configurations"
+    R = make_walkers(system, nw, seed=77) if R is None else R
     g32, g64 = Crowd(dsys32, nw, k), Crowd(ds64, nw, k)
     errs = []
     for g in (g32, g64):
@@ -205,7 +207,8 @@ def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4):
     e = np.concatenate(errs)
     del g32, g64, ds64
     return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(e.max()),
-            "moves": int(e.size), "against": "FP64 move loop, same positions and coefficients"}
+            "moves": int(e.size), "against": "FP64 move loop, same positions and coefficients",
+            "walkers": label}
 
 
 def effective_samples(args, system, dsys32, seed: int):
@@ -535,7 +538,9 @@ def run_ours(args, rank: int, world: int):
     eff = None
     rerr = None
     if world == 1 and not args.no_effective and args.workload == "c1_384e":
-        rerr = ratio_error(system, dsys, 64, k)
+        Req = crowd.positions()[:64]
+        rerr = {"uniform_start": ratio_error(system, dsys, 64, k),
+                "equilibrated": ratio_error(system, dsys, 64, k, R=Req)}
         eff = effective_samples(args, system, dsys, seed + 11)
     line = {
         "metric": "walker-moves/s", "value": value, "unit": "walker-moves/s", "n_gpus": world,
