@@ -400,6 +400,201 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double
   }
 }
 
+// Variant with the CTA's column block resident in shared memory (when it fits): the
+// pivot search, row swap, scaling and elimination touch only shared memory, and the
+// other CTAs read the owner's pivot data from its shared memory over the cluster
+// (distributed shared memory).  Global memory is touched once to load the block and
+// once to write the result.
+__device__ __forceinline__ unsigned dsm_map(const void* p, unsigned rank)
+{
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"((unsigned)__cvta_generic_to_shared(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ double dsm_ld(unsigned addr)
+{
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ int dsm_ldi(unsigned addr)
+{
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];\n" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+__host__ __device__ inline size_t gj_smem_bytes(int n)
+{
+  const int cw = (n + GJ_CL - 1) / GJ_CL;
+  return sizeof(double) * ((size_t)n * (cw + 1) + 2 * (size_t)n + 4) + sizeof(int) * 2 * (size_t)n;
+}
+
+template<typename T>
+__global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, double* Mt, int masked)
+{
+  const int slot = blockIdx.x / GJ_CL;
+  if (skip_walker(s, slot % s.nw, masked)) // uniform over the cluster
+    return;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const int n = s.norb, r = (int)cluster_rank();
+  const int cw = (n + GJ_CL - 1) / GJ_CL, ld = cw + 1;
+  const int c0 = r * cw, c1 = min(n, c0 + cw), ncw = max(0, c1 - c0);
+  double* blk = reinterpret_cast<double*>(gsm);        // [n][ld] own columns
+  double* pcs = blk + (size_t)n * ld;                  // [2][n] published pivot column
+  double* pds = pcs + 2 * (size_t)n;                   // [2][2] published pivot row, value
+  int* perm   = reinterpret_cast<int*>(pds + 4);       // [n] pivot rows of the columns this CTA owns
+  int* cmap   = perm + n;                              // [n]
+  __shared__ double bval[GJ_NT / 32];
+  __shared__ int bidx[GJ_NT / 32];
+  double* a = Mt + (size_t)slot * n * n;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = wid; i < n; i += GJ_NT / 32)
+    for (int jj = lane; jj < ncw; jj += 32)
+      blk[(size_t)i * ld + jj] = a[(size_t)i * n + c0 + jj];
+  __syncthreads();
+  double logabs = 0.0;
+  int sgn = 1, bad = 0;
+  for (int k = 0; k < n; k++)
+  {
+    const int b     = k & 1;
+    const int owner = k / cw;
+    if (owner == r)
+    {
+      const int kk = k - c0;
+      double bv    = -1.0;
+      int bi       = n;
+      for (int i = k + tid; i < n; i += GJ_NT)
+      {
+        const double v = fabs(blk[(size_t)i * ld + kk]);
+        if (v > bv || (v == bv && i < bi))
+        {
+          bv = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi    = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi))
+        {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0)
+      {
+        bval[wid] = bv;
+        bidx[wid] = bi;
+      }
+      __syncthreads();
+      double pb = bval[0];
+      int p     = bidx[0];
+      for (int w = 1; w < GJ_NT / 32; w++)
+        if (bval[w] > pb || (bval[w] == pb && bidx[w] < p))
+        {
+          pb = bval[w];
+          p  = bidx[w];
+        }
+      if (!(pb > 0.0))
+        p = k;
+      for (int i = tid; i < n; i += GJ_NT)
+      {
+        const int src        = (i == p) ? k : i;
+        pcs[(size_t)b * n + i] = (i == k) ? 0.0 : blk[(size_t)src * ld + kk];
+      }
+      if (tid == 0)
+      {
+        pds[2 * b]     = (double)p;
+        pds[2 * b + 1] = pb > 0.0 ? blk[(size_t)p * ld + kk] : 0.0;
+        perm[k]        = p;
+      }
+    }
+    cluster_sync_all();
+    const unsigned rpd = dsm_map(pds + 2 * b, (unsigned)owner);
+    const int p        = (int)dsm_ld(rpd);
+    const double d     = dsm_ld(rpd + 8);
+    if (!(fabs(d) > 0.0))
+    {
+      bad = 1;
+      break;
+    }
+    logabs += log(fabs(d));
+    if (d < 0.0)
+      sgn = -sgn;
+    if (p != k)
+      sgn = -sgn;
+    if (p != k)
+      for (int jj = tid; jj < ncw; jj += GJ_NT)
+      {
+        const double t            = blk[(size_t)k * ld + jj];
+        blk[(size_t)k * ld + jj]  = blk[(size_t)p * ld + jj];
+        blk[(size_t)p * ld + jj]  = t;
+      }
+    __syncthreads();
+    for (int jj = tid; jj < ncw; jj += GJ_NT)
+      blk[(size_t)k * ld + jj] = (c0 + jj == k ? 1.0 : blk[(size_t)k * ld + jj]) / d;
+    __syncthreads();
+    const unsigned rpc = dsm_map(pcs + (size_t)b * n, (unsigned)owner);
+    for (int i = wid; i < n; i += GJ_NT / 32)
+    {
+      if (i == k)
+        continue;
+      const double f = dsm_ld(rpc + 8u * (unsigned)i);
+      double* bi     = blk + (size_t)i * ld;
+      const double* bk = blk + (size_t)k * ld;
+      for (int jj = lane; jj < ncw; jj += 32)
+      {
+        const double base = (c0 + jj == k) ? 0.0 : bi[jj];
+        bi[jj]            = base - f * bk[jj];
+      }
+    }
+    __syncthreads();
+  }
+  // results back to global memory, then the column interchanges (column j holds working
+  // column cmap[j], possibly of another CTA)
+  for (int i = wid; i < n; i += GJ_NT / 32)
+    for (int jj = lane; jj < ncw; jj += 32)
+      a[(size_t)i * n + c0 + jj] = blk[(size_t)i * ld + jj];
+  cluster_sync_all();
+  if (bad)
+  {
+    if (r == 0 && tid == 0)
+    {
+      atomicOr(s.status + (slot % s.nw), ST_SINGULAR);
+      s.log_abs[slot] = -INFINITY;
+      s.sign[slot]    = 0;
+    }
+    cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
+    return;
+  }
+  if (tid == 0)
+  {
+    for (int j = 0; j < n; j++)
+      cmap[j] = j;
+    for (int k = n - 1; k >= 0; k--)
+    {
+      const int p = dsm_ldi(dsm_map(perm + k, (unsigned)(k / cw)));
+      const int t = cmap[k];
+      cmap[k]     = cmap[p];
+      cmap[p]     = t;
+    }
+  }
+  __syncthreads();
+  T* A = s.Ainv + (size_t)slot * n * s.lda;
+  for (int i = wid; i < n; i += GJ_NT / 32)
+    for (int jj = lane; jj < ncw; jj += 32)
+      A[(size_t)i * s.lda + c0 + jj] = static_cast<T>(__ldcg(a + (size_t)i * n + cmap[c0 + jj]));
+  if (r == 0 && tid == 0)
+  {
+    s.log_abs[slot] = logabs;
+    s.sign[slot]    = sgn;
+  }
+  cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
+}
+
 // grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
 // Vat, Grad, Lap over the ions.
 template<typename T, int NT>
@@ -513,7 +708,13 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
     attr[0].val.clusterDim.z = 1;
     cfg.attrs                = attr;
     cfg.numAttrs             = 1;
-    e = cudaLaunchKernelEx(&cfg, gj_cluster_kernel<T>, s, Mt, masked);
+    if (gj_smem_bytes(s.norb) <= 200 * 1024)
+    {
+      cfg.dynamicSmemBytes = gj_smem_bytes(s.norb);
+      e = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<T>, s, Mt, masked);
+    }
+    else
+      e = cudaLaunchKernelEx(&cfg, gj_cluster_kernel<T>, s, Mt, masked);
   }
   else
   {
@@ -536,7 +737,10 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
 template<typename T>
 cudaError_t setup_recompute_kernels()
 {
-  return cudaFuncSetAttribute(vgl_all_kernel<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(vgl_all_kernel<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(gj_cluster_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  return e;
 }
 template cudaError_t setup_recompute_kernels<float>();
 template cudaError_t setup_recompute_kernels<double>();
