@@ -379,12 +379,14 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 
 // ---------------------------------------------------------------------------
 // N-tiled variant for large determinants and delay ranks up to 64: the second
-// product runs over column tiles of TT_TN inverse columns, W = Binv V is formed
+// product runs over column tiles of TN inverse columns, W = Binv V is formed
 // per tile from global V, so neither N nor k is bounded by TMEM or by a full V in
-// shared memory.  TMEM: T1 in columns [0, 64), the product tile in [64, 64 + TT_TN).
+// shared memory.  TMEM: T1 in columns [0, KM), the product tile in [KM, KM + TN).
+// Two instances: delay ranks up to 64 with 128-column tiles (256 TMEM columns, one CTA
+// per SM by shared memory), and delay ranks up to 32 with 96-column tiles (128 TMEM
+// columns and 70 KB of shared memory: three CTAs per SM).
 // ---------------------------------------------------------------------------
 constexpr int TT_KC = 32;  // K chunk of the first product
-constexpr int TT_TN = 128; // inverse columns per tile of the second product
 constexpr int TT_KMAX = 64;
 
 struct TtPlan
@@ -395,7 +397,7 @@ struct TtPlan
   uint32_t binv, dl, bar, total;
 };
 
-__host__ __device__ inline TtPlan tt_plan(int k)
+__host__ __device__ inline TtPlan tt_plan(int k, int TN)
 {
   TtPlan p;
   p.k1    = ((k + 15) / 16) * 16;
@@ -408,8 +410,8 @@ __host__ __device__ inline TtPlan tt_plan(int k)
   uint32_t o2 = 0;
   p.a2_hi = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
-  p.w_hi  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
-  p.w_lo  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
+  p.w_hi  = o2; o2 = al(o2 + TN * p.k1 * 4);
+  p.w_lo  = o2; o2 = al(o2 + TN * p.k1 * 4);
   o = o > o2 ? o : o2;
   p.binv  = o; o = al(o + k * k * 4);
   p.dl    = o; o = al(o + k * 4);
@@ -418,13 +420,14 @@ __host__ __device__ inline TtPlan tt_plan(int k)
   return p;
 }
 
-template<int TERMS>
-__global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<float> f, int* err)
+template<int TERMS, int TN, int KM, int MINB>
+__global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<float> f, int* err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
-  const TtPlan P = tt_plan(f.k);
+  constexpr int TMC = (KM + TN <= 128) ? 128 : 256; // TMEM columns allocated
+  const TtPlan P = tt_plan(f.k, TN);
   const int n = f.n, k = f.k, dc = f.dc, lda = f.lda, k1 = P.k1;
   const int iw = blockIdx.x, r0 = blockIdx.y * TC_M;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -442,7 +445,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
     mbar_init(bar);
   }
   if (warp == 0)
-    tmem_alloc(smem_u32(&s_tmem), 256);
+    tmem_alloc(smem_u32(&s_tmem), TMC);
   for (int e = tid; e < dc * dc; e += TC_NT)
     Bs[e] = Bi[(size_t)(e / dc) * k + (e % dc)];
   for (int e = tid; e < dc; e += TC_NT)
@@ -451,7 +454,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
-  const uint32_t d1 = tmem, d2 = tmem + 64;
+  const uint32_t d1 = tmem, d2 = tmem + KM;
   uint32_t phase = 0;
   auto split_store = [&](float4 x, uint32_t hi_base, uint32_t lo_base, uint32_t off) {
     const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
@@ -546,15 +549,16 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
     }
   }
   // ---------------- column tiles: W_tile = Binv V[:, tile], P_tile = (T1 - E) W_tile^T, Ainv -= P
-  for (int t0 = 0; t0 < n && ok; t0 += TT_TN)
+  for (int t0 = 0; t0 < n && ok; t0 += TN)
   {
+    if (tid < TN)
     {
       // thread i owns column t0 + i of the tile
       const int i = tid;
       const int col = t0 + i;
-      float vcol[TT_KMAX];
+      float vcol[KM];
 #pragma unroll
-      for (int l = 0; l < TT_KMAX; l++)
+      for (int l = 0; l < KM; l++)
         vcol[l] = (l < dc && col < n) ? V[(size_t)l * lda + col] : 0.f;
       for (int c4 = 0; c4 < k1; c4 += 4)
       {
@@ -566,7 +570,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
           float a     = 0.f;
           if (c < dc)
 #pragma unroll
-            for (int l = 0; l < TT_KMAX; l++)
+            for (int l = 0; l < KM; l++)
               if (l < dc)
                 a += Bs[c * dc + l] * vcol[l];
           w[q] = a;
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
     if (tid == 0)
     {
       tc_fence_after();
-      const uint32_t id = idesc_tf32(TC_M, TT_TN);
+      const uint32_t id = idesc_tf32(TC_M, TN);
       const uint32_t ah = smem_u32(sm + P.a2_hi), al = smem_u32(sm + P.a2_lo);
       const uint32_t bh = smem_u32(sm + P.w_hi), bl = smem_u32(sm + P.w_lo);
       for (int ks = 0; ks < k1 / 8; ks++)
@@ -602,7 +606,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
     const int r  = warp * 32 + lane;
     const int gr = r0 + r;
     float* row   = A + (size_t)(gr < n ? gr : 0) * lda + t0;
-    for (int c0 = 0; c0 < TT_TN; c0 += 32)
+    for (int c0 = 0; c0 < TN; c0 += 32)
     {
       float p[32];
       tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
@@ -627,7 +631,7 @@ __global__ void __launch_bounds__(TC_NT, 1) flush_tc_tiled_kernel(FlushArgs<floa
   tc_fence_before();
   __syncthreads();
   if (warp == 0)
-    tmem_dealloc(tmem, 256);
+    tmem_dealloc(tmem, TMC);
 }
 
 // the compact kernel: whole product in TMEM, k <= 32, and the second product is one
@@ -640,9 +644,12 @@ static bool flush_tc_compact_ok(int n, int k)
 
 bool flush_tc_supported(int n, int k, int lda)
 {
-  // 16-byte aligned rows; delay rank up to 64 (the tiled kernel covers any N)
-  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k).total <= 200 * 1024;
+  // 16-byte aligned rows; delay rank up to 64 (the tiled kernels cover any N)
+  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k, 128).total <= 200 * 1024;
 }
+
+#define QMCG_TILED_BIG(TERMS) flush_tc_tiled_kernel<TERMS, 128, 64, 1>
+#define QMCG_TILED_SMALL(TERMS) flush_tc_tiled_kernel<TERMS, 96, 32, 3>
 
 cudaError_t setup_flush_tc()
 {
@@ -650,10 +657,24 @@ cudaError_t setup_flush_tc()
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(flush_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(flush_tc_tiled_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    e = cudaFuncSetAttribute(QMCG_TILED_BIG(1), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(flush_tc_tiled_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    e = cudaFuncSetAttribute(QMCG_TILED_BIG(3), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(QMCG_TILED_SMALL(1), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(QMCG_TILED_SMALL(3), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   return e;
+}
+
+// which kernel flushes a shape: 0 one-pass, 1 tiled (k <= 32, 96-column tiles), 2 tiled (k <= 64)
+int flush_tc_variant(int n, int k)
+{
+  if (flush_tc_compact_ok(n, k))
+    return 0;
+  if (k <= 32)
+    return 1;
+  return 2;
 }
 
 cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cudaStream_t st)
@@ -661,7 +682,8 @@ cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cuda
   if (f.dc <= 0 || f.nw <= 0)
     return cudaSuccess;
   dim3 grid(f.nw, (f.n + TC_M - 1) / TC_M);
-  if (flush_tc_compact_ok(f.n, f.k))
+  const int v = flush_tc_variant(f.n, f.k);
+  if (v == 0 && flush_tc_compact_ok(f.n, f.k))
   {
     const TcPlan p = tc_plan(f.n, f.k);
     if (terms == 1)
@@ -669,15 +691,23 @@ cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cuda
     else
       flush_tc_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
   }
+  else if (v == 1)
+  {
+    const TtPlan p = tt_plan(f.k, 96);
+    if (terms == 1)
+      QMCG_TILED_SMALL(1)<<<grid, TC_NT, p.total, st>>>(f, err);
+    else
+      QMCG_TILED_SMALL(3)<<<grid, TC_NT, p.total, st>>>(f, err);
+  }
   else
   {
     if (f.k > TT_KMAX)
       return cudaErrorInvalidValue;
-    const TtPlan p = tt_plan(f.k);
+    const TtPlan p = tt_plan(f.k, 128);
     if (terms == 1)
-      flush_tc_tiled_kernel<1><<<grid, TC_NT, p.total, st>>>(f, err);
+      QMCG_TILED_BIG(1)<<<grid, TC_NT, p.total, st>>>(f, err);
     else
-      flush_tc_tiled_kernel<3><<<grid, TC_NT, p.total, st>>>(f, err);
+      QMCG_TILED_BIG(3)<<<grid, TC_NT, p.total, st>>>(f, err);
   }
   return cudaGetLastError();
 }
