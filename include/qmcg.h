@@ -292,10 +292,12 @@ int qmcg_mw_update_inv_mat(int precision, int num_walkers, int n, int lda, int d
 
 /* qmcg_mw_update_inv_mat with a choice of method: 0 = SIMT, 1 = tcgen05 tensor cores
  * in TF32, 3 = tcgen05 tensor cores in 3xTF32 split precision.  Methods 1 and 3 need
- * precision 4, delay_rank <= 64 and n, lda multiples of 4; other cases return
- * QMCG_ERR_ARG.  Shapes whose second product is one MMA (delay_rank <= 32, n padded to
- * 16 <= 256) run in one pass; others run the second product over tiles of 128 inverse
- * columns.  A tensor-core wait that times out returns QMCG_ERR_CUDA. */
+ * precision 4, delay_rank <= 64, n and lda multiples of 4 and ainv, u, v on 16-byte
+ * boundaries; other cases return QMCG_ERR_ARG.  The update is evaluated as
+ * ((T1 - E) Binv) V with T1 = Ainv U^T.  Shapes whose last product is one MMA
+ * (delay_rank <= 32, n padded to 16 <= 256) run in one pass; others run the last
+ * product over tiles of inverse columns.  A tensor-core wait that times out returns
+ * QMCG_ERR_CUDA. */
 int qmcg_mw_update_inv_mat_ex(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                               void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                               int method, void* stream);

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <deque>
@@ -2134,6 +2135,8 @@ extern "C" int qmcg_mw_update_inv_mat_ex(int precision, int nw, int n, int lda, 
     return rc;
   if (precision != 4 || !flush_tc_supported(n, k, lda))
     return fail(QMCG_ERR_ARG, "tensor-core flush needs precision 4, delay_rank <= 64, n and lda multiples of 4");
+  if (((uintptr_t)ainv | (uintptr_t)u | (uintptr_t)v) & 15)
+    return fail(QMCG_ERR_ARG, "tensor-core flush needs ainv, u and v on 16-byte boundaries");
   if (nw == 0 || dc == 0)
     return QMCG_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -1,6 +1,7 @@
 // Delayed-update flush on the 5th-generation tensor cores (tcgen05, kind::tf32):
-//   T1 = Ainv[rows] U^T            (128 x k,   K = n)   -> TMEM columns [0, 32..64)
-//   P  = (T1 - E) W,  W = Binv V   (128 x n,   K = k)   -> TMEM columns [64, 64+n)
+//   T1 = Ainv[rows] U^T            (128 x k,   K = n)   -> TMEM columns [0, k1)
+//   X  = (T1 - E) Binv             (128 x k,   K = k)   -> TMEM columns [0, k1)
+//   P  = X V                       (128 x n,   K = k)   -> TMEM columns [64, 64+n) (one-pass)
 //   Ainv[rows] -= P
 // DelayedUpdateBatched::mw_updateInvMat (DelayedUpdateBatched.h:675-738) for one
 // walker and a block of 128 inverse rows per CTA.  Operands are staged in shared
@@ -27,7 +28,7 @@ namespace qmcg
 constexpr int TC_M     = 128; // rows per CTA (TMEM lanes)
 constexpr int TC_NT    = 128; // 4 warps: warp w owns TMEM lanes 32w..32w+31
 constexpr int TC_KC    = 64;  // K chunk of the first product
-// TMEM columns allocated: T1 in [0, 32), P in [64, 64 + n_pad); a power of two
+// TMEM columns allocated: T1 and X in [0, 32), P in [64, 64 + n_pad); a power of two
 __host__ __device__ constexpr int tc_cols(int npad) { return 64 + npad <= 256 ? 256 : 512; }
 // byte offset of element (r, k) of an R x KC tile in the K-major core-matrix layout
 __device__ __forceinline__ uint32_t cm_off(int r, int k, int kc)
@@ -69,10 +70,11 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
 struct TcPlan
 {
   int n, k1, kc;   // n = orbitals, k1 = delay rank padded to 32, kc = K chunk
-  uint32_t a_hi, a_lo, b_hi, b_lo; // first product: 128 x kc and k1 x kc tiles
-  uint32_t a2_hi, a2_lo, w_hi, w_lo; // second product: 128 x k1 and n_pad x k1 tiles
-  uint32_t v, binv, dl, bar, tslot, total;
-  int npad;        // n padded to 16 (N of the second product)
+  uint32_t a_hi, a_lo, b_hi, b_lo;   // first product: 128 x kc and k1 x kc tiles
+  uint32_t a2_hi, a2_lo, w_hi, w_lo; // later products: 128 x k1 (T1 - E, then X) and n_pad x k1 (V^T)
+  uint32_t v, bt_hi, bt_lo;          // V (k x n) as stored; Binv^T (k1 x k1) over it once V^T is formed
+  uint32_t dl, bar, tslot, total;
+  int npad;        // n padded to 16 (N of the last product)
 };
 
 __host__ __device__ inline TcPlan tc_plan(int n, int k)
@@ -88,15 +90,18 @@ __host__ __device__ inline TcPlan tc_plan(int n, int k)
   p.a_lo  = o; o = al(o + TC_M * p.kc * 4);
   p.b_hi  = o; o = al(o + p.k1 * p.kc * 4);
   p.b_lo  = o; o = al(o + p.k1 * p.kc * 4);
-  // the second product reuses the first product's region
+  // the later products reuse the first product's region
   uint32_t o2 = 0;
   p.a2_hi = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.w_hi  = o2; o2 = al(o2 + p.npad * p.k1 * 4);
   p.w_lo  = o2; o2 = al(o2 + p.npad * p.k1 * 4);
   o = o > o2 ? o : o2;
-  p.v     = o; o = al(o + k * n * 4);
-  p.binv  = o; o = al(o + k * k * 4);
+  p.v     = o;
+  p.bt_hi = o;
+  p.bt_lo = al(o + p.k1 * p.k1 * 4);
+  const uint32_t vend = al(o + k * n * 4), btend = al(p.bt_lo + p.k1 * p.k1 * 4);
+  o = vend > btend ? vend : btend;
   p.dl    = o; o = al(o + k * 4);
   p.bar   = o; o += 16;
   p.tslot = o; o += 16;
@@ -104,12 +109,57 @@ __host__ __device__ inline TcPlan tc_plan(int n, int k)
   return p;
 }
 
+// Binv^T into a (k1 x k1) K-major operand tile: element (l, c) = Binv[c][l], zero
+// outside dc x dc; consecutive threads take consecutive rows l
+template<int TERMS>
+__device__ __forceinline__ void stage_binv_t(unsigned char* sm, uint32_t hi, uint32_t lo, const float* Binv, int k,
+                                             int dc, int k1, int tid)
+{
+  for (int e = tid; e < k1 * (k1 / 4); e += TC_NT)
+  {
+    const int l = e % k1, c4 = (e / k1) * 4;
+    float x[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      x[q] = (c4 + q < dc && l < dc) ? Binv[(size_t)(c4 + q) * k + l] : 0.f;
+    const float4 h = make_float4(tf32_hi(x[0]), tf32_hi(x[1]), tf32_hi(x[2]), tf32_hi(x[3]));
+    const uint32_t off = cm_off(l, c4, k1);
+    *reinterpret_cast<float4*>(sm + hi + off) = h;
+    if (TERMS > 1)
+      *reinterpret_cast<float4*>(sm + lo + off) = make_float4(x[0] - h.x, x[1] - h.y, x[2] - h.z, x[3] - h.w);
+  }
+}
+
+// the three-term (or one-term) product D = A B^T over K = k1 from two K-major tiles
+// with row pitch k1, issued by one thread
+template<int TERMS>
+__device__ __forceinline__ void mma_k1(uint32_t d, unsigned char* sm, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                       uint32_t b_lo, int k1, uint32_t idesc)
+{
+  const uint32_t ah = smem_u32(sm + a_hi), al = smem_u32(sm + a_lo);
+  const uint32_t bh = smem_u32(sm + b_hi), bl = smem_u32(sm + b_lo);
+  for (int ks = 0; ks < k1 / 8; ks++)
+  {
+    const uint32_t adv = ks * 256; // two core matrices along K per k-step of 8
+    mma_tf32(d, smem_desc(ah + adv, k1), smem_desc(bh + adv, k1), idesc, ks ? 1 : 0);
+    if (TERMS > 1)
+    {
+      mma_tf32(d, smem_desc(ah + adv, k1), smem_desc(bl + adv, k1), idesc, 1);
+      mma_tf32(d, smem_desc(al + adv, k1), smem_desc(bh + adv, k1), idesc, 1);
+    }
+  }
+}
+
+// The update is evaluated as P = ((T1 - E) Binv) V: the k x k product runs on the
+// tensor cores once per row block (128 x k1 x k1) instead of forming W = Binv V
+// (k x k x n) on the CUDA cores in every row block; V enters the last product as
+// its transpose, staged from shared memory.
 template<int TERMS>
 __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, int* err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   const TcPlan P = tc_plan(f.n, f.k);
-  const int n = f.n, k = f.k, dc = f.dc, lda = f.lda;
+  const int n = f.n, k = f.k, dc = f.dc, lda = f.lda, k1 = P.k1;
   const int iw = blockIdx.x, r0 = blockIdx.y * TC_M;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float* A             = f.ainv + (size_t)iw * f.sA;
@@ -117,8 +167,7 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
   const float* V       = f.v + (size_t)iw * f.sU;
   const float* Binv    = f.binv + (size_t)iw * f.sB;
   const int* dlist     = f.delay_list + (size_t)iw * f.sD;
-  float* Vs            = reinterpret_cast<float*>(sm + P.v);
-  float* Bs            = reinterpret_cast<float*>(sm + P.binv);
+  const float* Vs      = reinterpret_cast<const float*>(sm + P.v);
   int* dls             = reinterpret_cast<int*>(sm + P.dl);
   const uint32_t bar   = smem_u32(sm + P.bar);
   uint32_t* tslot      = reinterpret_cast<uint32_t*>(sm + P.tslot);
@@ -127,37 +176,47 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
   if (tid == 0)
   {
     s_fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    mbar_init(bar);
   }
   const int cols = tc_cols(P.npad);
   if (warp == 0)
+    tmem_alloc(smem_u32(tslot), cols);
+  // V (dc x n) into shared memory with cp.async: it lands while the first product runs
   {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
-                 "r"(cols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    const int nv4 = n >> 2;
+    for (int e = tid; e < dc * nv4; e += TC_NT)
+    {
+      const int l = e / nv4, c4 = (e - l * nv4) * 4;
+      const uint32_t sa = smem_u32(sm + P.v + (uint32_t)(l * n + c4) * 4);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(V + (size_t)l * lda + c4) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
-  for (int e = tid; e < dc * n; e += TC_NT)
-    Vs[e] = V[(size_t)(e / n) * lda + (e % n)];
-  for (int e = tid; e < dc * dc; e += TC_NT)
-    Bs[e] = Binv[(size_t)(e / dc) * k + (e % dc)];
   for (int e = tid; e < dc; e += TC_NT)
     dls[e] = dlist[e];
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  tc_fence_before();
   __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t d1   = tmem;      // columns [0, k1)
-  const uint32_t d2   = tmem + 64; // columns [64, 64 + npad)
+  const uint32_t d1   = tmem;      // columns [0, k1): T1, then X
+  const uint32_t d2   = tmem + 64; // columns [64, 64 + npad): P
   uint32_t phase      = 0;
-  bool ok             = true;
+  // every thread waits on the MMA barrier; a timeout anywhere stops the whole CTA
+  auto wait_mma = [&]() {
+    if (!mbar_wait(bar, phase))
+      atomicExch(&s_fail, 1);
+    phase ^= 1;
+    tc_fence_after();
+    __syncthreads();
+    return s_fail == 0;
+  };
+  bool ok = true;
 
   // ---------------- T1 = Ainv[rows] U^T, K in chunks of kc.  The next chunk's
   // global loads are issued before waiting for the current chunk's MMAs.
   constexpr int AV = TC_M * (TC_KC / 4) / TC_NT; // float4 of the Ainv chunk per thread (16)
   const int nchunks = (n + P.kc - 1) / P.kc;
-  const int ub      = P.k1 * (P.kc / 4);         // float4 of the U chunk (all threads)
+  const int ub      = k1 * (P.kc / 4);           // float4 of the U chunk (all threads)
   float4 ra[AV];
   float4 ru[(32 * (TC_KC / 4) + TC_NT - 1) / TC_NT * 2];
   // slot e of a (rows x kc) tile: 8 consecutive slots are the 8 rows of one core
@@ -208,13 +267,13 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
       if (e < ub)
         split_store(ru[q], P.b_hi, P.b_lo, cm_off(slot_row(e), slot_col(e), P.kc));
     }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
     if (tid == 0)
     {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t idesc = idesc_tf32(TC_M, P.k1);
+      tc_fence_after();
+      const uint32_t idesc = idesc_tf32(TC_M, k1);
       const uint32_t ah = smem_u32(sm + P.a_hi), al = smem_u32(sm + P.a_lo);
       const uint32_t bh = smem_u32(sm + P.b_hi), bl = smem_u32(sm + P.b_lo);
       for (int ks = 0; ks < P.kc / 8; ks++)
@@ -232,107 +291,84 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
     }
     if (ch + 1 < nchunks)
       load_chunk(ch + 1);
-    if (!mbar_wait(bar, phase))
-      ok = false;
-    phase ^= 1;
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    ok = wait_mma();
   }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 
+  const int r = warp * 32 + lane; // this thread's TMEM lane = block row
   if (ok)
   {
-    // ---------------- W = Binv V, stored transposed (n_pad rows x k1) for the second product
-    for (int i = tid; i < P.npad; i += TC_NT)
+    // ---------------- T1 - E from TMEM into the A tile of the second product
+    for (int c0 = 0; c0 < k1; c0 += 32)
     {
-      float vcol[32];
+      float t[32];
+      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
 #pragma unroll
-      for (int l = 0; l < 32; l++)
-        vcol[l] = (l < dc && i < n) ? Vs[l * n + i] : 0.f;
-      for (int c4 = 0; c4 < P.k1; c4 += 4)
+      for (int q = 0; q < 32; q++)
       {
-        float w[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-        {
-          const int c = c4 + q;
-          float a     = 0.f;
-          if (c < dc)
-#pragma unroll
-            for (int l = 0; l < 32; l++)
-              if (l < dc)
-                a += Bs[c * dc + l] * vcol[l];
-          w[q] = a;
-        }
-        float4 h = make_float4(tf32_hi(w[0]), tf32_hi(w[1]), tf32_hi(w[2]), tf32_hi(w[3]));
-        float4 lo = make_float4(w[0] - h.x, w[1] - h.y, w[2] - h.z, w[3] - h.w);
-        const uint32_t off = cm_off(i, c4, P.k1);
-        *reinterpret_cast<float4*>(sm + P.w_hi + off) = h;
-        if (TERMS > 1)
-          *reinterpret_cast<float4*>(sm + P.w_lo + off) = lo;
+        const int c = c0 + q;
+        if (c >= dc)
+          t[q] = 0.f;
+        else if (dls[c] == r0 + r)
+          t[q] -= 1.f;
       }
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        split_store(make_float4(t[q], t[q + 1], t[q + 2], t[q + 3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
     }
-    // ---------------- T1 - E from TMEM into the second product's A tile
+    __syncthreads(); // V has landed for every thread's copies
+    // ---------------- V^T into the B tile of the last product: element (i, l) = V[l][i]
+    for (int e = tid; e < P.npad * (k1 / 4); e += TC_NT)
     {
-      const int r = warp * 32 + lane; // this thread's TMEM lane = block row
-      for (int c0 = 0; c0 < P.k1; c0 += 32)
-      {
-        float t[32];
-        tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+      const int i = e % P.npad, l4 = (e / P.npad) * 4;
+      float x[4];
 #pragma unroll
-        for (int q = 0; q < 32; q++)
-        {
-          const int c = c0 + q;
-          if (c >= dc)
-            t[q] = 0.f;
-          else if (dls[c] == r0 + r)
-            t[q] -= 1.f;
-        }
-#pragma unroll
-        for (int q = 0; q < 32; q += 4)
-        {
-          float4 h = make_float4(tf32_hi(t[q]), tf32_hi(t[q + 1]), tf32_hi(t[q + 2]), tf32_hi(t[q + 3]));
-          float4 lo = make_float4(t[q] - h.x, t[q + 1] - h.y, t[q + 2] - h.z, t[q + 3] - h.w);
-          const uint32_t off = cm_off(r, c0 + q, P.k1);
-          *reinterpret_cast<float4*>(sm + P.a2_hi + off) = h;
-          if (TERMS > 1)
-            *reinterpret_cast<float4*>(sm + P.a2_lo + off) = lo;
-        }
-      }
+      for (int q = 0; q < 4; q++)
+        x[q] = (l4 + q < dc && i < n) ? Vs[(l4 + q) * n + i] : 0.f;
+      split_store(make_float4(x[0], x[1], x[2], x[3]), P.w_hi, P.w_lo, cm_off(i, l4, k1));
     }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads(); // V is read; Binv^T takes its place
+    stage_binv_t<TERMS>(sm, P.bt_hi, P.bt_lo, Binv, k, dc, k1, tid);
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
-    // ---------------- P = (T1 - E) W
+    // ---------------- X = (T1 - E) Binv into TMEM columns [0, k1)
     if (tid == 0)
     {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t idesc = idesc_tf32(TC_M, P.npad);
-      const uint32_t ah = smem_u32(sm + P.a2_hi), al = smem_u32(sm + P.a2_lo);
-      const uint32_t bh = smem_u32(sm + P.w_hi), bl = smem_u32(sm + P.w_lo);
-      for (int ks = 0; ks < P.k1 / 8; ks++)
-      {
-        const uint32_t adv = ks * 256;
-        mma_tf32(d2, smem_desc(ah + adv, P.k1), smem_desc(bh + adv, P.k1), idesc, ks ? 1 : 0);
-        if (TERMS > 1)
-        {
-          mma_tf32(d2, smem_desc(ah + adv, P.k1), smem_desc(bl + adv, P.k1), idesc, 1);
-          mma_tf32(d2, smem_desc(al + adv, P.k1), smem_desc(bh + adv, P.k1), idesc, 1);
-        }
-      }
+      tc_fence_after();
+      mma_k1<TERMS>(d1, sm, P.a2_hi, P.a2_lo, P.bt_hi, P.bt_lo, k1, idesc_tf32(TC_M, k1));
       mma_commit(bar);
     }
-    if (!mbar_wait(bar, phase))
-      ok = false;
-    phase ^= 1;
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    ok = wait_mma();
+  }
+  if (ok)
+  {
+    // ---------------- X from TMEM into the A tile of the last product
+    for (int c0 = 0; c0 < k1; c0 += 32)
+    {
+      float t[32];
+      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        split_store(make_float4(t[q], t[q + 1], t[q + 2], t[q + 3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
+    }
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
+    // ---------------- P = X V
+    if (tid == 0)
+    {
+      tc_fence_after();
+      mma_k1<TERMS>(d2, sm, P.a2_hi, P.a2_lo, P.w_hi, P.w_lo, k1, idesc_tf32(TC_M, P.npad));
+      mma_commit(bar);
+    }
+    ok = wait_mma();
   }
 
   if (ok)
   {
     // ---------------- epilogue: Ainv[rows] -= P, each thread one row; the next
     // 32-column piece of the row is loaded while the current one is written
-    const int r  = warp * 32 + lane;
     const int gr = r0 + r;
     float* row   = A + (size_t)(gr < n ? gr : 0) * lda;
     float4 cur[8], nxt[8];
@@ -378,10 +414,11 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 }
 
 // ---------------------------------------------------------------------------
-// N-tiled variant for large determinants and delay ranks up to 64: the second
-// product runs over column tiles of TN inverse columns, W = Binv V is formed
-// per tile from global V, so neither N nor k is bounded by TMEM or by a full V in
-// shared memory.  TMEM: T1 in columns [0, KM), the product tile in [KM, KM + TN).
+// N-tiled variant for large determinants and delay ranks up to 64: X = (T1 - E) Binv
+// is formed once, the last product runs over column tiles of TN inverse columns
+// with each V^T tile staged from global V, so neither N nor k is bounded by TMEM or
+// by a full V in shared memory.  TMEM: T1 and then X in columns [0, KM), the
+// product tile in [KM, KM + TN).
 // Two instances: delay ranks up to 64 with 128-column tiles (256 TMEM columns, one CTA
 // per SM by shared memory), and delay ranks up to 32 with 96-column tiles (128 TMEM
 // columns and 70 KB of shared memory: three CTAs per SM).
@@ -391,10 +428,11 @@ constexpr int TT_KMAX = 64;
 
 struct TtPlan
 {
-  int k1;                    // delay rank padded to 16
-  uint32_t a_hi, a_lo, u_hi, u_lo; // first product: 128 x KC and k1 x KC
-  uint32_t a2_hi, a2_lo, w_hi, w_lo; // second product: 128 x k1 and TN x k1
-  uint32_t binv, dl, bar, total;
+  int k1;                            // delay rank padded to 16
+  uint32_t a_hi, a_lo, u_hi, u_lo;   // first product: 128 x KC and k1 x KC
+  uint32_t a2_hi, a2_lo, w_hi, w_lo; // later products: 128 x k1 (T1 - E, then X) and TN x k1 (V^T tile)
+  uint32_t bt_hi, bt_lo;             // Binv^T: k1 x k1
+  uint32_t dl, bar, total;
 };
 
 __host__ __device__ inline TtPlan tt_plan(int k, int TN)
@@ -412,8 +450,9 @@ __host__ __device__ inline TtPlan tt_plan(int k, int TN)
   p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.w_hi  = o2; o2 = al(o2 + TN * p.k1 * 4);
   p.w_lo  = o2; o2 = al(o2 + TN * p.k1 * 4);
+  p.bt_hi = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
+  p.bt_lo = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
   o = o > o2 ? o : o2;
-  p.binv  = o; o = al(o + k * k * 4);
   p.dl    = o; o = al(o + k * 4);
   p.bar   = o; o += 16;
   p.total = al(o);
@@ -436,7 +475,6 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
   const float* V   = f.v + (size_t)iw * f.sU;
   const float* Bi  = f.binv + (size_t)iw * f.sB;
   const int* dlist = f.delay_list + (size_t)iw * f.sD;
-  float* Bs        = reinterpret_cast<float*>(sm + P.binv);
   int* dls         = reinterpret_cast<int*>(sm + P.dl);
   const uint32_t bar = smem_u32(sm + P.bar);
   if (tid == 0)
@@ -446,8 +484,6 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
   }
   if (warp == 0)
     tmem_alloc(smem_u32(&s_tmem), TMC);
-  for (int e = tid; e < dc * dc; e += TC_NT)
-    Bs[e] = Bi[(size_t)(e / dc) * k + (e % dc)];
   for (int e = tid; e < dc; e += TC_NT)
     dls[e] = dlist[e];
   tc_fence_before();
@@ -520,10 +556,10 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     ok = wait_mma();
   }
 
-  // ---------------- (T1 - E) from TMEM into the second product's A operand
+  // ---------------- (T1 - E) from TMEM into the A operand of X = (T1 - E) Binv
+  const int r = warp * 32 + lane;
   if (ok)
   {
-    const int r = warp * 32 + lane;
     for (int c0 = 0; c0 < k1; c0 += 32)
     {
       float t[32];
@@ -547,36 +583,43 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
           split_store(make_float4(v[0], v[1], v[2], v[3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
         }
     }
+    stage_binv_t<TERMS>(sm, P.bt_hi, P.bt_lo, Bi, k, dc, k1, tid);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0)
+    {
+      tc_fence_after();
+      mma_k1<TERMS>(d1, sm, P.a2_hi, P.a2_lo, P.bt_hi, P.bt_lo, k1, idesc_tf32(TC_M, k1));
+      mma_commit(bar);
+    }
+    ok = wait_mma();
   }
-  // ---------------- column tiles: W_tile = Binv V[:, tile], P_tile = (T1 - E) W_tile^T, Ainv -= P
+  // ---------------- X from TMEM into the A operand of the column-tile products
+  if (ok)
+  {
+    for (int c0 = 0; c0 < k1; c0 += 32)
+    {
+      float t[32];
+      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        if (c0 + q < k1)
+          split_store(make_float4(t[q], t[q + 1], t[q + 2], t[q + 3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
+    }
+  }
+  // ---------------- column tiles: P_tile = X V[:, tile], Ainv -= P
   for (int t0 = 0; t0 < n && ok; t0 += TN)
   {
-    if (tid < TN)
+    // V^T tile: element (i, l) = V[l][t0 + i], consecutive threads on consecutive columns
+    for (int e = tid; e < TN * (k1 / 4); e += TC_NT)
     {
-      // thread i owns column t0 + i of the tile
-      const int i = tid;
-      const int col = t0 + i;
-      float vcol[KM];
+      const int i = e % TN, l4 = (e / TN) * 4, col = t0 + i;
+      float x[4];
 #pragma unroll
-      for (int l = 0; l < KM; l++)
-        vcol[l] = (l < dc && col < n) ? V[(size_t)l * lda + col] : 0.f;
-      for (int c4 = 0; c4 < k1; c4 += 4)
-      {
-        float w[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-        {
-          const int c = c4 + q;
-          float a     = 0.f;
-          if (c < dc)
-#pragma unroll
-            for (int l = 0; l < KM; l++)
-              if (l < dc)
-                a += Bs[c * dc + l] * vcol[l];
-          w[q] = a;
-        }
-        split_store(make_float4(w[0], w[1], w[2], w[3]), P.w_hi, P.w_lo, cm_off(i, c4, k1));
-      }
+      for (int q = 0; q < 4; q++)
+        x[q] = (l4 + q < dc && col < n) ? V[(size_t)(l4 + q) * lda + col] : 0.f;
+      split_store(make_float4(x[0], x[1], x[2], x[3]), P.w_hi, P.w_lo, cm_off(i, l4, k1));
     }
     fence_async_smem();
     tc_fence_before();
@@ -584,26 +627,13 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     if (tid == 0)
     {
       tc_fence_after();
-      const uint32_t id = idesc_tf32(TC_M, TN);
-      const uint32_t ah = smem_u32(sm + P.a2_hi), al = smem_u32(sm + P.a2_lo);
-      const uint32_t bh = smem_u32(sm + P.w_hi), bl = smem_u32(sm + P.w_lo);
-      for (int ks = 0; ks < k1 / 8; ks++)
-      {
-        const uint32_t adv = ks * 256;
-        mma_tf32(d2, smem_desc(ah + adv, k1), smem_desc(bh + adv, k1), id, ks ? 1 : 0);
-        if (TERMS > 1)
-        {
-          mma_tf32(d2, smem_desc(ah + adv, k1), smem_desc(bl + adv, k1), id, 1);
-          mma_tf32(d2, smem_desc(al + adv, k1), smem_desc(bh + adv, k1), id, 1);
-        }
-      }
+      mma_k1<TERMS>(d2, sm, P.a2_hi, P.a2_lo, P.w_hi, P.w_lo, k1, idesc_tf32(TC_M, TN));
       mma_commit(bar);
     }
     ok = wait_mma();
     if (!ok)
       break;
     // epilogue: each thread one inverse row, 32 columns at a time
-    const int r  = warp * 32 + lane;
     const int gr = r0 + r;
     float* row   = A + (size_t)(gr < n ? gr : 0) * lda + t0;
     for (int c0 = 0; c0 < TN; c0 += 32)

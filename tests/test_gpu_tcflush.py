@@ -34,7 +34,7 @@ def call_ex(method, arrays, dc):
 
 @pytest.mark.parametrize("method,tol", [(3, 1e-5), (1, 5e-3)])
 @pytest.mark.parametrize("nw,n,lda,k,dc", [(3, 20, 32, 4, 4), (2, 64, 64, 16, 9), (4, 192, 192, 32, 32),
-                                           (2, 200, 208, 32, 17),
+                                           (2, 200, 208, 32, 17), (2, 256, 256, 32, 5), (3, 96, 100, 8, 8),
                                            # N-tiled kernel: k > 32 or n_pad > 256 (one MMA's largest N)
                                            (3, 192, 192, 64, 37), (2, 300, 304, 48, 41), (2, 520, 528, 16, 9),
                                            (2, 384, 384, 32, 32),
@@ -53,6 +53,23 @@ def test_tensor_core_flush_rejects_fp64():
     from qmcpack_gb300 import _lib
     L = _lib.load()
     assert L.qmcg_mw_update_inv_mat_ex(8, 1, 16, 16, 4, 2, None, None, None, None, None, 3, None) == -1
+
+
+def test_tensor_core_flush_rejects_misaligned_buffers():
+    """Rows are moved as 16-byte vectors: a base off a 16-byte boundary is an argument error."""
+    import ctypes as C
+    import torch
+    from qmcpack_gb300 import _lib
+    L = _lib.load()
+    A, U, V, B, dl = flush_case(1, 16, 16, 4, 4, seed=1)
+    tA, tU, tV, tB = (torch.tensor(x, dtype=torch.float32, device="cuda") for x in (A, U, V, B))
+    tD = torch.tensor(dl, dtype=torch.int32, device="cuda")
+    before = tA.clone()
+    rc = L.qmcg_mw_update_inv_mat_ex(4, 1, 12, 16, 4, 4, C.c_void_p(tA.data_ptr() + 4), C.c_void_p(tU.data_ptr()),
+                                     C.c_void_p(tV.data_ptr()), C.c_void_p(tB.data_ptr()),
+                                     C.c_void_p(tD.data_ptr()), 3, None)
+    assert rc == -1 and b"16-byte" in L.qmcg_last_error()
+    assert torch.equal(before, tA)
 
 
 def test_fullsize_sweeps_with_tensor_core_flush():
