@@ -150,6 +150,63 @@ __device__ __forceinline__ void mma_k1(uint32_t d, unsigned char* sm, uint32_t a
   }
 }
 
+// Ainv[r0 + (0..127), c_begin + [0, ncol)) -= P with P in TMEM columns [dcol, dcol + ncol),
+// ncol a multiple of 32.  P passes through shared memory E (128 rows of pitch EW + 4
+// floats: 16-byte stores by row and loads along a row are both conflict-free) in chunks
+// of EW columns, so every global load and store of a warp covers whole 128-byte row
+// segments; a chunk's loads are all issued before its first store.
+template<int EW>
+__device__ __forceinline__ void epilogue_rows(float* A, int lda, int n, int r0, int c_begin, int ncol, uint32_t dcol,
+                                              float* E, int tid)
+{
+  static_assert(EW == 32 || EW == 64, "chunk of 32 or 64 columns");
+  constexpr int EP = EW + 4;
+  constexpr int Q  = EW / 4; // float4 per thread of a full chunk: 128 rows x EW / 4 / 128 threads
+  const int warp   = tid >> 5; // this thread's TMEM lane is block row tid
+  for (int c0 = 0; c0 < ncol; c0 += EW)
+  {
+    const int w = ncol - c0 < EW ? ncol - c0 : EW; // 32 or EW
+#pragma unroll
+    for (int h = 0; h < EW; h += 32)
+      if (h < w)
+      {
+        float p[32];
+        tmem_ld32(dcol + ((uint32_t)(warp * 32) << 16) + c0 + h, p);
+#pragma unroll
+        for (int q = 0; q < 32; q += 4)
+          *reinterpret_cast<float4*>(E + tid * EP + h + q) = make_float4(p[q], p[q + 1], p[q + 2], p[q + 3]);
+      }
+    __syncthreads();
+    const int sh = (w == 64) ? 4 : 3; // log2 of the float4 in one row of the chunk
+    float4 av[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+    {
+      const int e = tid + q * TC_NT, rr = e >> sh, c4 = (e & ((1 << sh) - 1)) * 4;
+      const int gr = r0 + rr, gc = c_begin + c0 + c4;
+      av[q] = (rr < TC_M && gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+    {
+      const int e = tid + q * TC_NT, rr = e >> sh, c4 = (e & ((1 << sh) - 1)) * 4;
+      const int gr = r0 + rr, gc = c_begin + c0 + c4;
+      if (rr < TC_M && gr < n && gc < n)
+      {
+        const float4 p = *reinterpret_cast<const float4*>(E + rr * EP + c4);
+        float4 a       = av[q];
+        a.x -= p.x;
+        a.y -= p.y;
+        a.z -= p.z;
+        a.w -= p.w;
+        *reinterpret_cast<float4*>(A + (size_t)gr * lda + gc) = a;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // The update is evaluated as P = ((T1 - E) Binv) V: the k x k product runs on the
 // tensor cores once per row block (128 x k1 x k1) instead of forming W = Binv V
 // (k x k x n) on the CUDA cores in every row block; V enters the last product as
@@ -367,42 +424,9 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 
   if (ok)
   {
-    // ---------------- epilogue: Ainv[rows] -= P, each thread one row; the next
-    // 32-column piece of the row is loaded while the current one is written
-    const int gr = r0 + r;
-    float* row   = A + (size_t)(gr < n ? gr : 0) * lda;
-    float4 cur[8], nxt[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++)
-      cur[q] = (gr < n && 4 * q < n) ? *reinterpret_cast<const float4*>(row + 4 * q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int c0 = 0; c0 < P.npad; c0 += 32)
-    {
-#pragma unroll
-      for (int q = 0; q < 8; q++)
-      {
-        const int c = c0 + 32 + 4 * q;
-        nxt[q] = (gr < n && c < n) ? *reinterpret_cast<const float4*>(row + c) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      float p[32];
-      tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
-      if (gr < n)
-      {
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-          if (c0 + 4 * q < n)
-          {
-            float4 a = cur[q];
-            a.x -= p[4 * q];
-            a.y -= p[4 * q + 1];
-            a.z -= p[4 * q + 2];
-            a.w -= p[4 * q + 3];
-            *reinterpret_cast<float4*>(row + c0 + 4 * q) = a;
-          }
-      }
-#pragma unroll
-      for (int q = 0; q < 8; q++)
-        cur[q] = nxt[q];
-    }
+    // ---------------- epilogue: Ainv[rows] -= P through shared memory over the
+    // first product's region (every MMA has completed)
+    epilogue_rows<64>(A, lda, n, r0, 0, (P.npad + 31) & ~31, d2, reinterpret_cast<float*>(sm), tid);
   }
   else if (tid == 0)
     atomicExch(err, 1);
@@ -424,6 +448,8 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 // columns and 70 KB of shared memory: three CTAs per SM).
 // ---------------------------------------------------------------------------
 constexpr int TT_KC = 32;  // K chunk of the first product
+// epilogue chunk (columns) of a product tile of TN columns
+__host__ __device__ constexpr int TT_EW(int TN) { return TN % 64 == 0 ? 64 : 32; }
 constexpr int TT_KMAX = 64;
 
 struct TtPlan
@@ -452,6 +478,9 @@ __host__ __device__ inline TtPlan tt_plan(int k, int TN)
   p.w_lo  = o2; o2 = al(o2 + TN * p.k1 * 4);
   p.bt_hi = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
   p.bt_lo = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
+  // the epilogue's staging of the product tile overlays the V^T tile and Binv^T
+  const uint32_t eend = al(p.w_hi + TC_M * (TT_EW(TN) + 4) * 4);
+  o2 = o2 > eend ? o2 : eend;
   o = o > o2 ? o : o2;
   p.dl    = o; o = al(o + k * 4);
   p.bar   = o; o += 16;
@@ -633,26 +662,8 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     ok = wait_mma();
     if (!ok)
       break;
-    // epilogue: each thread one inverse row, 32 columns at a time
-    const int gr = r0 + r;
-    float* row   = A + (size_t)(gr < n ? gr : 0) * lda + t0;
-    for (int c0 = 0; c0 < TN; c0 += 32)
-    {
-      float p[32];
-      tmem_ld32(d2 + ((uint32_t)(warp * 32) << 16) + c0, p);
-      if (gr < n)
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-          if (t0 + c0 + 4 * q < n)
-          {
-            float4 a = *reinterpret_cast<const float4*>(row + c0 + 4 * q);
-            a.x -= p[4 * q];
-            a.y -= p[4 * q + 1];
-            a.z -= p[4 * q + 2];
-            a.w -= p[4 * q + 3];
-            *reinterpret_cast<float4*>(row + c0 + 4 * q) = a;
-          }
-    }
+    // epilogue through shared memory over the V^T tile (its MMA has completed)
+    epilogue_rows<TT_EW(TN)>(A, lda, n, r0, t0, TN, d2, reinterpret_cast<float*>(sm + P.w_hi), tid);
     tc_fence_before();
     __syncthreads();
   }
