@@ -38,20 +38,11 @@ struct Vec<double>
   }
 };
 
-// ---------------------------------------------------------------------------
-// Tricubic spline VGL of all orbitals at one position, split over the block:
-// a work unit is (orbital vector c, x-offset i); it reads the 16 (y,z) rows of
-// its x-plane with vector loads that are contiguous over orbitals, and writes
-// 7 partial sums (v, gx, gy, gz, hxx, hyy, hzz) to part[i][7][lda].
-// ---------------------------------------------------------------------------
-// Units [u_lo, u_hi) are handed to threads t, t + nt, ... (t = the caller's rank).
+// fractional coordinates of pos in [0, 1): the FP64 part of a spline evaluation, which
+// one thread can do for a whole CTA (FP64 arithmetic is slow on this GPU)
 template<typename T>
-__device__ __forceinline__ void spline_partials(const DevState<T>& s, const double pos[3], T* part,
-                                                int t = threadIdx.x, int nt = blockDim.x, int u_lo = 0,
-                                                int u_hi = 1 << 30)
+__device__ __forceinline__ void spline_frac(const DevState<T>& s, const double pos[3], T ru[3])
 {
-  constexpr int W = Vec<T>::W;
-  T ru[3];
 #pragma unroll
   for (int d = 0; d < 3; d++)
   {
@@ -62,6 +53,35 @@ __device__ __forceinline__ void spline_partials(const DevState<T>& s, const doub
       u -= floor(u);
     ru[d] = u;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Tricubic spline VGL of all orbitals at one position, split over the block:
+// a work unit is (orbital vector c, x-offset i); it reads the 16 (y,z) rows of
+// its x-plane with vector loads that are contiguous over orbitals, and writes
+// 7 partial sums (v, gx, gy, gz, hxx, hyy, hzz) to part[i][7][lda].
+// ---------------------------------------------------------------------------
+// Units [u_lo, u_hi) are handed to threads t, t + nt, ... (t = the caller's rank).
+template<typename T>
+__device__ __forceinline__ void spline_partials_frac(const DevState<T>& s, const T ru[3], T* part,
+                                                     int t = threadIdx.x, int nt = blockDim.x, int u_lo = 0,
+                                                     int u_hi = 1 << 30);
+
+template<typename T>
+__device__ __forceinline__ void spline_partials(const DevState<T>& s, const double pos[3], T* part,
+                                                int t = threadIdx.x, int nt = blockDim.x, int u_lo = 0,
+                                                int u_hi = 1 << 30)
+{
+  T ru[3];
+  spline_frac(s, pos, ru);
+  spline_partials_frac(s, ru, part, t, nt, u_lo, u_hi);
+}
+
+template<typename T>
+__device__ __forceinline__ void spline_partials_frac(const DevState<T>& s, const T ru[3], T* part, int t, int nt,
+                                                     int u_lo, int u_hi)
+{
+  constexpr int W = Vec<T>::W;
   int ix, iy, iz;
   T tx, ty, tz;
   spline_bound(ru[0] * T(s.gx), s.gx - 1, ix, tx);

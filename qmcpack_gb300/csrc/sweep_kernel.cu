@@ -76,29 +76,40 @@ __device__ __forceinline__ void prefetch_rows(const DevState<T>& s, size_t slot,
 }
 
 // out[c] = scale * (rows[c] . x) for c < nrows (rows in global memory, stride ld,
-// x in shared memory): every warp owns up to 8 rows and issues all their loads
-// before reducing
+// x in shared memory): every warp owns up to 8 rows and issues the loads of four
+// 32-column strips of all of them (32 loads in flight) before the first product
 template<typename T, int NT>
 __device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const T* x, int n, T* out, T scale)
 {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int NW = NT / 32;
+  constexpr int JB = 4; // 32-column strips per batch of loads
   for (int c0 = wid; c0 < nrows; c0 += 8 * NW)
   {
     T a[8];
 #pragma unroll
     for (int q = 0; q < 8; q++)
       a[q] = T(0);
-    for (int j = lane; j < n; j += 32)
+    for (int jb = lane; jb < n; jb += 32 * JB)
     {
-      const T xj = x[j];
+      T v[JB][8], xv[JB];
 #pragma unroll
-      for (int q = 0; q < 8; q++)
+      for (int u = 0; u < JB; u++)
       {
-        const int c = c0 + q * NW;
-        if (c < nrows)
-          a[q] += rows[(size_t)c * ld + j] * xj;
+        const int j = jb + 32 * u;
+        xv[u]       = j < n ? x[j] : T(0);
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+        {
+          const int c = c0 + q * NW;
+          v[u][q]     = (c < nrows && j < n) ? rows[(size_t)c * ld + j] : T(0);
+        }
       }
+#pragma unroll
+      for (int u = 0; u < JB; u++)
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          a[q] += v[u][q] * xv[u];
     }
 #pragma unroll
     for (int q = 0; q < 8; q++)
@@ -132,6 +143,8 @@ template<typename T, bool LEARNED>
 struct SweepShared
 {
   double pos[3];
+  T posT[3]; // the proposed position in the move-loop precision
+  T ru[3];   // its fractional coordinates (spline_frac)
   T disp[3];
   T gauss[3];
   T loggf;
@@ -295,7 +308,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
               const T dd = drift[d] + st * mu + st * exp(sd) * sh.gauss[d];
               sh.disp[d]  = dd;
               sh.pos[d]   = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(dd);
+              sh.posT[d]  = static_cast<T>(sh.pos[d]);
             }
+            spline_frac(s, sh.pos, sh.ru);
             sh.loggf = -sum_s - T(0.5) * x2;
           }
           __syncthreads();
@@ -333,7 +348,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           {
             sh.disp[d] = drift[d];
             sh.pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
+            sh.posT[d] = static_cast<T>(sh.pos[d]);
           }
+          spline_frac(s, sh.pos, sh.ru);
           sh.loggf = s.use_drift
               ? -(T(0.5) / tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
               : T(0);
@@ -342,12 +359,12 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         }
       }
       // ------------------------------------------------ evaluation at the proposed position
-      const double pos[3] = {sh.pos[0], sh.pos[1], sh.pos[2]};
+      // the FP64 position and its fractional coordinates were converted once, by thread 0
       T acc[14];
 #pragma unroll
       for (int q = 0; q < 14; q++)
         acc[q] = T(0);
-      const T x0 = static_cast<T>(pos[0]), y0 = static_cast<T>(pos[1]), z0 = static_cast<T>(pos[2]);
+      const T x0 = sh.posT[0], y0 = sh.posT[1], z0 = sh.posT[2];
       // Jastrow rows against the positions in shared memory, threads t0, t0 + stride, ...
       auto jastrow_rows = [&](int t0, int stride) {
         if (s.has_j2)
@@ -393,7 +410,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
             }
           }
       };
-      spline_partials(s, pos, part);
+      spline_partials_frac(s, sh.ru, part);
       jastrow_rows(threadIdx.x, NT);
       __syncthreads();
       for (int o = threadIdx.x; o < n; o += NT)
@@ -485,7 +502,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       if constexpr (LEARNED)
       {
         // the network at the proposed position: the reverse density q(r | R')
-        const T pn[3] = {T(sh.pos[0]), T(sh.pos[1]), T(sh.pos[2])};
+        const T pn[3] = {sh.posT[0], sh.posT[1], sh.posT[2]};
         features_cta(s, Rs, iat, pn, sh.lsm.g, sh.lsm.x);
         __syncthreads();
         mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, sh.lsm.x, sh.lsm.h, sh.lsm.red, sh.lsm.out);
