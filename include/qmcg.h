@@ -157,6 +157,17 @@ int qmcg_mw_accept_reject_move(qmcg_crowd crowd, int iat, const int* accepted);
 /* Flush pending delayed updates.  TrialWaveFunction::mw_completeUpdates (TrialWaveFunction.cpp:833). */
 int qmcg_mw_complete_updates(qmcg_crowd crowd);
 
+/* From-scratch recompute of the walkers with flags[iw] != 0 (host array [nw]) by the
+ * repair path the resident sweeps use when a walker's tracked inverse loses accuracy:
+ * orbitals, inverse and log|det| of both spins and the Jastrow state.  The inverse is a
+ * Gauss-Jordan elimination over a cluster of SMs per matrix, in FP32 for precision-4
+ * crowds (FP64 log|det| sums; the reference inverts in full precision, which this GPU
+ * runs at a small fraction of its FP32 rate) and in FP64 otherwise.
+ * TrialWaveFunction::mw_recompute with its recompute mask (TrialWaveFunction.cpp:225-240;
+ * DiracDeterminantBatched::mw_recompute, DiracDeterminantBatched.cpp:1121-1196).
+ * Returns QMCG_ERR_STATE while delayed updates are pending. */
+int qmcg_mw_recompute_walkers(qmcg_crowd crowd, const int* flags);
+
 /* Tracked log|psi| per walker (determinant logs accumulated from accepted ratios plus
  * the Jastrow state), signs (+1/-1), parts [nw][4] = log|det_up|, log|det_dn|, log J1,
  * log J2.  Any pointer may be NULL. */

@@ -14,7 +14,7 @@ _ip = C.POINTER(C.c_int)
 EXPORTS = [
     "qmcg_last_error", "qmcg_device_count", "qmcg_system_create", "qmcg_system_destroy",
     "qmcg_crowd_create", "qmcg_crowd_destroy", "qmcg_crowd_stream", "qmcg_load_walkers",
-    "qmcg_get_positions", "qmcg_mw_evaluate_log", "qmcg_mw_prepare_group", "qmcg_mw_eval_grad",
+    "qmcg_get_positions", "qmcg_mw_evaluate_log", "qmcg_mw_recompute_walkers", "qmcg_mw_prepare_group", "qmcg_mw_eval_grad",
     "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
@@ -78,6 +78,7 @@ def load(path: str = LIB_PATH):
         "qmcg_load_walkers": [vp, _dp],
         "qmcg_get_positions": [vp, _dp],
         "qmcg_mw_evaluate_log": [vp, _dp, _ip],
+        "qmcg_mw_recompute_walkers": [vp, _ip],
         "qmcg_mw_prepare_group": [vp, C.c_int],
         "qmcg_mw_eval_grad": [vp, C.c_int, _dp],
         "qmcg_mw_make_move": [vp, C.c_int, _dp, _ip],

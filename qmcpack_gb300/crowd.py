@@ -117,6 +117,11 @@ class Crowd:
         check(self.L.qmcg_mw_evaluate_log(self.handle, _p(lp), _p(sg, _ip)))
         return lp, sg
 
+    def mw_recompute_walkers(self, flags):
+        """From-scratch recompute of the flagged walkers by the repair path."""
+        f = np.ascontiguousarray(np.asarray(flags, dtype=np.int32).reshape(self.nw))
+        check(self.L.qmcg_mw_recompute_walkers(self.handle, _p(f, _ip)))
+
     def mw_prepareGroup(self, group: int):
         check(self.L.qmcg_mw_prepare_group(self.handle, group))
 

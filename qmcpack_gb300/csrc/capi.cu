@@ -403,6 +403,7 @@ struct qmcg_crowd_s
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
   virtual int local_energy(double* el, double* ke, double* vp) = 0;
   virtual int set_threads(int nt)                        = 0;
+  virtual int recompute_walkers(const int* flags)        = 0;
   virtual int proposal_init(uint64_t seed, double scale)  = 0;
   virtual int proposal_params(float* get, const float* set) = 0;
   virtual int proposal_forward(int rows, const float* x, float* out, float* hidden) = 0;
@@ -1042,6 +1043,23 @@ struct Crowd final : qmcg_crowd_s
         std::copy_n(h.data() + ((size_t)it * 3 + 1) * nw, nw, ke + (size_t)it * nw);
     }
     return QMCG_OK;
+  }
+
+  // the masked (repair) recompute of the flagged walkers
+  int recompute_walkers(const int* flags) override
+  {
+    if (!flags)
+      return fail(QMCG_ERR_ARG, "null flags");
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "delayed updates pending: call qmcg_mw_complete_updates first");
+    std::vector<int> st(nw);
+    for (int i = 0; i < nw; i++)
+      st[i] = flags[i] ? ST_ILLCOND : 0;
+    CUDA_TRY(cudaMemcpyAsync(s.status, st.data(), nw * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(launch_recompute<T>(s, Mt, 1, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    invrow_iat = -1;
+    return status_check();
   }
 
   int set_threads(int nt) override
@@ -1972,6 +1990,7 @@ extern "C" int qmcg_crowd_stream(qmcg_crowd c, void** stream)
 extern "C" int qmcg_load_walkers(qmcg_crowd c, const double* R) { CROWD_CALL(c, load(R)); }
 extern "C" int qmcg_get_positions(qmcg_crowd c, double* R) { CROWD_CALL(c, positions(R)); }
 extern "C" int qmcg_mw_evaluate_log(qmcg_crowd c, double* lp, int* sg) { CROWD_CALL(c, evaluate_log(lp, sg)); }
+extern "C" int qmcg_mw_recompute_walkers(qmcg_crowd c, const int* flags) { CROWD_CALL(c, recompute_walkers(flags)); }
 extern "C" int qmcg_mw_prepare_group(qmcg_crowd c, int group)
 {
   if (!c || group < 0 || group > 1)

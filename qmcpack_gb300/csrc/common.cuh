@@ -23,8 +23,16 @@ enum : int
   ST_NONFINITE   = 2,  // NaN/Inf ratio or gradient
   ST_SINGULAR    = 4,  // exact zero pivot in the FP64 inverse
   ST_ILLCOND     = 8,  // the tracked inverse lost accuracy: |Ainv[row] . phi(r_row) - 1| above tolerance
-  ST_REPAIR_MASK = ST_NONFINITE | ST_ILLCOND,
+  ST_ILLCOND_UP  = 16, // the same, found in the spin-up determinant only
+  ST_ILLCOND_DN  = 32, // the same, found in the spin-down determinant only
+  ST_REPAIR_MASK = ST_NONFINITE | ST_ILLCOND | ST_ILLCOND_UP | ST_ILLCOND_DN,
 };
+
+// repair bits that call for a new inverse of spin `spin`
+__host__ __device__ constexpr int st_repair_spin(int spin)
+{
+  return ST_NONFINITE | ST_ILLCOND | (spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
+}
 
 // tolerance of the self-ratio health check |Ainv[row] . phi(r_row) - 1|
 template<typename T>

@@ -9,6 +9,8 @@
 // mixed-precision move loop.  The inverse is a Gauss-Jordan elimination with
 // partial pivoting (same pivots as LU with partial pivoting), one CTA per matrix,
 // in FP64 whatever the move-loop precision.
+#include <type_traits>
+
 #include "common.cuh"
 #include "launch.h"
 #include "spline.cuh"
@@ -22,6 +24,14 @@ template<typename T>
 __device__ __forceinline__ bool skip_walker(const DevState<T>& s, int iw, int masked)
 {
   return masked && !(s.status[iw] & ST_REPAIR_MASK);
+}
+
+// the same for the inverse of one spin slot (spin * nw + iw): a walker whose check failed
+// in one determinant only has only that one inverted again
+template<typename T>
+__device__ __forceinline__ bool skip_slot(const DevState<T>& s, int slot, int masked)
+{
+  return masked && !(s.status[slot % s.nw] & st_repair_spin(slot / s.nw));
 }
 
 constexpr int VGL_EPB = 8; // electrons per CTA of the all-electron VGL
@@ -74,7 +84,7 @@ __global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt, 
 template<typename T, int NT>
 __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* Mt, int masked)
 {
-  if (skip_walker(s, blockIdx.x % s.nw, masked))
+  if (skip_slot(s, blockIdx.x, masked))
     return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = s.norb;
@@ -229,6 +239,7 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
 // ---------------------------------------------------------------------------
 constexpr int GJ_CL = 8;
 constexpr int GJ_NT = 256;
+constexpr int GJ_SMEM_MAX = 200 * 1024; // dynamic shared memory of the resident-block variant
 
 __device__ __forceinline__ void cluster_sync_all()
 {
@@ -248,7 +259,7 @@ template<typename T>
 __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double* Mt, int masked)
 {
   const int slot = blockIdx.x / GJ_CL;
-  if (skip_walker(s, slot % s.nw, masked)) // uniform over the cluster
+  if (skip_slot(s, slot, masked)) // uniform over the cluster
     return;
   extern __shared__ __align__(16) unsigned char gsm[];
   const int n = s.norb, r = (int)cluster_rank();
@@ -417,41 +428,60 @@ __device__ __forceinline__ double dsm_ld(unsigned addr)
   asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(addr) : "memory");
   return v;
 }
+__device__ __forceinline__ float dsm_ldf(unsigned addr)
+{
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];\n" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
 __device__ __forceinline__ int dsm_ldi(unsigned addr)
 {
   int v;
   asm volatile("ld.shared::cluster.s32 %0, [%1];\n" : "=r"(v) : "r"(addr) : "memory");
   return v;
 }
+template<typename W>
+__device__ __forceinline__ W dsm_ldw(unsigned addr);
+template<>
+__device__ __forceinline__ double dsm_ldw<double>(unsigned addr) { return dsm_ld(addr); }
+template<>
+__device__ __forceinline__ float dsm_ldw<float>(unsigned addr) { return dsm_ldf(addr); }
 
-__host__ __device__ inline size_t gj_smem_bytes(int n)
+// shared memory of the cluster Gauss-Jordan: pivot (row, value) [2][2] in FP64, the
+// CTA's column block [n][cw + 1], the published pivot column [2][n] and the local copy
+// of the current one [n] in the working type, pivot rows and the column map [n] each
+__host__ __device__ inline size_t gj_smem_bytes(int n, int cl, int wsize)
 {
-  const int cw = (n + GJ_CL - 1) / GJ_CL;
-  return sizeof(double) * ((size_t)n * (cw + 1) + 2 * (size_t)n + 4) + sizeof(int) * 2 * (size_t)n;
+  const int cw = (n + cl - 1) / cl;
+  return 4 * sizeof(double) + (size_t)wsize * ((size_t)n * (cw + 1) + 3 * (size_t)n) + sizeof(int) * 2 * (size_t)n;
 }
 
-template<typename T>
+// W = working precision of the elimination (the log|det| sums are FP64 either way);
+// CL = CTAs per matrix.  FP32 crowds repair in FP32: GB300's FP64 rate is a small
+// fraction of its FP32 rate, and the repaired inverse is stored in FP32.
+template<typename T, typename W, int CL>
 __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, double* Mt, int masked)
 {
-  const int slot = blockIdx.x / GJ_CL;
-  if (skip_walker(s, slot % s.nw, masked)) // uniform over the cluster
+  const int slot = blockIdx.x / CL;
+  if (skip_slot(s, slot, masked)) // uniform over the cluster
     return;
   extern __shared__ __align__(16) unsigned char gsm[];
   const int n = s.norb, r = (int)cluster_rank();
-  const int cw = (n + GJ_CL - 1) / GJ_CL, ld = cw + 1;
+  const int cw = (n + CL - 1) / CL, ld = cw + 1;
   const int c0 = r * cw, c1 = min(n, c0 + cw), ncw = max(0, c1 - c0);
-  double* blk = reinterpret_cast<double*>(gsm);        // [n][ld] own columns
-  double* pcs = blk + (size_t)n * ld;                  // [2][n] published pivot column
-  double* pds = pcs + 2 * (size_t)n;                   // [2][2] published pivot row, value
-  int* perm   = reinterpret_cast<int*>(pds + 4);       // [n] pivot rows of the columns this CTA owns
+  double* pds = reinterpret_cast<double*>(gsm);        // [2][2] published pivot row, value
+  W* blk      = reinterpret_cast<W*>(pds + 4);         // [n][ld] own columns
+  W* pcs      = blk + (size_t)n * ld;                  // [2][n] published pivot column
+  W* pcl      = pcs + 2 * (size_t)n;                   // [n] this step's pivot column, local copy
+  int* perm   = reinterpret_cast<int*>(pcl + n);       // [n] pivot rows of the columns this CTA owns
   int* cmap   = perm + n;                              // [n]
-  __shared__ double bval[GJ_NT / 32];
+  __shared__ W bval[GJ_NT / 32];
   __shared__ int bidx[GJ_NT / 32];
   double* a = Mt + (size_t)slot * n * n;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   for (int i = wid; i < n; i += GJ_NT / 32)
     for (int jj = lane; jj < ncw; jj += 32)
-      blk[(size_t)i * ld + jj] = a[(size_t)i * n + c0 + jj];
+      blk[(size_t)i * ld + jj] = static_cast<W>(a[(size_t)i * n + c0 + jj]);
   __syncthreads();
   double logabs = 0.0;
   int sgn = 1, bad = 0;
@@ -462,11 +492,11 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
     if (owner == r)
     {
       const int kk = k - c0;
-      double bv    = -1.0;
+      W bv         = W(-1);
       int bi       = n;
       for (int i = k + tid; i < n; i += GJ_NT)
       {
-        const double v = fabs(blk[(size_t)i * ld + kk]);
+        const W v = fabs(blk[(size_t)i * ld + kk]);
         if (v > bv || (v == bv && i < bi))
         {
           bv = v;
@@ -476,8 +506,8 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
       {
-        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi    = __shfl_xor_sync(0xffffffffu, bi, o);
+        const W ov   = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ov > bv || (ov == bv && oi < bi))
         {
           bv = ov;
@@ -490,65 +520,74 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
         bidx[wid] = bi;
       }
       __syncthreads();
-      double pb = bval[0];
-      int p     = bidx[0];
+      W pb  = bval[0];
+      int p = bidx[0];
       for (int w = 1; w < GJ_NT / 32; w++)
         if (bval[w] > pb || (bval[w] == pb && bidx[w] < p))
         {
           pb = bval[w];
           p  = bidx[w];
         }
-      if (!(pb > 0.0))
+      if (!(pb > W(0)))
         p = k;
       for (int i = tid; i < n; i += GJ_NT)
       {
-        const int src        = (i == p) ? k : i;
-        pcs[(size_t)b * n + i] = (i == k) ? 0.0 : blk[(size_t)src * ld + kk];
+        const int src          = (i == p) ? k : i;
+        pcs[(size_t)b * n + i] = (i == k) ? W(0) : blk[(size_t)src * ld + kk];
       }
       if (tid == 0)
       {
         pds[2 * b]     = (double)p;
-        pds[2 * b + 1] = pb > 0.0 ? blk[(size_t)p * ld + kk] : 0.0;
+        pds[2 * b + 1] = pb > W(0) ? static_cast<double>(blk[(size_t)p * ld + kk]) : 0.0;
         perm[k]        = p;
       }
     }
     cluster_sync_all();
     const unsigned rpd = dsm_map(pds + 2 * b, (unsigned)owner);
     const int p        = (int)dsm_ld(rpd);
-    const double d     = dsm_ld(rpd + 8);
-    if (!(fabs(d) > 0.0))
+    const double dd    = dsm_ld(rpd + 8);
+    if (!(fabs(dd) > 0.0))
     {
       bad = 1;
       break;
     }
-    logabs += log(fabs(d));
-    if (d < 0.0)
+    logabs += log(fabs(dd));
+    if (dd < 0.0)
       sgn = -sgn;
     if (p != k)
       sgn = -sgn;
+    const W d = static_cast<W>(dd);
     if (p != k)
       for (int jj = tid; jj < ncw; jj += GJ_NT)
       {
-        const double t            = blk[(size_t)k * ld + jj];
-        blk[(size_t)k * ld + jj]  = blk[(size_t)p * ld + jj];
-        blk[(size_t)p * ld + jj]  = t;
+        const W t                = blk[(size_t)k * ld + jj];
+        blk[(size_t)k * ld + jj] = blk[(size_t)p * ld + jj];
+        blk[(size_t)p * ld + jj] = t;
       }
+    // the owner's pivot column into local shared memory: one round trip over the cluster
+    // for all rows instead of one per row
+    const unsigned rpc = dsm_map(pcs + (size_t)b * n, (unsigned)owner);
+    for (int i = tid; i < n; i += GJ_NT)
+      pcl[i] = dsm_ldw<W>(rpc + (unsigned)sizeof(W) * (unsigned)i);
     __syncthreads();
     for (int jj = tid; jj < ncw; jj += GJ_NT)
-      blk[(size_t)k * ld + jj] = (c0 + jj == k ? 1.0 : blk[(size_t)k * ld + jj]) / d;
+      blk[(size_t)k * ld + jj] = (c0 + jj == k ? W(1) : blk[(size_t)k * ld + jj]) / d;
     __syncthreads();
-    const unsigned rpc = dsm_map(pcs + (size_t)b * n, (unsigned)owner);
-    for (int i = wid; i < n; i += GJ_NT / 32)
+    // elimination over (rows x own columns) with 16 threads along a row
     {
-      if (i == k)
-        continue;
-      const double f = dsm_ld(rpc + 8u * (unsigned)i);
-      double* bi     = blk + (size_t)i * ld;
-      const double* bk = blk + (size_t)k * ld;
-      for (int jj = lane; jj < ncw; jj += 32)
+      const int tx = tid & 15, ty = tid >> 4;
+      const W* bk  = blk + (size_t)k * ld;
+      for (int i = ty; i < n; i += GJ_NT / 16)
       {
-        const double base = (c0 + jj == k) ? 0.0 : bi[jj];
-        bi[jj]            = base - f * bk[jj];
+        if (i == k)
+          continue;
+        const W f = pcl[i];
+        W* bi     = blk + (size_t)i * ld;
+        for (int jj = tx; jj < ncw; jj += 16)
+        {
+          const W base = (c0 + jj == k) ? W(0) : bi[jj];
+          bi[jj]       = base - f * bk[jj];
+        }
       }
     }
     __syncthreads();
@@ -557,7 +596,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
   // column cmap[j], possibly of another CTA)
   for (int i = wid; i < n; i += GJ_NT / 32)
     for (int jj = lane; jj < ncw; jj += 32)
-      a[(size_t)i * n + c0 + jj] = blk[(size_t)i * ld + jj];
+      a[(size_t)i * n + c0 + jj] = static_cast<double>(blk[(size_t)i * ld + jj]);
   cluster_sync_all();
   if (bad)
   {
@@ -682,6 +721,8 @@ __global__ void finish_repair_kernel(DevState<T> s)
   }
 }
 
+static bool gj_cluster16_ok();
+
 template<typename T>
 cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaStream_t st)
 {
@@ -694,27 +735,48 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
     return e;
   if (masked && s.gj_scratch)
   {
-    // the few flagged matrices: a cluster of GJ_CL SMs each
+    // the few flagged matrices: a cluster of SMs each
+    const int n            = s.norb;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim            = dim3(2 * s.nw * GJ_CL);
     cfg.blockDim           = dim3(GJ_NT);
-    const int cw           = (s.norb + GJ_CL - 1) / GJ_CL;
-    cfg.dynamicSmemBytes   = (size_t)cw * sizeof(double) + (size_t)s.norb * sizeof(int);
     cfg.stream             = st;
     cudaLaunchAttribute attr[1];
     attr[0].id               = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = GJ_CL;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs                = attr;
     cfg.numAttrs             = 1;
-    if (gj_smem_bytes(s.norb) <= 200 * 1024)
+    auto with_cluster = [&](int cl, size_t smem) {
+      cfg.gridDim              = dim3(2 * s.nw * cl);
+      attr[0].val.clusterDim.x = cl;
+      cfg.dynamicSmemBytes     = smem;
+    };
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value)
     {
-      cfg.dynamicSmemBytes = gj_smem_bytes(s.norb);
-      e = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<T>, s, Mt, masked);
+      if (gj_smem_bytes(n, 8, 4) <= GJ_SMEM_MAX)
+      {
+        with_cluster(8, gj_smem_bytes(n, 8, 4));
+        e    = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<float, float, 8>, s, Mt, masked);
+        done = true;
+      }
+      else if (gj_smem_bytes(n, 16, 4) <= GJ_SMEM_MAX && gj_cluster16_ok())
+      {
+        with_cluster(16, gj_smem_bytes(n, 16, 4));
+        e    = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<float, float, 16>, s, Mt, masked);
+        done = true;
+      }
     }
-    else
+    if (!done && gj_smem_bytes(n, GJ_CL, 8) <= GJ_SMEM_MAX)
+    {
+      with_cluster(GJ_CL, gj_smem_bytes(n, GJ_CL, 8));
+      e = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<T, double, GJ_CL>, s, Mt, masked);
+    }
+    else if (!done)
+    {
+      with_cluster(GJ_CL, (size_t)((n + GJ_CL - 1) / GJ_CL) * sizeof(double) + (size_t)n * sizeof(int));
       e = cudaLaunchKernelEx(&cfg, gj_cluster_kernel<T>, s, Mt, masked);
+    }
   }
   else
   {
@@ -739,9 +801,50 @@ cudaError_t setup_recompute_kernels()
 {
   cudaError_t e = cudaFuncSetAttribute(vgl_all_kernel<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(gj_cluster_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    e = cudaFuncSetAttribute(gj_cluster_smem_kernel<T, double, GJ_CL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             GJ_SMEM_MAX);
+  if constexpr (std::is_same<T, float>::value)
+  {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gj_cluster_smem_kernel<float, float, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               GJ_SMEM_MAX);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gj_cluster_smem_kernel<float, float, 16>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, GJ_SMEM_MAX);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gj_cluster_smem_kernel<float, float, 16>,
+                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  }
   return e;
 }
+
+// whether a cluster of 16 CTAs with the largest column block can be resident on this
+// GPU (16 is above the portable cluster size); asked once per process
+static bool gj_cluster16_ok()
+{
+  static int ok = -1;
+  if (ok < 0)
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = dim3(16);
+    cfg.blockDim           = dim3(GJ_NT);
+    cfg.dynamicSmemBytes   = GJ_SMEM_MAX;
+    cudaLaunchAttribute attr[1];
+    attr[0].id               = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs                = attr;
+    cfg.numAttrs             = 1;
+    int nc                   = 0;
+    const cudaError_t e      = cudaOccupancyMaxActiveClusters(&nc, gj_cluster_smem_kernel<float, float, 16>, &cfg);
+    if (e != cudaSuccess)
+      (void)cudaGetLastError();
+    ok = (e == cudaSuccess && nc >= 1) ? 1 : 0;
+  }
+  return ok == 1;
+}
+
 template cudaError_t setup_recompute_kernels<float>();
 template cudaError_t setup_recompute_kernels<double>();
 template cudaError_t launch_recompute<float>(const DevState<float>&, double*, int, cudaStream_t);

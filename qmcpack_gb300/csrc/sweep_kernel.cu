@@ -277,7 +277,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           if (threadIdx.x == 0)
           {
             if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
-              atomicOr(s.status + w, ST_ILLCOND);
+              atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
             for (int d = 0; d < 3; d++)
             {
               T gs = g[d];
@@ -320,7 +320,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         if (threadIdx.x == 0)
         {
           if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
-            atomicOr(s.status + w, ST_ILLCOND);
+            atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
           T gn[3];
           for (int d = 0; d < 3; d++)
           {
