@@ -10,9 +10,10 @@
 // back with tcgen05.ld for the epilogue.
 //
 // Split precision (3xTF32): every FP32 operand x is split as hi = rna_tf32(x),
-// lo = x - hi, and each product is accumulated as hi*hi + hi*lo + lo*hi in FP32,
-// which keeps the flush close to FP32 accuracy; with one term (TF32) the products
-// carry the 2^-11 relative error of TF32.
+// lo = x - hi, and each product is accumulated as hi*hi + hi*lo + lo*hi, which keeps
+// the flush close to FP32 accuracy; the first product's K chunks are summed in FP32
+// outside the tensor core.  With one term (TF32) the products carry the 2^-11
+// relative error of TF32.
 //
 // Every wait on an mbarrier is bounded; on timeout the CTA records an error in
 // *err, skips its epilogue, frees its TMEM and returns.
@@ -308,6 +309,13 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
     if (TERMS > 1)
       *reinterpret_cast<float4*>(sm + lo_base + off) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
   };
+  // with split precision the K chunks are summed here in FP32 (round to nearest), each
+  // chunk's MMA starting from zero: the tensor core's own FP32 accumulation over all of
+  // K = n would add an error growing with n
+  float t1[32];
+#pragma unroll
+  for (int q = 0; q < 32; q++)
+    t1[q] = 0.f;
   load_chunk(0);
   for (int ch = 0; ch < nchunks && ok; ch++)
   {
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
       for (int ks = 0; ks < P.kc / 8; ks++)
       {
         const uint32_t adv = ks * 256; // two core matrices along K per k-step of 8
-        const int first    = (ch == 0 && ks == 0);
+        const int first    = TERMS > 1 ? (ks == 0) : (ch == 0 && ks == 0);
         mma_tf32(d1, smem_desc(ah + adv, P.kc), smem_desc(bh + adv, P.kc), idesc, first ? 0 : 1);
         if (TERMS > 1)
         {
@@ -349,17 +357,32 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
     if (ch + 1 < nchunks)
       load_chunk(ch + 1);
     ok = wait_mma();
+    if (TERMS > 1 && ok)
+    {
+      float t[32];
+      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16), t);
+#pragma unroll
+      for (int q = 0; q < 32; q++)
+        t1[q] += t[q];
+    }
   }
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 
   const int r = warp * 32 + lane; // this thread's TMEM lane = block row
   if (ok)
   {
-    // ---------------- T1 - E from TMEM into the A tile of the second product
+    // ---------------- T1 - E into the A tile of the second product (k1 = 32)
     for (int c0 = 0; c0 < k1; c0 += 32)
     {
       float t[32];
-      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+      if (TERMS > 1)
+      {
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+          t[q] = t1[q];
+      }
+      else
+        tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
 #pragma unroll
       for (int q = 0; q < 32; q++)
       {
@@ -540,7 +563,12 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
   auto slot_col = [](int e) { return ((e >> 3) % (TT_KC / 4)) * 4; };
   bool ok = true;
 
-  // ---------------- T1 = Ainv[rows] U^T over K = n in chunks of KC
+  // ---------------- T1 = Ainv[rows] U^T over K = n in chunks of KC; with split
+  // precision the chunks are summed in FP32 here (round to nearest)
+  float t1[KM];
+#pragma unroll
+  for (int q = 0; q < KM; q++)
+    t1[q] = 0.f;
   constexpr int AV = TC_M * (TT_KC / 4) / TC_NT; // 8 float4 per thread
   const int ub = k1 * (TT_KC / 4);
   for (int k0 = 0; k0 < n && ok; k0 += TT_KC)
@@ -573,7 +601,8 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
       for (int ks = 0; ks < TT_KC / 8; ks++)
       {
         const uint32_t adv = ks * 256;
-        mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, (k0 == 0 && ks == 0) ? 0 : 1);
+        const int first    = TERMS > 1 ? (ks == 0) : (k0 == 0 && ks == 0);
+        mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, first ? 0 : 1);
         if (TERMS > 1)
         {
           mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bl + adv, TT_KC), id, 1);
@@ -583,16 +612,39 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
       mma_commit(bar);
     }
     ok = wait_mma();
+    if (TERMS > 1 && ok)
+    {
+#pragma unroll
+      for (int c0 = 0; c0 < KM; c0 += 32)
+        if (c0 < k1)
+        {
+          float t[32];
+          tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+#pragma unroll
+          for (int q = 0; q < 32; q++)
+            t1[c0 + q] += t[q];
+        }
+    }
   }
 
-  // ---------------- (T1 - E) from TMEM into the A operand of X = (T1 - E) Binv
+  // ---------------- (T1 - E) into the A operand of X = (T1 - E) Binv
   const int r = warp * 32 + lane;
   if (ok)
   {
-    for (int c0 = 0; c0 < k1; c0 += 32)
+#pragma unroll
+    for (int c0 = 0; c0 < KM; c0 += 32)
     {
+      if (c0 >= k1)
+        break;
       float t[32];
-      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+      if (TERMS > 1)
+      {
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+          t[q] = t1[c0 + q];
+      }
+      else
+        tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
 #pragma unroll
       for (int q = 0; q < 32; q += 4)
         if (c0 + q < k1)
