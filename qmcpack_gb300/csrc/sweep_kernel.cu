@@ -146,7 +146,8 @@ struct SweepShared
   T posT[3]; // the proposed position in the move-loop precision
   T ru[3];   // its fractional coordinates (spline_frac)
   T disp[3];
-  T gauss[3];
+  T rgauss[32][3]; // Gaussians of the proposals of a block of 32 electrons
+  T runif[32];     // uniforms of their acceptance tests
   T loggf;
   int acc;
   T det;
@@ -205,8 +206,27 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       T* arow       = pre + ((iat - i0) & 1) * 5 * lda; // this electron's prefetched rows
       const T* dg   = arow + lda;
       const T* pv0  = arow + 4 * lda;
-      if (threadIdx.x == 32)
-        gaussians<T>((uint32_t)w, (uint32_t)iat, sweep, k0, k1, sh.gauss);
+      // the random numbers of the next 32 electrons, one electron per thread (counter-based:
+      // the same values the single-electron calls would draw)
+      const int jj = (iat - i0) & 31;
+      if (jj == 0 && threadIdx.x < 32 && iat + threadIdx.x < i1)
+      {
+        const uint32_t e = (uint32_t)(iat + threadIdx.x);
+        gaussians<T>((uint32_t)w, e, sweep, k0, k1, sh.rgauss[threadIdx.x]);
+        const u4 r2            = philox4x32_10(u4{(uint32_t)w, e, sweep, 2u}, k0, k1);
+        sh.runif[threadIdx.x]  = T(u01(r2.x, r2.y));
+      }
+      // thread 0's operands of the proposal and the decision, loaded ahead of their use
+      double r_now[3] = {0, 0, 0};
+      T j1_now[4]     = {0, 0, 0, 0}; // Vat, Grad xyz of this electron
+      if (threadIdx.x == 0)
+      {
+        for (int d = 0; d < 3; d++)
+          r_now[d] = s.R[((size_t)w * 3 + d) * s.ne_pad + iat];
+        if (s.has_j1)
+          for (int q = 0; q < 4; q++)
+            j1_now[q] = s.J1[((size_t)w * 5 + q) * s.ne_pad + iat];
+      }
       async_wait_all();
       __syncthreads();
       // ------------------------------------------------ up-to-date inverse row, fused with
@@ -282,7 +302,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
             {
               T gs = g[d];
               if (s.has_j1)
-                gs += s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat];
+                gs += j1_now[1 + d];
               if (s.has_j2)
                 gs += J2s[(1 + d) * s.ne_pad + iat];
               sh.lsm.g[d] = gs;
@@ -304,10 +324,10 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
               const T mu = T(clampf(sh.lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
               const T sd = T(clampf(sh.lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
               sum_s += sd;
-              x2 += sh.gauss[d] * sh.gauss[d];
-              const T dd = drift[d] + st * mu + st * exp(sd) * sh.gauss[d];
+              x2 += sh.rgauss[jj][d] * sh.rgauss[jj][d];
+              const T dd = drift[d] + st * mu + st * exp(sd) * sh.rgauss[jj][d];
               sh.disp[d]  = dd;
-              sh.pos[d]   = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(dd);
+              sh.pos[d]   = r_now[d] + static_cast<double>(dd);
               sh.posT[d]  = static_cast<T>(sh.pos[d]);
             }
             spline_frac(s, sh.pos, sh.ru);
@@ -326,7 +346,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           {
             T gs = g[d];
             if (s.has_j1)
-              gs += s.J1[((size_t)w * 5 + 1 + d) * s.ne_pad + iat];
+              gs += j1_now[1 + d];
             if (s.has_j2)
               gs += J2s[(1 + d) * s.ne_pad + iat];
             gn[d] = gs;
@@ -334,7 +354,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           const T sqrttau = sqrt(tau);
           T delta[3], drift[3];
           for (int d = 0; d < 3; d++)
-            delta[d] = sh.gauss[d] * sqrttau;
+            delta[d] = sh.rgauss[jj][d] * sqrttau;
           if (s.use_drift)
           {
             unr_drift_t(tau, gn, drift);
@@ -347,7 +367,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           for (int d = 0; d < 3; d++)
           {
             sh.disp[d] = drift[d];
-            sh.pos[d]  = s.R[((size_t)w * 3 + d) * s.ne_pad + iat] + static_cast<double>(drift[d]);
+            sh.pos[d]  = r_now[d] + static_cast<double>(drift[d]);
             sh.posT[d] = static_cast<T>(sh.pos[d]);
           }
           spline_frac(s, sh.pos, sh.ru);
@@ -434,7 +454,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         T logj       = T(0);
         if (s.has_j1)
         {
-          logj += s.J1[((size_t)w * 5) * s.ne_pad + iat] - acc[10];
+          logj += j1_now[0] - acc[10];
           g[0] += acc[11];
           g[1] += acc[12];
           g[2] += acc[13];
@@ -481,8 +501,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         int a = 0;
         if (p >= Eps<T>::v)
         {
-          const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
-          a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - sh.loggf) ? 1 : 0;
+          a = sh.runif[jj] < p * exp(log_gb - sh.loggf) ? 1 : 0;
         }
         if (a)
         {
@@ -526,8 +545,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           int a          = 0;
           if (p >= Eps<T>::v)
           {
-            const u4 r2 = philox4x32_10(u4{(uint32_t)w, (uint32_t)iat, sweep, 2u}, k0, k1);
-            a           = T(u01(r2.x, r2.y)) < p * exp(log_gb - sh.loggf) ? 1 : 0;
+            a = sh.runif[jj] < p * exp(log_gb - sh.loggf) ? 1 : 0;
           }
           if (a)
           {
