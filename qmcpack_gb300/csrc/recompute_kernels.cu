@@ -634,6 +634,204 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
   cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
 }
 
+// ---------------------------------------------------------------------------
+// Gauss-Jordan inverse with partial pivoting (FP32 elimination, FP64 log|det| sums) of
+// one n x n matrix held in registers, n <= min(TY * NAR, 16 * NB): thread (ty, tx) of a
+// TY x 16 block owns rows ty + TY a (a < NAR) and columns tx + 16 b (b < NB).  Per pivot step the column
+// and the two interchanged rows pass through shared memory and every thread applies
+// the rank-1 elimination to its own elements.  For the repair of small determinants
+// (FP32 crowds), where a cluster's barrier would be the latency of every step.
+// ---------------------------------------------------------------------------
+template<typename T, int TY, int NAR, int NB>
+__global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const double* Mt, int masked)
+{
+  const int slot = blockIdx.x;
+  if (skip_slot(s, slot, masked))
+    return;
+  constexpr int NMAX = 16 * NB > TY * NAR ? 16 * NB : TY * NAR;
+  // rows and columns beyond n hold zeros throughout (their factors and pivot-row
+  // entries are zero), so the staging below needs no bounds checks
+  __shared__ float colk[NMAX]; // column k before the interchange
+  __shared__ float rowk[NMAX]; // row k before the interchange
+  __shared__ float rowp[NMAX]; // the pivot row before the interchange
+  __shared__ int perm[NMAX];   // pivot row of every step
+  __shared__ int cinv[NMAX];   // output column of every working column
+  __shared__ int s_p;
+  const int n = s.norb, tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, lane = tid & 31;
+  const double* M = Mt + (size_t)slot * n * n;
+  float a[NAR][NB];
+#pragma unroll
+  for (int ia = 0; ia < NAR; ia++)
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int i = ty + TY * ia, j = tx + 16 * ib;
+      a[ia][ib]   = (i < n && j < n) ? static_cast<float>(M[(size_t)i * n + j]) : 0.f;
+    }
+  double logabs = 0.0;
+  int sgn = 1, bad = 0;
+  for (int k = 0; k < n; k++)
+  {
+    const int kt = k & 15, kb = k >> 4;       // owners of column k
+    const int kr = k % TY, ka = k / TY;       // owners of row k
+    if (tx == kt)
+#pragma unroll
+      for (int c = 0; c < NB; c++)
+        if (c == kb)
+#pragma unroll
+          for (int ia = 0; ia < NAR; ia++)
+            colk[ty + TY * ia] = a[ia][c];
+    __syncthreads();
+    if (tid < 32)
+    {
+      float bv = -1.f;
+      int bi   = n;
+      for (int i = k + lane; i < n; i += 32)
+      {
+        const float v = fabsf(colk[i]);
+        if (v > bv || (v == bv && i < bi))
+        {
+          bv = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi   = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi))
+        {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0)
+      {
+        s_p     = bv > 0.f ? bi : -1;
+        perm[k] = bi;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p < 0)
+    {
+      bad = 1;
+      break;
+    }
+    const float d = colk[p];
+    logabs += log(fabs(static_cast<double>(d)));
+    if (d < 0.f)
+      sgn = -sgn;
+    if (p != k)
+      sgn = -sgn;
+    const int pr = p % TY, pa = p / TY;       // owners of row p
+    if (ty == kr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == ka)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            rowk[tx + 16 * ib] = a[c][ib];
+    if (ty == pr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == pa)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            rowp[tx + 16 * ib] = a[c][ib];
+    __syncthreads();
+    // new pivot row rk = (old row p with 1 at column k) / d; factors f = column k after
+    // the interchange, 0 at row k
+    const float rinv = 1.f / d;
+    float rk[NB], f[NAR];
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int j = tx + 16 * ib;
+      rk[ib]      = j < n ? (j == k ? 1.f : rowp[j]) * rinv : 0.f;
+    }
+#pragma unroll
+    for (int ia = 0; ia < NAR; ia++)
+    {
+      const int i = ty + TY * ia;
+      f[ia]       = (i < n && i != k) ? colk[i == p ? k : i] : 0.f;
+    }
+    // the interchange: row p takes row k's old values
+    if (ty == pr && p != k)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == pa)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            a[c][ib] = rowk[tx + 16 * ib];
+    // elimination of every element, then row k and column k set to their new values
+#pragma unroll
+    for (int ia = 0; ia < NAR; ia++)
+#pragma unroll
+      for (int ib = 0; ib < NB; ib++)
+        a[ia][ib] = fmaf(-f[ia], rk[ib], a[ia][ib]);
+    if (tx == kt)
+#pragma unroll
+      for (int c = 0; c < NB; c++)
+        if (c == kb)
+#pragma unroll
+          for (int ia = 0; ia < NAR; ia++)
+            a[ia][c] = -f[ia] * rinv;
+    if (ty == kr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == ka)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            a[c][ib] = rk[ib];
+    __syncthreads(); // colk, rowk, rowp are rewritten by the next step
+  }
+  if (bad)
+  {
+    if (tid == 0)
+    {
+      atomicOr(s.status + (slot % s.nw), ST_SINGULAR);
+      s.log_abs[slot] = -INFINITY;
+      s.sign[slot]    = 0;
+    }
+    return;
+  }
+  // the row interchanges become column interchanges applied in reverse order: output
+  // column c holds working column cmap[c]; cinv is its inverse
+  if (tid == 0)
+  {
+    int* cmap = reinterpret_cast<int*>(rowk); // rowk is free now (same size as an int array)
+    for (int j = 0; j < n; j++)
+      cmap[j] = j;
+    for (int k = n - 1; k >= 0; k--)
+    {
+      const int p = perm[k];
+      const int t = cmap[k];
+      cmap[k]     = cmap[p];
+      cmap[p]     = t;
+    }
+    for (int c = 0; c < n; c++)
+      cinv[cmap[c]] = c;
+  }
+  __syncthreads();
+  T* A = s.Ainv + (size_t)slot * n * s.lda;
+#pragma unroll
+  for (int ia = 0; ia < NAR; ia++)
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int i = ty + TY * ia, j = tx + 16 * ib;
+      if (i < n && j < n)
+        A[(size_t)i * s.lda + cinv[j]] = static_cast<T>(a[ia][ib]);
+    }
+  if (tid == 0)
+  {
+    s.log_abs[slot] = logabs;
+    s.sign[slot]    = sgn;
+  }
+}
+
 // grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
 // Vat, Grad, Lap over the ions.
 template<typename T, int NT>
@@ -754,7 +952,21 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
     bool done = false;
     if constexpr (std::is_same<T, float>::value)
     {
-      if (gj_smem_bytes(n, 8, 4) <= GJ_SMEM_MAX)
+      if (n <= 192)
+      {
+        // register-resident, one CTA per matrix
+        if (n <= 32)
+          gj_reg_kernel<float, 16, 2, 2><<<2 * s.nw, 256, 0, st>>>(s, Mt, masked);
+        else if (n <= 64)
+          gj_reg_kernel<float, 16, 4, 4><<<2 * s.nw, 256, 0, st>>>(s, Mt, masked);
+        else if (n <= 128)
+          gj_reg_kernel<float, 32, 4, 8><<<2 * s.nw, 512, 0, st>>>(s, Mt, masked);
+        else
+          gj_reg_kernel<float, 24, 8, 12><<<2 * s.nw, 384, 0, st>>>(s, Mt, masked);
+        e    = cudaGetLastError();
+        done = true;
+      }
+      else if (gj_smem_bytes(n, 8, 4) <= GJ_SMEM_MAX)
       {
         with_cluster(8, gj_smem_bytes(n, 8, 4));
         e    = cudaLaunchKernelEx(&cfg, gj_cluster_smem_kernel<float, float, 8>, s, Mt, masked);
