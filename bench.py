@@ -72,7 +72,7 @@ def bytes_per_walker_move(system, k: int, with_flush: bool = True) -> int:
 def launches_per_sweep(system, k: int) -> int:
     """Kernels per sweep on the walker-resident path: one resident launch and one batched
     flush per segment of up to k electrons of a spin group (one resident launch for the
-    sweep with rank-1 updates), the masked FP64 repair (vgl_all, gj_inverse, jastrow_full,
+    sweep with rank-1 updates), the masked repair (vgl_all, Gauss-Jordan, jastrow_full,
     finish_repair) and the counter bump."""
     if k > 1:
         segs = 2 * ((system.spec.n_up + k - 1) // k)

@@ -6,12 +6,12 @@ FP32 tolerance, runs are deterministic for a seed, and no walker reports a statu
 
 From a uniform (non-equilibrated) start a few walkers sit close to a node where
 the FP32 inverse loses accuracy; the sweep's health check (|Ainv[row].phi - 1| >
-1e-2) flags the ones whose inverse broke down and the masked FP64 recompute
+1e-2) flags the ones whose inverse broke down and the masked recompute
 rebuilds them.  FP32 contract checked here, after 2 sweeps from that start:
 median |log psi tracked - fresh| < 1e-3 and every walker < 1e-3 x |log psi|
 (0.27 for log psi ~ 270); inverses: median walker within 1e-3 of its largest
 element, every walker within 2e-2 (a walker's inverse may drift up to the health
-threshold before the check sends it to the FP64 repair).
+threshold before the check sends it to the repair).
 """
 import numpy as np
 import pytest
