@@ -614,13 +614,14 @@ struct Crowd
     }
   }
 
-  // SplineR2R::convertPos (SplineR2R.h:156-169) for an orthorhombic cell
-  // (PrimLattice.toUnit is a per-axis scaling); the Gamma-point sign is +1.
+  // SplineR2R::convertPos (SplineR2R.h:156-169) for an orthorhombic cell:
+  // PrimLattice.toUnit is r . G (CrystalLattice.h:182-185) with G = R^-1, a per-axis
+  // product with 1/L here; the Gamma-point sign is +1.
   void convert_pos(const double r[3], T ru[3]) const
   {
     for (int d = 0; d < 3; d++)
     {
-      T u = static_cast<T>(r[d] / lattice[d]);
+      T u = static_cast<T>(r[d] * (1.0 / lattice[d]));
       if (-std::numeric_limits<T>::epsilon() < u && u < 0)
         u = T(0);
       else

@@ -505,7 +505,13 @@ struct Crowd final : qmcg_crowd_s
     d.ys        = (long long)(sys->grid[2] + 3) * d.zs;
     d.xs        = (long long)(sys->grid[1] + 3) * d.ys;
     for (int q = 0; q < 3; q++)
+    {
       d.L[q] = sys->L[q];
+      d.G[q] = 1.0 / sys->L[q];
+    }
+    d.grid_scale[0] = static_cast<T>(sys->grid[0] / sys->L[0]);
+    d.grid_scale[1] = static_cast<T>(sys->grid[1] / sys->L[1]);
+    d.grid_scale[2] = static_cast<T>(sys->grid[2] / sys->L[2]);
     d.ions        = static_cast<const T*>(sys->ions);
     d.ion_species = sys->ion_species;
     d.j1c         = static_cast<const T*>(sys->j1c);

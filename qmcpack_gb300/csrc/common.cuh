@@ -58,6 +58,8 @@ struct DevState
   int gx, gy, gz;
   long long xs, ys, zs; // element strides of the coefficient table
   double L[3];          // orthorhombic cell lengths
+  double G[3];          // 1 / L: the diagonal of the reciprocal lattice G = R^-1 (CrystalLattice::G)
+  T grid_scale[3];      // g_d / L_d in the move precision: the Cartesian factor of spline derivatives
   const T* ions;        // [3][nions_pad]
   const int* ion_species;
   const T* j1c;         // [n_ion_species][j1_ncoef]

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
   T* pos = reinterpret_cast<T*>(le_smem); // [3][ne], wrapped into the cell
   T* tab = pos + 3 * ne;                   // [LE_CH][3][nm1] complex
   const T Lc[3]   = {T(s.L[0]), T(s.L[1]), T(s.L[2])};
-  const T Li[3]   = {T(1.0 / s.L[0]), T(1.0 / s.L[1]), T(1.0 / s.L[2])};
+  const T Li[3]   = {T(s.G[0]), T(s.G[1]), T(s.G[2])};
 
   for (int i = tid; i < ne; i += LE_NT)
 #pragma unroll

@@ -88,7 +88,7 @@ __device__ __noinline__ void features_cta(const DevState<T>& s, const T* Rs, int
 {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const T L[3]  = {T(s.L[0]), T(s.L[1]), T(s.L[2])};
-  const T Li[3] = {T(1.0 / s.L[0]), T(1.0 / s.L[1]), T(1.0 / s.L[2])};
+  const T Li[3] = {T(s.G[0]), T(s.G[1]), T(s.G[2])};
   if (wid < 2)
   {
     float bd[8];

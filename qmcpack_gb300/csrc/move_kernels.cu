@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(NT) ratio_kernel(DevState<T> s, int iat, int d
     acc[q] = T(0);
   const T x0 = static_cast<T>(pos[0]), y0 = static_cast<T>(pos[1]), z0 = static_cast<T>(pos[2]);
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
-  const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+  const T Li0 = T(s.G[0]), Li1 = T(s.G[1]), Li2 = T(s.G[2]);
   if (s.has_j2)
   {
     const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(NT) accept_kernel(DevState<T> s, int iat, int 
             zn = static_cast<T>(s.active_pos[iw * 3 + 2]);
     const T xo = Rx[iat], yo = Rx[s.ne_pad + iat], zo = Rx[2 * s.ne_pad + iat];
     const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
-    const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+    const T Li0 = T(s.G[0]), Li1 = T(s.G[1]), Li2 = T(s.G[2]);
     for (int j = threadIdx.x; j < s.ne; j += blockDim.x)
     {
       if (j == iat)

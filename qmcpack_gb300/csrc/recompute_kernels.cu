@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int mas
   const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
   const T xi = Rx[i], yi = Rx[s.ne_pad + i], zi = Rx[2 * s.ne_pad + i];
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
-  const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+  const T Li0 = T(s.G[0]), Li1 = T(s.G[1]), Li2 = T(s.G[2]);
   {
     T u = 0, gx = 0, gy = 0, gz = 0, lap = 0;
     if (s.has_j2)

@@ -46,7 +46,7 @@ __device__ __forceinline__ void spline_frac(const DevState<T>& s, const double p
 #pragma unroll
   for (int d = 0; d < 3; d++)
   {
-    T u = static_cast<T>(pos[d] / s.L[d]);
+    T u = static_cast<T>(pos[d] * s.G[d]); // CrystalLattice::toUnit: r . G
     if (-Eps<T>::v < u && u < T(0))
       u = T(0);
     else
@@ -157,7 +157,7 @@ __device__ __forceinline__ void spline_combine(const DevState<T>& s, const T* pa
   for (int q = 0; q < 7; q++)
     r[q] = part[(0 * 7 + q) * s.lda + o] + part[(1 * 7 + q) * s.lda + o] + part[(2 * 7 + q) * s.lda + o] +
         part[(3 * 7 + q) * s.lda + o];
-  const T fx = T(s.gx / s.L[0]), fy = T(s.gy / s.L[1]), fz = T(s.gz / s.L[2]);
+  const T fx = s.grid_scale[0], fy = s.grid_scale[1], fz = s.grid_scale[2];
   out[0] = r[0];
   out[1] = r[1] * fx;
   out[2] = r[2] * fy;

@@ -180,7 +180,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
-  const T Li0 = T(1.0 / s.L[0]), Li1 = T(1.0 / s.L[1]), Li2 = T(1.0 / s.L[2]);
+  const T Li0 = T(s.G[0]), Li1 = T(s.G[1]), Li2 = T(s.G[2]);
   const T tau       = T(s.tau);
   const int spin    = i0 >= s.nup ? 1 : 0;
   const int first   = spin ? s.nup : 0;
