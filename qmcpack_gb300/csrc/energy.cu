@@ -42,6 +42,29 @@ size_t local_energy_smem(int ne, int nmax, int tsize)
   return (size_t)tsize * (3 * (size_t)ne + (size_t)LE_CH * 3 * (nmax + 1) * 2);
 }
 
+// a thread's sum of many terms: compensated (Kahan) in FP32, which keeps the sum to
+// about one rounding of its value without FP64 additions; plain FP64 otherwise
+template<typename T>
+struct CompSum
+{
+  double s = 0;
+  __device__ void add(T x) { s += static_cast<double>(x); }
+  __device__ double get() const { return s; }
+};
+template<>
+struct CompSum<float>
+{
+  float s = 0.f, c = 0.f;
+  __device__ void add(float x)
+  {
+    const float y = x - c;
+    const float t = s + y;
+    c             = (t - s) - y;
+    s             = t;
+  }
+  __device__ double get() const { return static_cast<double>(s) - static_cast<double>(c); }
+};
+
 template<typename T>
 __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, EwaldDev<T> ew, double* out)
 {
@@ -59,12 +82,13 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
     for (int d = 0; d < 3; d++)
     {
       double x = s.R[((size_t)iw * 3 + d) * s.ne_pad + i];
-      x -= s.L[d] * floor(x / s.L[d]);
+      x -= s.L[d] * floor(x * s.G[d]);
       pos[d * ne + i] = static_cast<T>(x);
     }
   __syncthreads();
 
-  double ke = 0, vr = 0, vk = 0;
+  double ke = 0, vk = 0;
+  CompSum<T> vr; // the ~300 pair terms of a thread
   // ---------------- kinetic energy: a warp per electron
   for (int i = warp; i < ne; i += LE_NT / 32)
   {
@@ -82,9 +106,11 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
       gz += av * g[2 * lda + o];
       lp += av * l[o];
     }
-    double G[3] = {warp_sum(static_cast<double>(gx)), warp_sum(static_cast<double>(gy)),
-                   warp_sum(static_cast<double>(gz))};
-    double L    = warp_sum(static_cast<double>(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+    // lane sums in the move precision (FP64 arithmetic is slow on this GPU), the
+    // per-electron combination in FP64
+    double G[3] = {static_cast<double>(warp_sum(gx)), static_cast<double>(warp_sum(gy)),
+                   static_cast<double>(warp_sum(gz))};
+    double L    = static_cast<double>(warp_sum(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
     if (lane == 0)
     {
       if (s.has_j2)
@@ -139,7 +165,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
     }
     const T r = sqrt(r2);
     if (r > T(0) && r < ew.rcut)
-      vr += static_cast<double>(t_erfc(al * r) / r);
+      vr.add(t_erfc(al * r) / r);
   }
   // electron-ion pairs
   for (int p = tid; p < ne * s.nions; p += LE_NT)
@@ -155,7 +181,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
     }
     const T r = sqrt(r2);
     if (r > T(0) && r < ew.rcut)
-      vr -= static_cast<double>(ew.ion_q[I] * t_erfc(al * r) / r);
+      vr.add(-(ew.ion_q[I] * t_erfc(al * r) / r));
   }
 
   // ---------------- reciprocal space
@@ -217,7 +243,7 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
     }
   }
 
-  double v[3] = {ke, vr, vk};
+  double v[3] = {ke, vr.get(), vk};
   block_sum<double, 3>(v, red);
   if (tid == 0)
   {
