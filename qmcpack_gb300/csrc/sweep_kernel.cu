@@ -46,7 +46,8 @@ static size_t sweep_smem_elems(const DevState<T>& s)
       + 8 * (size_t)s.ne_pad   // positions, J2 state
       + (size_t)s.k * s.k      // Binv
       + 3 * (size_t)s.k        // p, t, y
-      + 16 * 32;               // block reductions
+      + 16 * 32                // block reductions
+      + (size_t)s.k * (s.k - 1) / 2; // U_c . Ainv[row_x] of the segment, c < x
 }
 
 // cp.async of n_elems elements (a multiple of 16 bytes) from global to shared
@@ -174,6 +175,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   T* tv     = pv + K;                         // K
   T* yv     = tv + K;                         // K
   T* red    = yv + K;                         // 16 x 32
+  T* tri    = red + 16 * 32;                  // K (K - 1) / 2: entry x (x - 1) / 2 + c = U_c . Ainv[row_x]
   const __nv_bfloat162* ml_pairs = reinterpret_cast<const __nv_bfloat162*>(s.mlp_simt);
   const __nv_bfloat16* ml_w4 = reinterpret_cast<const __nv_bfloat16*>(ml_pairs + MS_NPAIRS);
 
@@ -235,9 +237,12 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       T g[4]       = {0, 0, 0, 0};
       if (K > 1 && dc > 0)
       {
-        const T* U = s.U + slot * K * lda;
         const T* V = s.V + slot * K * lda;
-        rows_dot<T, NT>(U, lda, dc, arow, n, pv, T(1));
+        // U_c . Ainv[row] of the earlier slots of this segment, formed when slot c was
+        // decided (zero for a rejected move)
+        const int base = dc * (dc - 1) / 2;
+        for (int c = threadIdx.x; c < dc; c += NT)
+          pv[c] = tri[base + c];
         __syncthreads();
         for (int i = threadIdx.x; i < dc; i += NT)
         {
@@ -571,17 +576,22 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         int* dlist = s.delay_list + slot * K;
         for (int j = threadIdx.x; j < n; j += NT)
           V[(size_t)dc * lda + j] = arow[j];
+        const int m = i1 - i0; // slots of this segment
         if (accd)
         {
           const T sigma = T(1) / sh.det;
-          rows_dot<T, NT>(V, lda, dc, phi, n, pv, T(-1));
+          // phi . Ainv[row_x] for every electron x of the segment: x < dc are the V_x . phi
+          // of the Binv update (V_x is Ainv[row_x]), x > dc the U . invRow terms of later slots
+          rows_dot<T, NT>(s.Ainv + (slot * n + (i0 - first)) * lda, lda, m, phi, n, pv, T(1));
           __syncthreads();
+          for (int x = dc + 1 + threadIdx.x; x < m; x += NT)
+            tri[x * (x - 1) / 2 + dc] = pv[x];
           for (int i = threadIdx.x; i < dc; i += NT)
           {
             T a = 0;
             for (int c = 0; c < dc; c++)
               a += Bs[i * K + c] * pv[c];
-            yv[i] = sigma * a;
+            yv[i] = -sigma * a;
           }
           __syncthreads();
           for (int e = threadIdx.x; e < dc * dc; e += NT)
@@ -605,6 +615,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         }
         else
         {
+          for (int x = dc + 1 + threadIdx.x; x < m; x += NT)
+            tri[x * (x - 1) / 2 + dc] = T(0);
           for (int j = threadIdx.x; j < n; j += NT)
             U[(size_t)dc * lda + j] = T(0);
           for (int i = threadIdx.x; i < dc; i += NT)
