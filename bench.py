@@ -279,13 +279,14 @@ def effective_samples(args, system, dsys32, seed: int):
     g.proposal_init(seed=seed)
     (_, _, _, tr), t_train = timed(lambda: g.vmc_sweeps_learned(args.train_sweeps, tau, seed + 2, train=True,
                                                                  lr=args.lr, recompute_every=rec, flush=args.flush))
+    params_finite = bool(np.isfinite(g.proposal_params()).all())
     (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_learned(n, tau, seed + 4, measure=True, recompute_every=rec,
                                                            flush=args.flush))
     summarize("learned_fp32", el, dt, n, {
         "acceptance": a / max(a + r, 1),
         "training": {"sweeps": args.train_sweeps, "moves": args.train_sweeps * nw * system.n_elec,
                      "seconds": t_train, "lr": args.lr, "final_mean_alpha_jump2": tr[0],
-                     "final_mean_alpha": tr[1], "final_objective": tr[2],
+                     "final_mean_alpha": tr[1], "final_objective": tr[2], "parameters_finite": params_finite,
                      "data": "configurations of the FP32 drift-diffusion run, continued on-policy"}})
     del g
     p64 = out["plain_fp64"]

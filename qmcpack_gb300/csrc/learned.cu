@@ -405,6 +405,10 @@ __global__ void mlp_loss_grad_kernel(DevState<T> s, const float* __restrict__ au
   const double inv_n = (lam2 * lam2 / (jw * jw) + 1.0) / s.nw;
   float* gf = g4 + (size_t)iw * 8;
   float* gr = g4 + (size_t)(s.nw + iw) * 8;
+  // a walker whose move produced a non-finite value (a proposal at a node of psi gives an
+  // infinite gradient of log psi) contributes nothing: one such value would otherwise
+  // reach every weight through the backward pass and the optimizer
+  bool finite = isfinite(alpha) && isfinite(j2);
 #pragma unroll
   for (int d = 0; d < 3; d++)
   {
@@ -429,8 +433,16 @@ __global__ void mlp_loss_grad_kernel(DevState<T> s, const float* __restrict__ au
     gf[3 + d] = (float)g_s;
     gr[d]     = (float)g_mr;
     gr[3 + d] = (float)g_sr;
+    finite    = finite && isfinite(gf[d]) && isfinite(gf[3 + d]) && isfinite(gr[d]) && isfinite(gr[3 + d]);
   }
   gf[6] = gf[7] = gr[6] = gr[7] = 0.f;
+  if (!finite)
+  {
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+      gf[q] = gr[q] = 0.f;
+    return;
+  }
   atomicAdd(stats, alpha * j2);
   atomicAdd(stats + 1, alpha);
   atomicAdd(stats + 2, lam2 * lam2 / jw - alpha * j2);
@@ -514,7 +526,7 @@ __global__ void mlp_adam_kernel(float* __restrict__ p, float* __restrict__ m, fl
   }
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const int t    = *step + 1;
-  const float gi = g[i];
+  const float gi = isfinite(g[i]) ? g[i] : 0.f; // a non-finite gradient counts as zero
   const float mi = b1 * m[i] + (1.f - b1) * gi;
   const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
   m[i]           = mi;
