@@ -131,13 +131,14 @@ struct LearnedSmem
 template<typename T>
 struct LearnedSmem<T, true>
 {
-  float x[ML_IN];
-  float h[2 * ML_H];
-  float red[ML_NOUT * 4];
-  float out[8];
   T g[3];
   T p;
 };
+// the network's features, activations, reduction scratch and outputs live in the spline
+// partials buffer, which is free while the network runs (before the spline partials of
+// the proposed position are formed, and after they are combined)
+constexpr int ML_SCRATCH_FLOATS = ML_IN + 2 * ML_H + ML_NOUT * 4 + 8;
+static_assert(ML_SCRATCH_FLOATS * 4 <= 28 * 16 * 4, "the network scratch fits the partials of the smallest padding");
 
 // per-CTA scalars of the resident sweep in shared memory
 template<typename T, bool LEARNED>
@@ -178,6 +179,10 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   T* tri    = red + 16 * 32;                  // K (K - 1) / 2: entry x (x - 1) / 2 + c = U_c . Ainv[row_x]
   const __nv_bfloat162* ml_pairs = reinterpret_cast<const __nv_bfloat162*>(s.mlp_simt);
   const __nv_bfloat16* ml_w4 = reinterpret_cast<const __nv_bfloat16*>(ml_pairs + MS_NPAIRS);
+  float* ml_x   = reinterpret_cast<float*>(part); // ML_SCRATCH_FLOATS <= 28 * lda elements of part
+  float* ml_h   = ml_x + ML_IN;
+  float* ml_red = ml_h + 2 * ML_H;
+  float* ml_out = ml_red + ML_NOUT * 4;
 
   const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
@@ -189,6 +194,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   const int lane    = threadIdx.x & 31, wid = threadIdx.x >> 5;
   (void)spare;
   (void)ml_w4;
+  (void)ml_out;
 
   {
     const size_t slot = (size_t)spin * s.nw + w;
@@ -315,9 +321,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           }
           __syncthreads();
           const T pc[3] = {Rs[iat], Rs[s.ne_pad + iat], Rs[2 * s.ne_pad + iat]};
-          features_cta(s, Rs, iat, pc, sh.lsm.g, sh.lsm.x);
+          features_cta(s, Rs, iat, pc, sh.lsm.g, ml_x);
           __syncthreads();
-          mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, sh.lsm.x, sh.lsm.h, sh.lsm.red, sh.lsm.out);
+          mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, ml_x, ml_h, ml_red, ml_out);
           if (threadIdx.x == 0)
           {
             const T st = sqrt(tau);
@@ -326,8 +332,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
             T sum_s = 0, x2 = 0;
             for (int d = 0; d < 3; d++)
             {
-              const T mu = T(clampf(sh.lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
-              const T sd = T(clampf(sh.lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+              const T mu = T(clampf(ml_out[d], -ML_MU_MAX, ML_MU_MAX));
+              const T sd = T(clampf(ml_out[3 + d], ML_S_MIN, ML_S_MAX));
               sum_s += sd;
               x2 += sh.rgauss[jj][d] * sh.rgauss[jj][d];
               const T dd = drift[d] + st * mu + st * exp(sd) * sh.rgauss[jj][d];
@@ -527,9 +533,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       {
         // the network at the proposed position: the reverse density q(r | R')
         const T pn[3] = {sh.posT[0], sh.posT[1], sh.posT[2]};
-        features_cta(s, Rs, iat, pn, sh.lsm.g, sh.lsm.x);
+        features_cta(s, Rs, iat, pn, sh.lsm.g, ml_x);
         __syncthreads();
-        mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, sh.lsm.x, sh.lsm.h, sh.lsm.red, sh.lsm.out);
+        mlp_eval_cta(ml_pairs, ml_w4, s.mlp_params, ml_x, ml_h, ml_red, ml_out);
         if (threadIdx.x == 0)
         {
           const T st = sqrt(tau);
@@ -538,8 +544,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           T sum_s = 0, z2 = 0;
           for (int d = 0; d < 3; d++)
           {
-            const T mu = T(clampf(sh.lsm.out[d], -ML_MU_MAX, ML_MU_MAX));
-            const T sd = T(clampf(sh.lsm.out[3 + d], ML_S_MIN, ML_S_MAX));
+            const T mu = T(clampf(ml_out[d], -ML_MU_MAX, ML_MU_MAX));
+            const T sd = T(clampf(ml_out[3 + d], ML_S_MIN, ML_S_MAX));
             sum_s += sd;
             const T z = (-sh.disp[d] - drift[d] - st * mu) / (st * exp(sd));
             z2 += z * z;
