@@ -339,11 +339,14 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double
       bad = 1;
       break;
     }
-    logabs += log(fabs(d));
-    if (d < 0.0)
-      sgn = -sgn;
-    if (p != k)
-      sgn = -sgn;
+    if (r == 0 && tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
+    {
+      logabs += log(fabs(d));
+      if (d < 0.0)
+        sgn = -sgn;
+      if (p != k)
+        sgn = -sgn;
+    }
     if (p != k)
       for (int j = c0 + tid; j < c1; j += GJ_NT)
       {
@@ -551,11 +554,14 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
       bad = 1;
       break;
     }
-    logabs += log(fabs(dd));
-    if (dd < 0.0)
-      sgn = -sgn;
-    if (p != k)
-      sgn = -sgn;
+    if (r == 0 && tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
+    {
+      logabs += log(fabs(dd));
+      if (dd < 0.0)
+        sgn = -sgn;
+      if (p != k)
+        sgn = -sgn;
+    }
     const W d = static_cast<W>(dd);
     if (p != k)
       for (int jj = tid; jj < ncw; jj += GJ_NT)
@@ -720,11 +726,14 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
       break;
     }
     const float d = colk[p];
-    logabs += log(fabs(static_cast<double>(d)));
-    if (d < 0.f)
-      sgn = -sgn;
-    if (p != k)
-      sgn = -sgn;
+    if (tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
+    {
+      logabs += log(fabs(static_cast<double>(d)));
+      if (d < 0.f)
+        sgn = -sgn;
+      if (p != k)
+        sgn = -sgn;
+    }
     const int pr = p % TY, pa = p / TY;       // owners of row p
     if (ty == kr)
 #pragma unroll
@@ -832,23 +841,24 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
   }
 }
 
-// grid (nw, ceil(ne/NT)): Uat, dUat, d2Uat of electron i over all j != i, and
-// Vat, Grad, Lap over the ions.
+// grid (nw, ceil(ne / (NT / 32))): one warp per electron i, its lanes over the partners;
+// Uat, dUat, d2Uat of electron i over all j != i, and Vat, Grad, Lap over the ions.
 template<typename T, int NT>
 __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int masked)
 {
-  const int iw = blockIdx.x;
-  const int i  = blockIdx.y * NT + threadIdx.x;
-  if (i >= s.ne || skip_walker(s, iw, masked))
+  const int iw   = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i    = blockIdx.y * (NT / 32) + (threadIdx.x >> 5);
+  if (i >= s.ne || skip_walker(s, iw, masked)) // uniform over the warp
     return;
   const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
   const T xi = Rx[i], yi = Rx[s.ne_pad + i], zi = Rx[2 * s.ne_pad + i];
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
   const T Li0 = T(s.G[0]), Li1 = T(s.G[1]), Li2 = T(s.G[2]);
   {
-    T u = 0, gx = 0, gy = 0, gz = 0, lap = 0;
+    T v[5] = {0, 0, 0, 0, 0}; // u, grad xyz, lap
     if (s.has_j2)
-      for (int j = 0; j < s.ne; j++)
+      for (int j = lane; j < s.ne; j += 32)
       {
         if (j == i)
           continue;
@@ -860,25 +870,31 @@ __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int mas
         {
           const int same = (j < s.nup) == (i < s.nup);
           T du, d2u;
-          u += functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
+          v[0] += functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
           du *= T(1) / r;
-          gx += du * dx;
-          gy += du * dy;
-          gz += du * dz;
-          lap += d2u + T(2) * du;
+          v[1] += du * dx;
+          v[2] += du * dy;
+          v[3] += du * dz;
+          v[4] += d2u + T(2) * du;
         }
       }
-    T* J2 = s.J2 + (size_t)iw * 5 * s.ne_pad;
-    J2[i]                = u;
-    J2[s.ne_pad + i]     = gx;
-    J2[2 * s.ne_pad + i] = gy;
-    J2[3 * s.ne_pad + i] = gz;
-    J2[4 * s.ne_pad + i] = -lap;
+#pragma unroll
+    for (int q = 0; q < 5; q++)
+      v[q] = warp_sum(v[q]);
+    if (lane == 0)
+    {
+      T* J2                = s.J2 + (size_t)iw * 5 * s.ne_pad;
+      J2[i]                = v[0];
+      J2[s.ne_pad + i]     = v[1];
+      J2[2 * s.ne_pad + i] = v[2];
+      J2[3 * s.ne_pad + i] = v[3];
+      J2[4 * s.ne_pad + i] = -v[4];
+    }
   }
   {
-    T u = 0, gx = 0, gy = 0, gz = 0, lap = 0;
+    T v[5] = {0, 0, 0, 0, 0};
     if (s.has_j1)
-      for (int j = 0; j < s.nions; j++)
+      for (int j = lane; j < s.nions; j += 32)
       {
         const T dx = min_image(s.ions[j] - xi, L0, Li0);
         const T dy = min_image(s.ions[s.nions_pad + j] - yi, L1, Li1);
@@ -887,20 +903,26 @@ __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int mas
         if (r < s.j1_rcut)
         {
           T du, d2u;
-          u += functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
+          v[0] += functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
           du *= T(1) / r;
-          gx += du * dx;
-          gy += du * dy;
-          gz += du * dz;
-          lap += d2u + T(2) * du;
+          v[1] += du * dx;
+          v[2] += du * dy;
+          v[3] += du * dz;
+          v[4] += d2u + T(2) * du;
         }
       }
-    T* J1 = s.J1 + (size_t)iw * 5 * s.ne_pad;
-    J1[i]                = u;
-    J1[s.ne_pad + i]     = gx;
-    J1[2 * s.ne_pad + i] = gy;
-    J1[3 * s.ne_pad + i] = gz;
-    J1[4 * s.ne_pad + i] = lap;
+#pragma unroll
+    for (int q = 0; q < 5; q++)
+      v[q] = warp_sum(v[q]);
+    if (lane == 0)
+    {
+      T* J1                = s.J1 + (size_t)iw * 5 * s.ne_pad;
+      J1[i]                = v[0];
+      J1[s.ne_pad + i]     = v[1];
+      J1[2 * s.ne_pad + i] = v[2];
+      J1[3 * s.ne_pad + i] = v[3];
+      J1[4 * s.ne_pad + i] = v[4];
+    }
   }
 }
 
@@ -999,7 +1021,7 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
   }
   if (e != cudaSuccess)
     return e;
-  dim3 grid(s.nw, (s.ne + 127) / 128);
+  dim3 grid(s.nw, (s.ne + 3) / 4);
   jastrow_full_kernel<T, 128><<<grid, 128, 0, st>>>(s, masked);
   e = cudaGetLastError();
   if (e != cudaSuccess || !masked)
