@@ -18,6 +18,22 @@
 namespace qmcg
 {
 
+// log|det| as the product of the pivots kept as an FP64 mantissa and a binary exponent:
+// one multiply per pivot and one log at the end, instead of a log per pivot (FP64
+// transcendentals are slow on this GPU and sit on the elimination's critical path)
+struct LogAbsProduct
+{
+  double m = 1.0;
+  int e    = 0;
+  __device__ void mul(double x)
+  {
+    int ex;
+    m = frexp(m * fabs(x), &ex);
+    e += ex;
+  }
+  __device__ double value() const { return log(m) + e * 0.69314718055994530942; }
+};
+
 // A walker takes part in a masked (repair) recompute only if its status has a
 // repair bit; an unmasked recompute takes every walker.
 template<typename T>
@@ -98,7 +114,7 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
   const int slot = blockIdx.x;
   double* a      = Mt + (size_t)slot * n * n;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double logabs = 0.0;
+  LogAbsProduct logabs;
   int sgn       = 1;
   if (threadIdx.x == 0)
     s_bad = 0;
@@ -175,7 +191,7 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
       pcol[i] = (i == k) ? 0.0 : a[(size_t)i * n + k];
     if (threadIdx.x == 0)
     {
-      logabs += log(fabs(d));
+      logabs.mul(d);
       if (d < 0.0)
         sgn = -sgn;
       if (p != k)
@@ -224,7 +240,7 @@ __global__ void __launch_bounds__(NT) gj_inverse_kernel(DevState<T> s, double* M
   }
   if (threadIdx.x == 0)
   {
-    s.log_abs[iw_spin] = logabs;
+    s.log_abs[iw_spin] = logabs.value();
     s.sign[iw_spin]    = sgn;
   }
 }
@@ -273,7 +289,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double
   double* pdv = scr + 2 * (size_t)n;                  // [2][2] pivot row, pivot value
   int* perm   = reinterpret_cast<int*>(scr + 2 * (size_t)n + 4);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  double logabs = 0.0;
+  LogAbsProduct logabs;
   int sgn = 1, bad = 0;
   for (int k = 0; k < n; k++)
   {
@@ -341,7 +357,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double
     }
     if (r == 0 && tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
     {
-      logabs += log(fabs(d));
+      logabs.mul(d);
       if (d < 0.0)
         sgn = -sgn;
       if (p != k)
@@ -409,7 +425,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_kernel(DevState<T> s, double
       A[(size_t)i * s.lda + c0 + jj] = static_cast<T>(__ldcg(a + (size_t)i * n + cmap[c0 + jj]));
   if (r == 0 && tid == 0)
   {
-    s.log_abs[slot] = logabs;
+    s.log_abs[slot] = logabs.value();
     s.sign[slot]    = sgn;
   }
 }
@@ -486,7 +502,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
     for (int jj = lane; jj < ncw; jj += 32)
       blk[(size_t)i * ld + jj] = static_cast<W>(a[(size_t)i * n + c0 + jj]);
   __syncthreads();
-  double logabs = 0.0;
+  LogAbsProduct logabs;
   int sgn = 1, bad = 0;
   for (int k = 0; k < n; k++)
   {
@@ -556,7 +572,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
     }
     if (r == 0 && tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
     {
-      logabs += log(fabs(dd));
+      logabs.mul(dd);
       if (dd < 0.0)
         sgn = -sgn;
       if (p != k)
@@ -634,7 +650,7 @@ __global__ void __launch_bounds__(GJ_NT) gj_cluster_smem_kernel(DevState<T> s, d
       A[(size_t)i * s.lda + c0 + jj] = static_cast<T>(__ldcg(a + (size_t)i * n + cmap[c0 + jj]));
   if (r == 0 && tid == 0)
   {
-    s.log_abs[slot] = logabs;
+    s.log_abs[slot] = logabs.value();
     s.sign[slot]    = sgn;
   }
   cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
@@ -657,12 +673,12 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
   constexpr int NMAX = 16 * NB > TY * NAR ? 16 * NB : TY * NAR;
   // rows and columns beyond n hold zeros throughout (their factors and pivot-row
   // entries are zero), so the staging below needs no bounds checks
-  __shared__ float colk[NMAX]; // column k before the interchange
-  __shared__ float rowk[NMAX]; // row k before the interchange
-  __shared__ float rowp[NMAX]; // the pivot row before the interchange
-  __shared__ int perm[NMAX];   // pivot row of every step
-  __shared__ int cinv[NMAX];   // output column of every working column
-  __shared__ int s_p;
+  __shared__ float colk[2][NMAX]; // column k before the interchange (double-buffered: the
+                                  // owners of column k + 1 write it during step k)
+  __shared__ float rowk[NMAX];    // row k before the interchange
+  __shared__ float rowp[NMAX];    // the pivot row before the interchange
+  __shared__ int perm[NMAX];      // pivot row of every step
+  __shared__ int cinv[NMAX];      // output column of every working column
   const int n = s.norb, tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, lane = tid & 31;
   const double* M = Mt + (size_t)slot * n * n;
   float a[NAR][NB];
@@ -674,61 +690,53 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
       const int i = ty + TY * ia, j = tx + 16 * ib;
       a[ia][ib]   = (i < n && j < n) ? static_cast<float>(M[(size_t)i * n + j]) : 0.f;
     }
-  double logabs = 0.0;
+  if (tx == 0)
+#pragma unroll
+    for (int ia = 0; ia < NAR; ia++)
+      colk[0][ty + TY * ia] = a[ia][0];
+  __syncthreads();
+  LogAbsProduct logabs;
   int sgn = 1, bad = 0;
   for (int k = 0; k < n; k++)
   {
+    const float* ck = colk[k & 1];
     const int kt = k & 15, kb = k >> 4;       // owners of column k
     const int kr = k % TY, ka = k / TY;       // owners of row k
-    if (tx == kt)
-#pragma unroll
-      for (int c = 0; c < NB; c++)
-        if (c == kb)
-#pragma unroll
-          for (int ia = 0; ia < NAR; ia++)
-            colk[ty + TY * ia] = a[ia][c];
-    __syncthreads();
-    if (tid < 32)
+    // every warp finds the pivot (same result, no broadcast)
+    float bv = -1.f;
+    int bi   = n;
+    for (int i = k + lane; i < n; i += 32)
     {
-      float bv = -1.f;
-      int bi   = n;
-      for (int i = k + lane; i < n; i += 32)
+      const float v = fabsf(ck[i]);
+      if (v > bv || (v == bv && i < bi))
       {
-        const float v = fabsf(colk[i]);
-        if (v > bv || (v == bv && i < bi))
-        {
-          bv = v;
-          bi = i;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-      {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi   = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > bv || (ov == bv && oi < bi))
-        {
-          bv = ov;
-          bi = oi;
-        }
-      }
-      if (lane == 0)
-      {
-        s_p     = bv > 0.f ? bi : -1;
-        perm[k] = bi;
+        bv = v;
+        bi = i;
       }
     }
-    __syncthreads();
-    const int p = s_p;
-    if (p < 0)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi   = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi))
+      {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (!(bv > 0.f))
     {
       bad = 1;
       break;
     }
-    const float d = colk[p];
+    const int p = bi;
+    if (tid == 0)
+      perm[k] = p;
+    const float d = ck[p];
     if (tid == 0) // the one thread that writes log|det| (FP64 log is slow on this GPU)
     {
-      logabs += log(fabs(static_cast<double>(d)));
+      logabs.mul(static_cast<double>(d));
       if (d < 0.f)
         sgn = -sgn;
       if (p != k)
@@ -764,7 +772,7 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
     for (int ia = 0; ia < NAR; ia++)
     {
       const int i = ty + TY * ia;
-      f[ia]       = (i < n && i != k) ? colk[i == p ? k : i] : 0.f;
+      f[ia]       = (i < n && i != k) ? ck[i == p ? k : i] : 0.f;
     }
     // the interchange: row p takes row k's old values
     if (ty == pr && p != k)
@@ -794,7 +802,16 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
 #pragma unroll
           for (int ib = 0; ib < NB; ib++)
             a[c][ib] = rk[ib];
-    __syncthreads(); // colk, rowk, rowp are rewritten by the next step
+    // column k + 1 for the next step's pivot search, by its owners
+    const int k1 = k + 1, k1t = k1 & 15, k1b = k1 >> 4;
+    if (k1 < n && tx == k1t)
+#pragma unroll
+      for (int c = 0; c < NB; c++)
+        if (c == k1b)
+#pragma unroll
+          for (int ia = 0; ia < NAR; ia++)
+            colk[k1 & 1][ty + TY * ia] = a[ia][c];
+    __syncthreads(); // rowk, rowp and the other column buffer are rewritten by the next step
   }
   if (bad)
   {
@@ -836,7 +853,7 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
     }
   if (tid == 0)
   {
-    s.log_abs[slot] = logabs;
+    s.log_abs[slot] = logabs.value();
     s.sign[slot]    = sgn;
   }
 }
