@@ -564,6 +564,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.sweep_counter, 1));
     CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
     CUDA_TRY(mem.alloc(&d.gj_scratch, 2 * (size_t)nw * gj_scratch_doubles((int)N)));
+    CUDA_TRY(mem.alloc(&d.repair_list, (size_t)nw + 1));
     CUDA_TRY(mem.alloc(&W, (size_t)nw * k * lda));
     const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
     CUDA_TRY(mem.alloc(&gauss_d, ng));

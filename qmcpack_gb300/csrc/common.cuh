@@ -111,6 +111,7 @@ struct DevState
   double tau;
   int use_drift;
   double* gj_scratch;  // [2 nw][3 N + 8] pivot broadcast of the cluster Gauss-Jordan repair
+  int* repair_list;     // [1 + nw]: count, then the walkers with a repair bit (masked recompute)
   // learned proposal (walker-resident path): SIMT weight image and FP32 master parameters
   const void* mlp_simt;
   const float* mlp_params;

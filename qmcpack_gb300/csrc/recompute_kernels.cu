@@ -9,6 +9,7 @@
 // mixed-precision move loop.  The inverse is a Gauss-Jordan elimination with
 // partial pivoting (same pivots as LU with partial pivoting), one CTA per matrix,
 // in FP64 whatever the move-loop precision.
+#include <algorithm>
 #include <type_traits>
 
 #include "common.cuh"
@@ -52,19 +53,21 @@ __device__ __forceinline__ bool skip_slot(const DevState<T>& s, int slot, int ma
 
 constexpr int VGL_EPB = 8; // electrons per CTA of the all-electron VGL
 
-// grid (nw * ceil(ne / VGL_EPB)): orbital VGL of VGL_EPB electrons of walker iw into
-// the FP64 Slater matrix (stored transposed: Mt[slot][o][row]) and the psiv / dgrad /
-// dlap rows.
+// Work items (walker, block of VGL_EPB electrons): orbital VGL of the block into the FP64
+// Slater matrix (stored transposed: Mt[slot][o][row]) and the psiv / dgrad / dlap rows.
+// Unmasked: one item per CTA over every walker.  Masked: the walkers of repair_list,
+// handed to a small grid in strides.
 template<typename T, int NT>
 __global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt, int masked)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* part        = reinterpret_cast<T*>(smem_raw);
-  const int nblk = (s.ne + VGL_EPB - 1) / VGL_EPB;
-  const int iw   = blockIdx.x / nblk;
-  if (skip_walker(s, iw, masked))
-    return;
-  const int e0 = (blockIdx.x % nblk) * VGL_EPB;
+  T* part          = reinterpret_cast<T*>(smem_raw);
+  const int nblk   = (s.ne + VGL_EPB - 1) / VGL_EPB;
+  const int nitems = (masked ? s.repair_list[0] : s.nw) * nblk;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x)
+  {
+  const int iw = masked ? s.repair_list[1 + item / nblk] : item / nblk;
+  const int e0 = (item % nblk) * VGL_EPB;
   for (int e = e0; e < min(e0 + VGL_EPB, s.ne); e++)
   {
   const int spin = e >= s.nup ? 1 : 0;
@@ -93,6 +96,23 @@ __global__ void __launch_bounds__(NT) vgl_all_kernel(DevState<T> s, double* Mt, 
   }
   __syncthreads();
   }
+  }
+}
+
+// the walkers with a repair bit: repair_list[0] = count, repair_list[1..] = walkers (one CTA)
+template<typename T>
+__global__ void __launch_bounds__(1024) repair_list_kernel(DevState<T> s)
+{
+  __shared__ int cnt;
+  if (threadIdx.x == 0)
+    cnt = 0;
+  __syncthreads();
+  for (int iw = threadIdx.x; iw < s.nw; iw += blockDim.x)
+    if (s.status[iw] & ST_REPAIR_MASK)
+      s.repair_list[1 + atomicAdd(&cnt, 1)] = iw;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    s.repair_list[0] = cnt;
 }
 
 // grid (2 * nw): in-place FP64 Gauss-Jordan inverse of Mt[slot] (n x n), log|det|
@@ -858,16 +878,22 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
   }
 }
 
-// grid (nw, ceil(ne / (NT / 32))): one warp per electron i, its lanes over the partners;
-// Uat, dUat, d2Uat of electron i over all j != i, and Vat, Grad, Lap over the ions.
+// Work items (walker, block of NT / 32 electrons), one warp per electron i with its lanes
+// over the partners: Uat, dUat, d2Uat of electron i over all j != i, and Vat, Grad, Lap
+// over the ions.  Unmasked: every walker; masked: the walkers of repair_list.
 template<typename T, int NT>
 __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int masked)
 {
-  const int iw   = blockIdx.x;
-  const int lane = threadIdx.x & 31;
-  const int i    = blockIdx.y * (NT / 32) + (threadIdx.x >> 5);
-  if (i >= s.ne || skip_walker(s, iw, masked)) // uniform over the warp
-    return;
+  constexpr int EPB = NT / 32;
+  const int lane   = threadIdx.x & 31;
+  const int nbj    = (s.ne + EPB - 1) / EPB;
+  const int nitems = (masked ? s.repair_list[0] : s.nw) * nbj;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x)
+  {
+  const int iw = masked ? s.repair_list[1 + item / nbj] : item / nbj;
+  const int i  = (item % nbj) * EPB + (threadIdx.x >> 5);
+  if (i >= s.ne) // uniform over the warp
+    continue;
   const T* Rx = s.Rt + ((size_t)iw * 3) * s.ne_pad;
   const T xi = Rx[i], yi = Rx[s.ne_pad + i], zi = Rx[2 * s.ne_pad + i];
   const T L0 = T(s.L[0]), L1 = T(s.L[1]), L2 = T(s.L[2]);
@@ -941,6 +967,7 @@ __global__ void __launch_bounds__(NT) jastrow_full_kernel(DevState<T> s, int mas
       J1[4 * s.ne_pad + i] = v[4];
     }
   }
+  }
 }
 
 // after a masked recompute: count and clear the repaired walkers' repair bits
@@ -966,7 +993,23 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
   constexpr int NT = 128;
   const size_t sm  = sizeof(T) * 4 * 7 * (size_t)s.lda;
   const int nblk   = (s.ne + VGL_EPB - 1) / VGL_EPB;
-  vgl_all_kernel<T, NT><<<s.nw * nblk, NT, sm, st>>>(s, Mt, masked);
+  static int sms   = 0;
+  if (sms == 0)
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms <= 0)
+      sms = 1;
+  }
+  // a repair touches a few walkers: their work items go to a grid of one wave
+  const int small = 8 * sms;
+  if (masked)
+  {
+    repair_list_kernel<T><<<1, 1024, 0, st>>>(s);
+    vgl_all_kernel<T, NT><<<std::min(small, s.nw * nblk), NT, sm, st>>>(s, Mt, masked);
+  }
+  else
+    vgl_all_kernel<T, NT><<<s.nw * nblk, NT, sm, st>>>(s, Mt, masked);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
@@ -1038,8 +1081,8 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
   }
   if (e != cudaSuccess)
     return e;
-  dim3 grid(s.nw, (s.ne + 3) / 4);
-  jastrow_full_kernel<T, 128><<<grid, 128, 0, st>>>(s, masked);
+  const int jitems = s.nw * ((s.ne + 3) / 4);
+  jastrow_full_kernel<T, 128><<<masked ? std::min(small, jitems) : jitems, 128, 0, st>>>(s, masked);
   e = cudaGetLastError();
   if (e != cudaSuccess || !masked)
     return e;
