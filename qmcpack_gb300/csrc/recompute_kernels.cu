@@ -878,6 +878,213 @@ __global__ void __launch_bounds__(16 * TY) gj_reg_kernel(DevState<T> s, const do
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident Gauss-Jordan over a cluster of CL CTAs (FP32 elimination, FP64
+// log|det| product), for determinants too large for one CTA's registers: CTA r owns the
+// columns [r cw, r cw + cw); inside it thread (ty, tx) owns rows ty + TY a (a < NAR) and
+// local columns tx + 16 b (b < NB).  Rows k and p and the pivot value are local to every
+// CTA (each holds its slice of every row); only the pivot column crosses CTAs: its owner
+// finds the pivot and publishes the column in shared memory (double-buffered), one
+// cluster barrier later every CTA copies it once over distributed shared memory and
+// eliminates its block in registers.
+// ---------------------------------------------------------------------------
+template<typename T, int CL, int TY, int NAR, int NB>
+__global__ void __launch_bounds__(16 * TY) gj_regcl_kernel(DevState<T> s, const double* Mt, int masked)
+{
+  const int slot = blockIdx.x / CL;
+  if (skip_slot(s, slot, masked)) // uniform over the cluster
+    return;
+  constexpr int NMAX = TY * NAR;   // rows
+  constexpr int CWMAX = 16 * NB;   // columns per CTA
+  __shared__ float colp[2][NMAX];  // published pivot column (before the interchange), owner CTA
+  __shared__ int pub[2];           // published pivot row (-1: singular)
+  __shared__ float colk[NMAX];     // this CTA's copy of the step's pivot column
+  __shared__ float rowk[CWMAX];    // this CTA's slice of row k before the interchange
+  __shared__ float rowp[CWMAX];    // this CTA's slice of the pivot row before the interchange
+  __shared__ int perm[NMAX];       // pivot row of every step
+  __shared__ int cinv[NMAX];       // output column of every working column
+  const int n = s.norb, r = (int)cluster_rank();
+  const int cw = (n + CL - 1) / CL, c0 = r * cw, ncw = max(0, min(n, c0 + cw) - c0);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4, lane = tid & 31;
+  const double* M = Mt + (size_t)slot * n * n;
+  float a[NAR][NB];
+#pragma unroll
+  for (int ia = 0; ia < NAR; ia++)
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int i = ty + TY * ia, jl = tx + 16 * ib;
+      a[ia][ib]   = (i < n && jl < ncw) ? static_cast<float>(M[(size_t)i * n + c0 + jl]) : 0.f;
+    }
+  LogAbsProduct logabs;
+  int sgn = 1, bad = 0;
+  for (int k = 0; k < n; k++)
+  {
+    const int b = k & 1;
+    const int owner = k / cw, kl = k - owner * cw; // owning CTA and its local column
+    const int kt = kl & 15, kb = kl >> 4;
+    if (owner == r)
+    {
+      // column k to shared memory, then every warp finds the pivot; warp 0 publishes it
+      if (tx == kt)
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+          if (c == kb)
+#pragma unroll
+            for (int ia = 0; ia < NAR; ia++)
+              colp[b][ty + TY * ia] = a[ia][c];
+      __syncthreads();
+      float bv = -1.f;
+      int bi   = n;
+      for (int i = k + lane; i < n; i += 32)
+      {
+        const float v = fabsf(colp[b][i]);
+        if (v > bv || (v == bv && i < bi))
+        {
+          bv = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi   = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi))
+        {
+          bv = ov;
+          bi = oi;
+        }
+      }
+      if (tid == 0)
+        pub[b] = bv > 0.f ? bi : -1;
+    }
+    cluster_sync_all();
+    const int p = dsm_ldi(dsm_map(&pub[b], (unsigned)owner));
+    if (p < 0)
+    {
+      bad = 1;
+      break;
+    }
+    // the pivot column from the owner, this CTA's slices of rows k and p
+    const unsigned rc = dsm_map(&colp[b][0], (unsigned)owner);
+    for (int i = tid; i < n; i += 16 * TY)
+      colk[i] = dsm_ldf(rc + 4u * (unsigned)i);
+    const int kr = k % TY, ka = k / TY, pr = p % TY, pa = p / TY;
+    if (ty == kr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == ka)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            rowk[tx + 16 * ib] = a[c][ib];
+    if (ty == pr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == pa)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            rowp[tx + 16 * ib] = a[c][ib];
+    __syncthreads();
+    const float d = colk[p];
+    if (tid == 0)
+      perm[k] = p;
+    if (r == 0 && tid == 0) // the one thread that writes log|det|
+    {
+      logabs.mul(static_cast<double>(d));
+      if (d < 0.f)
+        sgn = -sgn;
+      if (p != k)
+        sgn = -sgn;
+    }
+    const float rinv = 1.f / d;
+    // new pivot row slice rk = (old row p with 1 at column k) / d
+    float rk[NB];
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int jl = tx + 16 * ib;
+      rk[ib]       = jl < ncw ? (c0 + jl == k ? 1.f : rowp[jl]) * rinv : 0.f;
+    }
+    // the interchange: row p takes row k's old values
+    if (ty == pr && p != k)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == pa)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            a[c][ib] = rowk[tx + 16 * ib];
+    // elimination with the factors of column k after the interchange (0 at row k)
+#pragma unroll
+    for (int ia = 0; ia < NAR; ia++)
+    {
+      const int i   = ty + TY * ia;
+      const float f = (i < n && i != k) ? colk[i == p ? k : i] : 0.f;
+#pragma unroll
+      for (int ib = 0; ib < NB; ib++)
+        a[ia][ib] = fmaf(-f, rk[ib], a[ia][ib]);
+      if (owner == r && tx == kt)
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+          if (c == kb)
+            a[ia][c] = -f * rinv;
+    }
+    if (ty == kr)
+#pragma unroll
+      for (int c = 0; c < NAR; c++)
+        if (c == ka)
+#pragma unroll
+          for (int ib = 0; ib < NB; ib++)
+            a[c][ib] = rk[ib];
+    __syncthreads(); // colk, rowk and rowp are rewritten by the next step
+  }
+  if (bad)
+  {
+    if (r == 0 && tid == 0)
+    {
+      atomicOr(s.status + (slot % s.nw), ST_SINGULAR);
+      s.log_abs[slot] = -INFINITY;
+      s.sign[slot]    = 0;
+    }
+    cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
+    return;
+  }
+  // output column c holds working column cmap[c] (built in colk's storage); cinv is its
+  // inverse.  Every CTA holds perm.
+  if (tid == 0)
+  {
+    int* cmap = reinterpret_cast<int*>(colk);
+    for (int j = 0; j < n; j++)
+      cmap[j] = j;
+    for (int k = n - 1; k >= 0; k--)
+    {
+      const int p = perm[k];
+      const int t = cmap[k];
+      cmap[k]     = cmap[p];
+      cmap[p]     = t;
+    }
+    for (int c = 0; c < n; c++)
+      cinv[cmap[c]] = c;
+  }
+  __syncthreads();
+  T* A = s.Ainv + (size_t)slot * n * s.lda;
+#pragma unroll
+  for (int ia = 0; ia < NAR; ia++)
+#pragma unroll
+    for (int ib = 0; ib < NB; ib++)
+    {
+      const int i = ty + TY * ia, jl = tx + 16 * ib;
+      if (i < n && jl < ncw)
+        A[(size_t)i * s.lda + cinv[c0 + jl]] = static_cast<T>(a[ia][ib]);
+    }
+  if (r == 0 && tid == 0)
+  {
+    s.log_abs[slot] = logabs.value();
+    s.sign[slot]    = sgn;
+  }
+  cluster_sync_all(); // the owners' shared memory stays valid until every CTA is done
+}
+
 // Work items (walker, block of NT / 32 electrons), one warp per electron i with its lanes
 // over the partners: Uat, dUat, d2Uat of electron i over all j != i, and Vat, Grad, Lap
 // over the ions.  Unmasked: every walker; masked: the walkers of repair_list.
@@ -1026,8 +1233,9 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
     attr[0].val.clusterDim.z = 1;
     cfg.attrs                = attr;
     cfg.numAttrs             = 1;
-    auto with_cluster = [&](int cl, size_t smem) {
+    auto with_cluster = [&](int cl, size_t smem, int threads = GJ_NT) {
       cfg.gridDim              = dim3(2 * s.nw * cl);
+      cfg.blockDim             = dim3(threads);
       attr[0].val.clusterDim.x = cl;
       cfg.dynamicSmemBytes     = smem;
     };
@@ -1046,6 +1254,22 @@ cudaError_t launch_recompute(const DevState<T>& s, double* Mt, int masked, cudaS
         else
           gj_reg_kernel<float, 24, 8, 12><<<2 * s.nw, 384, 0, st>>>(s, Mt, masked);
         e    = cudaGetLastError();
+        done = true;
+      }
+      else if (n <= 384)
+      {
+        // register-resident over a cluster of 8 CTAs (48 columns each)
+        with_cluster(8, 0, 16 * 32);
+        e    = cudaLaunchKernelEx(&cfg, gj_regcl_kernel<float, 8, 32, 12, 3>, s, static_cast<const double*>(Mt),
+                                  masked);
+        done = true;
+      }
+      else if (n <= 768 && gj_cluster16_ok())
+      {
+        // register-resident over a cluster of 16 CTAs (48 columns each)
+        with_cluster(16, 0, 16 * 48);
+        e    = cudaLaunchKernelEx(&cfg, gj_regcl_kernel<float, 16, 48, 16, 3>, s, static_cast<const double*>(Mt),
+                                  masked);
         done = true;
       }
       else if (gj_smem_bytes(n, 8, 4) <= GJ_SMEM_MAX)
@@ -1107,6 +1331,9 @@ cudaError_t setup_recompute_kernels()
                                cudaFuncAttributeMaxDynamicSharedMemorySize, GJ_SMEM_MAX);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(gj_cluster_smem_kernel<float, float, 16>,
+                               cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gj_regcl_kernel<float, 16, 48, 16, 3>,
                                cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   }
   return e;

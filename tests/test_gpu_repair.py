@@ -2,8 +2,8 @@
 lost accuracy (qmcg_mw_recompute_walkers; TrialWaveFunction::mw_recompute with its
 recompute mask, TrialWaveFunction.cpp:225-240).
 
-FP32 crowds eliminate in FP32 over a cluster of 8 CTAs (small matrices) or 16 CTAs
-(768 x 768); FP64 crowds in FP64.  Against the FP64 recompute of mw_evaluateLog:
+FP32 crowds eliminate in FP32 with the matrix in registers: one CTA up to 192 x 192, a
+cluster of 8 CTAs up to 384 x 384, 16 CTAs up to 768 x 768; FP64 crowds in FP64.  Against the FP64 recompute of mw_evaluateLog:
 FP64 inverse within 1e-10 of the largest element, log|det| within 1e-9; FP32 inverse
 within 2e-4 in the relative Frobenius norm and log|det| within 2e-4 (an FP32 elimination
 of a matrix with condition number c carries about c * 6e-8); walkers without a flag
@@ -27,9 +27,10 @@ def _crowd(spec, nw, delay, seed):
 
 
 @pytest.mark.parametrize("name,prec", [
-    ("c0_32e", 4),    # 16 x 16: 8-CTA cluster, FP32
-    ("c1_384e", 4),   # 192 x 192: 8-CTA cluster, FP32
-    ("c2_1536e", 4),  # 768 x 768: 16-CTA cluster, FP32
+    ("c0_32e", 4),    # 16 x 16: one CTA, registers, FP32
+    ("c1_384e", 4),   # 192 x 192: one CTA, registers, FP32
+    ("c3_768e", 4),   # 384 x 384: 8-CTA cluster, registers, FP32
+    ("c2_1536e", 4),  # 768 x 768: 16-CTA cluster, registers, FP32
     ("c1_384e", 8),   # 192 x 192: 8-CTA cluster, FP64
 ])
 def test_repair_matches_fp64_recompute(name, prec):
