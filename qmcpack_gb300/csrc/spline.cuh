@@ -12,7 +12,7 @@ struct Vec;
 // FP32 coefficients are read as float2: with 128-512 threads per walker and 192-768
 // orbitals this gives a whole number of (column, x-plane) units per thread (measured
 // 4% faster at 192 orbitals than float4, which left half the threads idle in the
-// last round)
+// last pass over the units)
 template<>
 struct Vec<float>
 {
