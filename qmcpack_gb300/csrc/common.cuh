@@ -296,24 +296,47 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T* scratch)
   __syncthreads();
 }
 
-// sum NV values over the block; results valid in warp 0 only (no trailing barrier:
-// the caller must synchronise before scratch is written again)
+// sum NV <= 16 values over the block; the totals are valid in warp 0 (thread 0 included).
+// Inside a warp a reduce-scatter halves the values a lane keeps at every step (16
+// shuffles for 16 values instead of 5 per value) until lane l holds the warp's total of
+// value l / 2; warp 0 then adds the warps' totals and broadcasts them to its lanes.
+// scratch: 16 * 32 elements.  No trailing barrier: the caller synchronises before scratch
+// is written again.
 template<typename T, int NV>
 __device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch)
 {
+  static_assert(NV <= 16, "up to 16 values");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+  T x[16];
 #pragma unroll
-  for (int q = 0; q < NV; q++)
-    v[q] = warp_sum(v[q]);
-  if (lane == 0)
+  for (int q = 0; q < 16; q++)
+    x[q] = q < NV ? v[q] : T(0);
 #pragma unroll
-    for (int q = 0; q < NV; q++)
-      scratch[q * 32 + wid] = v[q];
+  for (int h = 8; h >= 1; h >>= 1) // exchange distance 2h, keep h values
+  {
+    const bool up = (lane & (2 * h)) != 0;
+#pragma unroll
+    for (int q = 0; q < h; q++)
+    {
+      const T send = up ? x[q] : x[q + h];
+      const T recv = __shfl_xor_sync(0xffffffffu, send, 2 * h);
+      x[q]         = (up ? x[q + h] : x[q]) + recv;
+    }
+  }
+  x[0] += __shfl_xor_sync(0xffffffffu, x[0], 1);
+  if ((lane & 1) == 0 && (lane >> 1) < NV)
+    scratch[(lane >> 1) * 32 + wid] = x[0];
   __syncthreads();
   if (wid == 0)
+  {
+    T t = T(0);
+    if (lane < NV)
+      for (int w = 0; w < nwarp; w++)
+        t += scratch[lane * 32 + w];
 #pragma unroll
     for (int q = 0; q < NV; q++)
-      v[q] = warp_sum(lane < nwarp ? scratch[q * 32 + lane] : T(0));
+      v[q] = __shfl_sync(0xffffffffu, t, q);
+  }
 }
 
 // Umrigar drift scaling (DriftModifierUNR::getDrift, a = 1)

@@ -301,7 +301,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
       // ------------------------------------------------ gradient, health check, proposal
       {
-        block_sum<T, 4>(g, red);
+        block_sum_to0<T, 4>(g, red); // thread 0 uses the sums
         if constexpr (LEARNED)
         {
           // the network at the current position: (mu, s) of the proposal
