@@ -244,17 +244,14 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       if (K > 1 && dc > 0)
       {
         const T* V = s.V + slot * K * lda;
-        // U_c . Ainv[row] of the earlier slots of this segment, formed when slot c was
-        // decided (zero for a rejected move)
-        const int base = dc * (dc - 1) / 2;
-        for (int c = threadIdx.x; c < dc; c += NT)
-          pv[c] = tri[base + c];
-        __syncthreads();
+        // pv_c = U_c . Ainv[row] of the earlier slots of this segment, formed when slot c
+        // was decided (zero for a rejected move), read straight from the table
+        const T* pvt = tri + dc * (dc - 1) / 2;
         for (int i = threadIdx.x; i < dc; i += NT)
         {
           T a = 0;
           for (int c = 0; c < dc; c++)
-            a += Bs[c * K + i] * pv[c];
+            a += Bs[c * K + i] * pvt[c];
           tv[i]          = -a;
           Bs[dc * K + i] = -a;
         }
