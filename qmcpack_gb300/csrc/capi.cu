@@ -371,6 +371,38 @@ struct HostStream
 };
 
 __global__ void bump_counter_kernel(unsigned long long* c) { c[0] += 1ull; }
+
+// walker positions between the caller's layout [nw][ne][3] and the device's [nw][3][ne_pad]
+// (FP64 and the move-precision copy; padding electrons at zero)
+template<typename T>
+__global__ void positions_from_caller_kernel(const double* __restrict__ aos, double* __restrict__ R,
+                                             T* __restrict__ Rt, int nw, int ne, int ne_pad)
+{
+  const size_t total = (size_t)nw * 3 * ne_pad;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
+  {
+    const int e       = (int)(t % ne_pad);
+    const size_t wq   = t / ne_pad; // iw * 3 + q
+    const int q       = (int)(wq % 3);
+    const size_t iw   = wq / 3;
+    const double x    = e < ne ? aos[(iw * ne + e) * 3 + q] : 0.0;
+    R[t]              = x;
+    Rt[t]             = static_cast<T>(x);
+  }
+}
+__global__ void positions_to_caller_kernel(const double* __restrict__ R, double* __restrict__ aos, int nw, int ne,
+                                           int ne_pad)
+{
+  const size_t total = (size_t)nw * ne * 3;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
+  {
+    const int q     = (int)(t % 3);
+    const size_t we = t / 3; // iw * ne + e
+    const int e     = (int)(we % ne);
+    const size_t iw = we / ne;
+    aos[t]          = R[(iw * 3 + q) * ne_pad + e];
+  }
+}
 __global__ void reset_cursor_kernel(int* c) { c[0] = 0; c[1] = 0; }
 
 // ---------------------------------------------------------------------------
@@ -420,6 +452,7 @@ struct Crowd final : qmcg_crowd_s
   DevState<T> s{};
   DeviceArena mem;
   double* Mt = nullptr; // FP64 Slater matrices for the recompute, [2][nw][N][N]
+  double* aos = nullptr; // positions in the caller's layout [nw][ne][3], staged for the copies
   T* W       = nullptr; // flush scratch, [nw][k][lda]
   double* gauss_d = nullptr;
   double* unif_d  = nullptr;
@@ -565,6 +598,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
     CUDA_TRY(mem.alloc(&d.gj_scratch, 2 * (size_t)nw * gj_scratch_doubles((int)N)));
     CUDA_TRY(mem.alloc(&d.repair_list, (size_t)nw + 1));
+    CUDA_TRY(mem.alloc(&aos, std::max<size_t>(1, (size_t)nw * sys->ne * 3)));
     CUDA_TRY(mem.alloc(&W, (size_t)nw * k * lda));
     const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
     CUDA_TRY(mem.alloc(&gauss_d, ng));
@@ -602,19 +636,12 @@ struct Crowd final : qmcg_crowd_s
   {
     if (!R)
       return fail(QMCG_ERR_ARG, "null positions");
+    // one copy of the caller's array as it is (a DMA when the caller's memory is pinned),
+    // the layout change on the device
     const int ne = sys->ne, ne_pad = s.ne_pad;
-    std::vector<double> h((size_t)nw * 3 * ne_pad, 0.0);
-    std::vector<T> ht((size_t)nw * 3 * ne_pad, T(0));
-    for (int iw = 0; iw < nw; iw++)
-      for (int e = 0; e < ne; e++)
-        for (int q = 0; q < 3; q++)
-        {
-          const double x                                  = R[((size_t)iw * ne + e) * 3 + q];
-          h[((size_t)iw * 3 + q) * ne_pad + e]            = x;
-          ht[((size_t)iw * 3 + q) * ne_pad + e]           = static_cast<T>(x);
-        }
-    CUDA_TRY(cudaMemcpyAsync(s.R, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(s.Rt, ht.data(), ht.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(aos, R, (size_t)nw * ne * 3 * sizeof(double), cudaMemcpyHostToDevice, stream));
+    positions_from_caller_kernel<T><<<304, 256, 0, stream>>>(aos, s.R, s.Rt, nw, ne, ne_pad);
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(stream));
     return QMCG_OK;
   }
@@ -622,13 +649,10 @@ struct Crowd final : qmcg_crowd_s
   int positions(double* R) override
   {
     const int ne = sys->ne, ne_pad = s.ne_pad;
-    std::vector<double> h((size_t)nw * 3 * ne_pad);
-    CUDA_TRY(cudaMemcpyAsync(h.data(), s.R, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    positions_to_caller_kernel<<<304, 256, 0, stream>>>(s.R, aos, nw, ne, ne_pad);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(R, aos, (size_t)nw * ne * 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
-    for (int iw = 0; iw < nw; iw++)
-      for (int e = 0; e < ne; e++)
-        for (int q = 0; q < 3; q++)
-          R[((size_t)iw * ne + e) * 3 + q] = h[((size_t)iw * 3 + q) * ne_pad + e];
     return QMCG_OK;
   }
 
