@@ -390,6 +390,30 @@ __global__ void positions_from_caller_kernel(const double* __restrict__ aos, dou
     Rt[t]             = static_cast<T>(x);
   }
 }
+// per walker the sums of the J2 and J1 values over its electrons (log J2 = -sum/2,
+// log J1 = -sum), a warp per walker: out[iw] (J2), out[nw + iw] (J1)
+template<typename T>
+__global__ void jastrow_log_sums_kernel(const T* __restrict__ J2, const T* __restrict__ J1, int nw, int ne,
+                                        int ne_pad, double* __restrict__ out)
+{
+  const int iw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (iw >= nw)
+    return;
+  double u2 = 0, u1 = 0;
+  for (int e = lane; e < ne; e += 32)
+  {
+    u2 += static_cast<double>(J2[(size_t)iw * 5 * ne_pad + e]);
+    u1 += static_cast<double>(J1[(size_t)iw * 5 * ne_pad + e]);
+  }
+  u2 = warp_sum(u2);
+  u1 = warp_sum(u1);
+  if (lane == 0)
+  {
+    out[iw]      = u2;
+    out[nw + iw] = u1;
+  }
+}
+
 __global__ void positions_to_caller_kernel(const double* __restrict__ R, double* __restrict__ aos, int nw, int ne,
                                            int ne_pad)
 {
@@ -453,6 +477,7 @@ struct Crowd final : qmcg_crowd_s
   DeviceArena mem;
   double* Mt = nullptr; // FP64 Slater matrices for the recompute, [2][nw][N][N]
   double* aos = nullptr; // positions in the caller's layout [nw][ne][3], staged for the copies
+  double* jsum = nullptr; // [2][nw] J2 and J1 value sums of every walker (get_log)
   T* W       = nullptr; // flush scratch, [nw][k][lda]
   double* gauss_d = nullptr;
   double* unif_d  = nullptr;
@@ -599,6 +624,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.gj_scratch, 2 * (size_t)nw * gj_scratch_doubles((int)N)));
     CUDA_TRY(mem.alloc(&d.repair_list, (size_t)nw + 1));
     CUDA_TRY(mem.alloc(&aos, std::max<size_t>(1, (size_t)nw * sys->ne * 3)));
+    CUDA_TRY(mem.alloc(&jsum, 2 * (size_t)nw));
     CUDA_TRY(mem.alloc(&W, (size_t)nw * k * lda));
     const size_t ng = (size_t)sys->ne * nw * 3, nu = (size_t)sys->ne * nw;
     CUDA_TRY(mem.alloc(&gauss_d, ng));
@@ -806,26 +832,20 @@ struct Crowd final : qmcg_crowd_s
 
   int get_log(double* lp, int* sg, double* parts) override
   {
-    std::vector<double> la;
+    std::vector<double> la, js;
     std::vector<int> sgn;
-    std::vector<T> j1, j2;
+    jastrow_log_sums_kernel<T><<<(nw + 7) / 8, 256, 0, stream>>>(s.J2, s.J1, nw, sys->ne, s.ne_pad, jsum);
+    CUDA_TRY(cudaGetLastError());
     int rc = d2h(la, s.log_abs, 2 * (size_t)nw);
     if (!rc)
       rc = d2h(sgn, s.sign, 2 * (size_t)nw);
     if (!rc)
-      rc = d2h(j2, s.J2, (size_t)nw * 5 * s.ne_pad);
-    if (!rc)
-      rc = d2h(j1, s.J1, (size_t)nw * 5 * s.ne_pad);
+      rc = d2h(js, jsum, 2 * (size_t)nw);
     if (rc)
       return rc;
     for (int iw = 0; iw < nw; iw++)
     {
-      double u2 = 0, u1 = 0;
-      for (int e = 0; e < sys->ne; e++)
-      {
-        u2 += static_cast<double>(j2[(size_t)iw * 5 * s.ne_pad + e]);
-        u1 += static_cast<double>(j1[(size_t)iw * 5 * s.ne_pad + e]);
-      }
+      const double u2 = js[iw], u1 = js[nw + iw];
       const double lj2 = s.has_j2 ? -0.5 * u2 : 0.0, lj1 = s.has_j1 ? -u1 : 0.0;
       if (lp)
         lp[iw] = la[iw] + la[nw + iw] + lj1 + lj2;
