@@ -212,20 +212,26 @@ def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4, R=None):
 
 
 def effective_samples(args, system, dsys32, seed: int):
-    """Effective independent samples/s = walker-sweeps/s / kappa, kappa the integrated
-    autocorrelation time of the crowd-averaged local energy per sweep (simstats), for
-      plain_fp64:   drift-diffusion, FP64 move loop (walker-resident path, SIMT flush)
+    """Effective independent samples/s = walker-sweeps/s / kappa for
+      plain_fp64:   drift-diffusion, FP64 move loop (the comparator the metric names)
       plain_fp32:   drift-diffusion, FP32 move loop, tcgen05 3xTF32 flush
-      learned_fp32: the learned MH proposal, trained on configurations of the FP32 plain run
+      learned_fp32: the learned MH proposal, trained on the FP32 plain run's configurations
                     (staged kernels, BF16 network on the tensor cores, hand-written backward
-                    and Adam), then run frozen on the walker-resident kernel
-    All three start from one configuration equilibrated by args.eff_equil plain FP32 sweeps.
-    FP32 runs: args.eff_sweeps timed sweeps; the FP64 run: args.eff_sweeps_fp64 timed sweeps,
-    and its kappa is the FP32 plain run's (the same drift-diffusion chain up to rounding; a
-    short FP64 series cannot resolve kappa).  Wall clock around each whole call, local
-    energy measured after every sweep."""
+                    and Adam), then run frozen on the walker-resident kernel.
+    Protocol: one FP32 drift-diffusion crowd is equilibrated in blocks of args.eff_block
+    sweeps, at least args.eff_min_blocks of them, until the last block's mean energy agrees
+    with the previous block's within 2 combined standard errors twice in a row (at most
+    args.eff_max_blocks blocks); the three methods then start from that configuration and
+    run the same number of sweeps (args.eff_sweeps), so their kappa estimates see series
+    of equal length.  Each method's kappa is its own: the autocorrelation function averaged
+    over the walkers' own E_L series (independent chains, simstats truncation rule);
+    kappa_resolved says whether it reached zero within the first quarter of the series
+    (otherwise kappa is bounded by the series length and the effective samples are upper
+    bounds).  Energies and variances of every method are compared with plain FP64 at 2
+    sigma.  Wall clock around each whole call; the local energy is measured after every
+    sweep in every method."""
     from qmcpack_gb300.crowd import Crowd, DeviceSystem
-    from qmcpack_gb300.stats import energy_statistics
+    from qmcpack_gb300.stats import agree_within, ensemble_statistics
     spec = system.spec
     nw, k, tau = spec.walkers, spec.delay, spec.tau
     rec = spec.recompute_every
@@ -237,27 +243,42 @@ def effective_samples(args, system, dsys32, seed: int):
         res = fn()
         return res, time.perf_counter() - t0
 
-    def summarize(name, el, dt, n, extra=None, kappa=None):
-        st = energy_statistics(el)
+    def summarize(name, el, dt, n, extra=None):
+        st = ensemble_statistics(el)
         wsps = nw * n / dt
-        kap = st["kappa"] if kappa is None else kappa
         h = el.mean(axis=1)
-        d = {"energy": st["energy"], "error": st["error"], "variance": st["variance"], "kappa": kap,
-             "kappa_own_series": st["kappa"], "energy_first_half": float(h[: n // 2].mean()),
-             "energy_second_half": float(h[n // 2:].mean()),
-             "walker_sweeps_per_s": wsps, "effective_samples_per_s": wsps / kap, "ms_per_sweep": dt / n * 1e3,
-             "sweeps": n}
+        d = dict(st)
+        d.update({"energy_first_half": float(h[: n // 2].mean()), "energy_second_half": float(h[n // 2:].mean()),
+                  "walker_sweeps_per_s": wsps, "effective_samples_per_s": wsps / st["kappa"],
+                  "ms_per_sweep": dt / n * 1e3})
         if extra:
             d.update(extra)
         out[name] = d
 
+    # equilibration until two consecutive block comparisons pass
     g = Crowd(dsys32, nw, k)
     g.load_walkers(make_walkers(system, nw, seed=300))
     g.mw_evaluateLog()
-    _, t_eq = timed(lambda: g.vmc_sweeps(args.eff_equil, tau, seed, rng_mode=1, recompute_every=rec,
-                                         flush=args.flush))
+    blocks, passes, t_eq = [], 0, 0.0
+    for _ in range(args.eff_max_blocks):
+        (_, _, el, _), dt = timed(lambda: g.vmc_sweeps_measure(args.eff_block, tau, seed, recompute_every=rec,
+                                                                flush=args.flush))
+        t_eq += dt
+        blocks.append(ensemble_statistics(el))
+        if len(blocks) >= max(2, args.eff_min_blocks) and agree_within(blocks[-1], blocks[-2], "energy", "error"):
+            passes += 1
+            if passes >= 2:
+                break
+        else:
+            passes = 0
+    out["equilibration"] = {"method": "plain FP32 drift-diffusion", "block_sweeps": args.eff_block,
+                            "blocks": len(blocks), "sweeps": len(blocks) * args.eff_block, "seconds": t_eq,
+                            "stationary": passes >= 2,
+                            "test": f"at least {args.eff_min_blocks} blocks, then the last block mean within 2 "
+                                    "sigma of the previous block, twice in a row",
+                            "block_energies": [b["energy"] for b in blocks],
+                            "block_errors": [b["error"] for b in blocks]}
     Req = g.positions()
-    # FP32 drift-diffusion
     n = args.eff_sweeps
     (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=rec, flush=args.flush))
     summarize("plain_fp32", el, dt, n, {"acceptance": a / max(a + r, 1)})
@@ -267,10 +288,8 @@ def effective_samples(args, system, dsys32, seed: int):
     g = Crowd(ds64, nw, k)
     g.load_walkers(Req)
     g.mw_evaluateLog()
-    n64 = args.eff_sweeps_fp64
-    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n64, tau, seed + 1, recompute_every=rec))
-    summarize("plain_fp64", el, dt, n64, {"acceptance": a / max(a + r, 1), "kappa_source": "plain_fp32"},
-              kappa=out["plain_fp32"]["kappa"])
+    (a, r, el, _), dt = timed(lambda: g.vmc_sweeps_measure(n, tau, seed + 1, recompute_every=rec))
+    summarize("plain_fp64", el, dt, n, {"acceptance": a / max(a + r, 1)})
     del g, ds64
     # learned proposal: trained on the plain run's configurations, then frozen
     g = Crowd(dsys32, nw, k)
@@ -284,19 +303,23 @@ def effective_samples(args, system, dsys32, seed: int):
                                                            flush=args.flush))
     summarize("learned_fp32", el, dt, n, {
         "acceptance": a / max(a + r, 1),
-        "training": {"sweeps": args.train_sweeps, "moves": args.train_sweeps * nw * system.n_elec,
+        "training": {"sweeps": args.train_sweeps, "electron_moves": args.train_sweeps * nw * system.n_elec,
                      "seconds": t_train, "lr": args.lr, "final_mean_alpha_jump2": tr[0],
                      "final_mean_alpha": tr[1], "final_objective": tr[2], "parameters_finite": params_finite,
-                     "data": "configurations of the FP32 drift-diffusion run, continued on-policy"}})
+                     "data": "configurations of the equilibrated FP32 drift-diffusion run, continued on-policy "
+                             "(one Adam step per electron move over the 512 walkers)"}})
     del g
     p64 = out["plain_fp64"]
     for name in ("plain_fp32", "learned_fp32"):
         o = out[name]
         o["speedup_vs_plain_fp64"] = o["effective_samples_per_s"] / p64["effective_samples_per_s"]
-        o["energy_within_2sigma_of_plain_fp32"] = bool(
-            abs(o["energy"] - out["plain_fp32"]["energy"]) <= 2 * np.hypot(o["error"], out["plain_fp32"]["error"]))
-    out["unit"] = "effective samples/s (walker-sweeps/s / kappa)"
-    out["equilibration"] = {"sweeps": args.eff_equil, "seconds": t_eq, "method": "plain FP32 drift-diffusion"}
+        o["energy_within_2sigma_of_plain_fp64"] = agree_within(o, p64, "energy", "error")
+        o["variance_within_2sigma_of_plain_fp64"] = agree_within(o, p64, "variance", "variance_error")
+    lf, pf = out["learned_fp32"], out["plain_fp32"]
+    lf["speedup_vs_plain_fp32"] = lf["effective_samples_per_s"] / pf["effective_samples_per_s"]
+    lf["energy_within_2sigma_of_plain_fp32"] = agree_within(lf, pf, "energy", "error")
+    lf["variance_within_2sigma_of_plain_fp32"] = agree_within(lf, pf, "variance", "variance_error")
+    out["unit"] = "effective samples/s (walker-sweeps/s / kappa, kappa per method from its own walker series)"
     return out
 
 
@@ -423,27 +446,58 @@ def run_c3(args, rank: int, world: int):
 
 
 def run_reference(args, rank: int, world: int):
+    """The reference's CPU implementation of the path (the oracle port of its algorithms,
+    mt19937 stream of StdRandom) on the full workload: all walkers of the config, one
+    sweep per step, W untimed warm-up sweeps, K timed sweeps, OpenMP over walkers on all
+    host cores; the periodic FP64 recompute is timed once and added pro rata."""
     if rank != 0:
         return
     if args.workload not in SPECS:
         print(json.dumps({"impl": "reference", "unavailable": "the CPU restatement is timed on single-system "
                           "workloads only (c0_32e, c1_384e, c2_1536e, c3_768e)"}), flush=True)
         return
+    from oracle import oracle as orc
     spec = SPECS[args.workload]
-    base = cpu_baseline(args.workload, max_seconds=max(5.0, 60.0 / max(args.steps, 1)))
+    system = make_system(spec)
+    cores = os.cpu_count() or 1
+    nw, ne = spec.walkers, system.n_elec
+    orc.set_threads(cores)
+    c = orc.Crowd(system, nw, spec.delay, spec.precision)
+    c.load_walkers(make_walkers(system, nw, seed=100))
+    t0 = time.perf_counter()
+    c.evaluate_log(nthreads=cores)
+    rec_s = time.perf_counter() - t0
+    rng = orc.Rng(11)
+    c.vmc_sweeps(rng, args.warmup, spec.tau, True)
+    t0 = time.perf_counter()
+    na, nr, _ = c.vmc_sweeps(rng, args.steps, spec.tau, True)
+    sweep_s = time.perf_counter() - t0
+    n_rec = args.steps / spec.recompute_every if spec.recompute_every else 0.0
+    total_s = sweep_s + n_rec * rec_s
+    moves = args.steps * nw * ne
+    value = moves / total_s
+    sample = (f"{args.steps} timed sweeps (after {args.warmup} warm-up) x {nw} walkers x {ne} electrons of "
+              f"{args.workload}, {'FP32' if spec.precision == 4 else 'FP64'} move loop, mt19937 stream, "
+              f"{sweep_s:.1f} s; FP64 recompute of all walkers {rec_s * 1e3:.0f} ms, added {n_rec:g} times")
+    base = {"value": value, "unit": "walker-moves/s", "cores": cores, "kind": "port", "sample": sample}
     line = {
-        "impl": "reference", "metric": "walker-moves/s", "value": base["value"], "unit": "walker-moves/s",
+        "impl": "reference", "metric": "walker-moves/s", "value": value, "unit": "walker-moves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": spec.walkers * SPECS[args.workload].n_up * 2 / base["value"] * 1e3,
+        "ms_per_step": total_s / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if spec.precision == 4 else "f64", "data": "synthetic",
         "config": {"workload": f"{args.workload}: {DESCRIPTIONS.get(args.workload, '')}",
                    "step": "one VMC sweep (every electron of every walker moved once)",
-                   "what_runs": "the CPU restatement of the reference algorithms (oracle/), all host cores; the "
-                                "reference's own GPU build needs LAPACK/HDF5/libxml2/Boost and an offload compiler "
-                                "that this image lacks"},
+                   "walkers": nw, "electrons": ne, "delay_rank": spec.delay,
+                   "recompute": f"FP64 recompute every {spec.recompute_every} sweeps, measured once and added "
+                                f"pro rata" if spec.recompute_every else "none",
+                   "what_runs": "the CPU restatement of the reference algorithms (oracle/), OpenMP over walkers "
+                                "on all host cores; the reference's own build needs LAPACK/HDF5/libxml2/Boost "
+                                "and an offload compiler that this image lacks, and its sources are not on the "
+                                "GPU host"},
+        "acceptance": na / max(na + nr, 1),
         "cpu_baseline": base,
-        "e2e": {"value": base["value"], "unit": "walker-moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": value, "unit": "walker-moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -469,10 +523,12 @@ def run_ours(args, rank: int, world: int):
     from qmcpack_gb300.replicas import aggregate_timing, replica_seed
     seed = replica_seed(2024, rank)
     recompute_every = spec.recompute_every
-    # equilibration from the uniform start (untimed), then warm-up (also captures the sweep graph)
+    # equilibration from the uniform start (untimed), then warm-up (also captures the sweep graph).
+    # The timed loops run the sweep graph alone; the periodic FP64 recompute (every
+    # recompute_every sweeps) is measured once and added pro rata: steps / recompute_every of it.
     if args.equil > 0:
         crowd.vmc_sweeps(args.equil, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
-    crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
+    crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=0, flush=args.flush)
     stream = torch.cuda.ExternalStream(crowd.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(dev)
@@ -491,12 +547,12 @@ def run_ours(args, rank: int, world: int):
     ms = e0.elapsed_time(e1)
     acc, rej = crowd.sync()
     repaired = crowd.last_repaired
+    rec_ms = crowd.profile_recompute() if recompute_every else 0.0
+    n_rec = args.steps / recompute_every if recompute_every else 0.0
+    sweep_ms = ms
+    ms = ms + n_rec * rec_ms
     moves, ms = aggregate_timing(args.steps * nw * system.n_elec, ms)
     value = moves / (ms / 1e3)
-    sweeps_done = args.equil + args.warmup
-    recomputes = 0
-    if recompute_every:
-        recomputes = (sweeps_done + args.steps) // recompute_every - sweeps_done // recompute_every
 
     # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
     Rh = torch.from_numpy(crowd.positions()).pin_memory()
@@ -507,11 +563,11 @@ def run_ours(args, rank: int, world: int):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         crowd.load_walkers(Rnp)
-        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
+        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=0, flush=args.flush)
         Rnp[...] = crowd.positions()
         lp, _, _ = crowd.get_log()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = time.perf_counter() - t0 + n_rec * rec_ms / 1e3
     _, e2e_s = aggregate_timing(0.0, e2e_s)
     e2e_value = moves / e2e_s
     h2d = Rnp.nbytes
@@ -555,6 +611,11 @@ def run_ours(args, rank: int, world: int):
                    "walkers_per_gpu": nw, "electrons": system.n_elec, "delay_rank": k,
                    "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32"}[args.flush],
                    "l2": "inputs larger than L2 (spline table 102 MB + inverses/gradients ~0.8 GB per sweep)",
+                   "recompute": ({"every_sweeps": recompute_every, "measured_ms": rec_ms, "added": n_rec,
+                                  "how": "the FP64 recompute of all walkers, timed once with CUDA events, added "
+                                         "steps/recompute_every times to the device and e2e totals"}
+                                 if recompute_every else None),
+                   "sweep_graph_ms_per_step": sweep_ms / args.steps,
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": "sweep_kernel (walker-resident; one launch = up to k electrons "
                                                  "of every walker)",
@@ -569,7 +630,7 @@ def run_ours(args, rank: int, world: int):
                                "achieved_gbs": flush_bytes / (flush_ms / 1e3) / 1e9 if flush_ms else None}},
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "walker-moves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches_per_sweep(system, k) * args.steps + 3 * recomputes,
+        "gpu_launches": launches_per_sweep(system, k) * args.steps,
         "clocks": clk,
         "acceptance": acc / max(acc + rej, 1),
         "walkers_repaired_in_timed_sweeps": repaired,
@@ -595,9 +656,10 @@ def main():
     ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
                     help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
     ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
-    ap.add_argument("--eff-sweeps", type=int, default=600, help="timed FP32 sweeps per method in the comparison")
-    ap.add_argument("--eff-sweeps-fp64", type=int, default=80, help="timed FP64 sweeps in the comparison")
-    ap.add_argument("--eff-equil", type=int, default=300)
+    ap.add_argument("--eff-sweeps", type=int, default=500, help="measured sweeps per method in the comparison")
+    ap.add_argument("--eff-block", type=int, default=250, help="sweeps per equilibration block")
+    ap.add_argument("--eff-min-blocks", type=int, default=8, help="fewest equilibration blocks")
+    ap.add_argument("--eff-max-blocks", type=int, default=16, help="most equilibration blocks")
     ap.add_argument("--train-sweeps", type=int, default=10)
     ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args()

@@ -187,7 +187,9 @@ int qmcg_get_phi_vgl(qmcg_crowd crowd, double* phi);
  * accepted or rejected for every walker), then mw_completeUpdates, with the FP64
  * recompute every params->recompute_every sweeps.  Replaces the body of
  * VMCBatched::advanceWalkers (VMCBatched.cpp:106-177); runs as one captured CUDA
- * graph per sweep.  accept_log [num_sweeps][n_elec][nw] (0/1) may be NULL. */
+ * graph per sweep.  accept_log [num_sweeps][n_elec][nw] (0/1) may be NULL; with
+ * rng_mode 1 and path 0 the decisions are recorded by the walker-resident kernel
+ * itself (its launches then run outside the graph), otherwise by the staged kernels. */
 int qmcg_vmc_sweeps(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, qmcg_sweep_stats* stats,
                     int* accept_log);
 
@@ -213,6 +215,77 @@ int qmcg_mw_evaluate_local_energy(qmcg_crowd crowd, double* e_local, double* kin
  * e_local and kinetic (may be NULL) are host arrays [num_sweeps][num_walkers]. */
 int qmcg_vmc_sweeps_measure(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, double* e_local,
                             double* kinetic, qmcg_sweep_stats* stats);
+
+/* Per-electron gradient and Laplacian of log psi from the tracked state, after all
+ * delayed updates: grads [nw][n_elec][3], laplacians [nw][n_elec], log_psi [nw] (the
+ * tracked log|psi|); any pointer may be NULL.  TrialWaveFunction::mw_evaluateGL with
+ * fromscratch = false (TrialWaveFunction.cpp:869-919: P.G and P.L, the inputs of the
+ * Hamiltonian's kinetic and other G/L-based terms); fromscratch = true is
+ * qmcg_mw_evaluate_log followed by this call.  Returns QMCG_ERR_STATE while delayed
+ * updates are pending. */
+int qmcg_mw_evaluate_gl(qmcg_crowd crowd, double* log_psi, double* grads, double* laplacians);
+
+/* Verification helper (no reference counterpart; it exposes what the driver loop of
+ * VMCBatched::advanceWalkers sees for every move): qmcg_vmc_sweeps on the
+ * walker-resident path (rng_mode 1, path 0, drift-diffusion) with one record per move,
+ * trace [num_sweeps][n_elec][nw][QMCG_TRACE_FIELDS] FP64:
+ *   0-2  proposed position          3  psi(R')/psi(R)
+ *   4-6  grad log psi at R'         7-9  grad log psi at R (the drift's input)
+ *   10   1 accepted / 0 rejected    11   Ainv[row] . phi(r_row) of the tracked inverse
+ *                                        (1 when exact; the repair health check's value)
+ * The kernels run outside the sweep graph while recording. */
+#define QMCG_TRACE_FIELDS 12
+int qmcg_vmc_sweeps_trace(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps, qmcg_sweep_stats* stats,
+                          double* trace);
+
+/* ---------------------------------------------------------------- diffusion Monte Carlo
+ * The DMC step of DMCBatched::advanceWalkers (src/QMCDrivers/DMC/DMCBatched.cpp:72-290) on
+ * the walker-resident path: a drift-diffusion sweep in which a move that changes the sign
+ * of psi is rejected (fixed node; SFNBranch::phaseChanged, SFNBranch.h:161-169), with
+ * tau |xi|^2 summed per walker over proposed and accepted moves (R2PROPOSED, R2ACCEPTED),
+ * then the local energy (as qmcg_mw_evaluate_local_energy) and the branch weight
+ * w *= exp(tau_eff' (2 E_trial - E_new - E_old)) of SFNBranch::branchWeight
+ * (SFNBranch.h:199-208), tau_eff' = tau_eff / 2 scaled down linearly between
+ * branch_cutoff and branch_max of x = max(E_ref - E_new, E_ref - E_old) and zero beyond.
+ * Population control (which walkers die or are copied, SFNBranch's E_trial feedback)
+ * stays on the host; qmcg_dmc_copy_walkers moves the walkers' device state. */
+typedef struct
+{
+  double e_trial;       /* SFNBranch ETRIAL */
+  double e_ref;         /* EREF, the centre of the branching cutoff window */
+  double tau_eff;       /* TAUEFF */
+  double branch_cutoff; /* BRANCHCUTOFF */
+  double branch_max;    /* BRANCHMAX, > branch_cutoff */
+} qmcg_branch_params;
+
+/* Starts DMC on the crowd's current walkers: weights 1, ages 0, and the local energy of
+ * every walker (e_local [nw], may be NULL) kept as the E_old of the first branch weight. */
+int qmcg_dmc_init(qmcg_crowd crowd, double* e_local);
+/* One DMC step (params: rng_mode 1, path 0; recompute_every counts steps).  Outputs (any
+ * may be NULL): weights [nw] after the branch factor, e_local [nw], age [nw] (steps since a
+ * walker's last proposed move, DMCBatched.cpp:271-274), sums [5] = sum w, sum w E_L,
+ * sum w E_L^2, sum R2ACCEPTED, sum R2PROPOSED (WalkerControl::computeCurData,
+ * WalkerControl.cpp:243-270), and trace (as qmcg_vmc_sweeps_trace, the step's sweep then
+ * runs outside its graph). */
+int qmcg_dmc_step(qmcg_crowd crowd, const qmcg_sweep_params* params, const qmcg_branch_params* branch,
+                  double* weights, double* e_local, int* age, double* sums, qmcg_sweep_stats* stats, double* trace);
+/* Population control on the device (Walker::makeCopy of WalkerControl::branch and
+ * WalkerReconfiguration::getIndexPermutation): slot i takes the state of walker src[i]
+ * (positions, inverses, orbital rows, Jastrow state, log|psi|, E_old, age); every walker
+ * whose state is copied must keep its own slot (src[src[i]] == src[i]); all weights
+ * become 1.  Returns QMCG_ERR_STATE while delayed updates are pending. */
+int qmcg_dmc_copy_walkers(qmcg_crowd crowd, const int* src);
+/* Population control with a fixed walker count, host part (no GPU needed): the comb of
+ * WalkerReconfiguration::getIndexPermutation (src/QMCDrivers/DMC/WalkerReconfiguration.cpp:30-107).
+ * num_walkers teeth at W (u + i) / num_walkers, W = sum |w|, 0 <= u < 1; walker i gets one copy
+ * per tooth inside its stretch of the cumulative weights.  src [num_walkers]: the walker each
+ * slot takes (slots of walkers without a copy take the extra copies of the others, in order;
+ * the others keep their own), ready for qmcg_dmc_copy_walkers; num_kept (may be NULL): walkers
+ * with at least one copy. */
+int qmcg_dmc_comb(int num_walkers, const double* weights, double u, int* src, int* num_kept);
+/* qmcg_dmc_comb on the crowd's current weights followed by qmcg_dmc_copy_walkers; src (may be
+ * NULL) receives the sources. */
+int qmcg_dmc_reconfigure(qmcg_crowd crowd, double u, int* src);
 
 /* ---------------------------------------------------------------- learned MH proposal
  * No reference counterpart: a new proposal for the same exact Metropolis-Hastings step
@@ -320,18 +393,21 @@ int qmcg_mw_update_inv_mat_ex(int precision, int num_walkers, int n, int lda, in
  * allocator, an offload runtime that reserves the device), code that cannot
  * afford the device-wide synchronisation cudaFree implies while other streams run,
  * and code running where allocation is forbidden (driver callbacks, real-time
- * threads).  Same arguments, layout and result as qmcg_mw_update_inv_mat; the
- * caller still passes every input and output.
- * Limit: its scratch is one fixed device array of QMCG_NOALLOC_SCRATCH_BYTES
- * (16 MiB) that every GPU on which this code is loaded holds until the process
- * exits; calls needing num_walkers*delay_rank*lda*element_size bytes beyond it
- * return QMCG_ERR_ARG and the caller splits its walkers into batches.
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  Every call shares the array and it keeps the last call's contents;
- * nothing in it has to start at zero (every element a call reads is written
- * earlier by the same call), but calls that overlap on the GPU race and must be
- * ordered by the caller, for example by issuing them on one stream. */
+ * threads).  Same arguments and layout as qmcg_mw_update_inv_mat, and the same
+ * kernel for every shape, hence the same result; the caller still passes every
+ * input and output.
+ * Limit: shapes whose per-walker tiles fit in shared memory need no scratch; the
+ * others use one fixed device array of QMCG_NOALLOC_SCRATCH_BYTES (16 MiB) that
+ * every GPU on which this code is loaded holds until the process exits, and calls
+ * needing num_walkers*delay_rank*lda*element_size bytes beyond it return
+ * QMCG_ERR_ARG: the caller splits its walkers into batches.
+ * The first call that uses the array on a device looks up its device address (once
+ * per device, with that device current, and again if the device's context was
+ * re-created); make that first call before any stream capture.  Every call shares
+ * the array and it keeps the last call's contents; nothing in it has to start at
+ * zero (every element a call reads is written earlier by the same call), but calls
+ * that overlap on the GPU race and must be ordered by the caller, for example by
+ * issuing them on one stream. */
 #define QMCG_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
 int qmcg_mw_update_inv_mat_noalloc(int precision, int num_walkers, int n, int lda, int delay_rank, int delay_count,
                                    void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
@@ -350,6 +426,12 @@ int qmcg_profile_ratio(qmcg_crowd crowd, int num_electrons, double* ms_per_launc
  * per batched flush launch, out[2] and out[3] = launches of each per sweep.
  * Needs a graph built by qmcg_vmc_sweeps with rng_mode 1 and path 0. */
 int qmcg_profile_sweep(qmcg_crowd crowd, int num_sweeps, double* out4);
+
+/* Measurement helper (no reference counterpart): device time in ms of one periodic
+ * FP64 recompute of every walker (the full recompute qmcg_vmc_sweeps runs every
+ * recompute_every sweeps), timed with CUDA events on the crowd's stream.  Leaves the
+ * crowd freshly recomputed; returns QMCG_ERR_STATE while delayed updates are pending. */
+int qmcg_profile_recompute(qmcg_crowd crowd, double* ms);
 
 #ifdef __cplusplus
 }

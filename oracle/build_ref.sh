@@ -1,10 +1,11 @@
 #!/bin/sh
 # Builds oracle/_ref/libref.so: the reference's header-only tricubic spline evaluator
-# compiled in place from REFERENCE_ROOT (default /root/reference), with a minimal
-# config.h shim.  Test infrastructure only; skipped when the reference is absent.
+# compiled in place from the reference's source tree (first argument, else
+# $QMCPACK_REFERENCE_DIR, else /root/reference), with a minimal config.h shim.
+# Test infrastructure only; skipped when the reference sources are absent.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+REF=${1:-${QMCPACK_REFERENCE_DIR:-/root/reference}}
 [ -d "$REF/src/spline2" ] || { echo "reference sources not found at $REF; skipping oracle/_ref"; exit 0; }
 mkdir -p "$HERE/_ref"
 ${CXX:-g++} -O2 -std=c++17 -fPIC -shared -Drestrict=__restrict__ \

@@ -18,6 +18,9 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_long)
 
+# fields of one move record: position xyz, ratio, grad at R' xyz, grad at R xyz, accepted, self ratio
+TRACE_FIELDS = 12
+
 
 def build(force: bool = False) -> str:
     so = os.path.join(_HERE, "liboracle.so")
@@ -57,6 +60,12 @@ def lib():
         L.orc_rng_uniform.argtypes = [C.c_void_p, _dp, C.c_long]
         L.orc_rng_gauss.argtypes = [C.c_void_p, _dp, C.c_long]
         L.orc_vmc_sweeps.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int, _lp, _lp, _ip]
+        L.orc_vmc_sweeps_philox.argtypes = [C.c_void_p, C.c_uint64, C.c_uint, C.c_int, C.c_double, C.c_int, _lp,
+                                            _lp, _dp]
+        L.orc_replay_trace.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
+        L.orc_replay_trace_philox.argtypes = [C.c_void_p, C.c_uint64, C.c_uint, C.c_int, C.c_double, C.c_int,
+                                              C.c_int, _dp, _dp, _dp]
+        L.orc_copy_walkers.argtypes = [C.c_void_p, _ip]
         L.orc_prefactors.argtypes = [C.c_double, _dp, _dp, _dp]
         L.orc_spline_vgh.argtypes = [_ip, C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp]
         L.orc_functor_eval.argtypes = [C.c_int, C.c_double, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
@@ -311,6 +320,44 @@ class Crowd:
         lib().orc_vmc_sweeps(self.h, rng.h, nsteps, tau, int(use_drift), C.byref(na), C.byref(nr),
                              _ptr(acc, _ip) if acc is not None else None)
         return na.value, nr.value, acc
+
+    def vmc_sweeps_philox(self, seed: int, nsteps: int, tau: float, use_drift: bool = True, sweep0: int = 0,
+                          trace: bool = False):
+        """Sweeps on the device's counter-based stream (Philox4x32-10, counter (walker, electron,
+        sweep, j)): (accepted, rejected, trace [nsteps][ne][nw][12] or None)."""
+        na, nr = C.c_long(0), C.c_long(0)
+        tr = np.zeros((nsteps, self.ne, self.nw, TRACE_FIELDS)) if trace else None
+        lib().orc_vmc_sweeps_philox(self.h, seed, sweep0, nsteps, tau, int(use_drift), C.byref(na), C.byref(nr),
+                                    _ptr(tr) if tr is not None else None)
+        return na.value, nr.value, tr
+
+    def replay(self, trace_in):
+        """Follow a recorded trajectory (proposed positions and decisions of trace_in
+        [nsteps][ne][nw][12]); returns this crowd's records on the same moves."""
+        ti = _d(trace_in)
+        assert ti.shape[1:] == (self.ne, self.nw, TRACE_FIELDS)
+        to = np.zeros_like(ti)
+        lib().orc_replay_trace(self.h, ti.shape[0], _ptr(ti), _ptr(to))
+        return to
+
+    def replay_philox(self, trace_in, seed: int, tau: float, use_drift: bool = True, sweep0: int = 0,
+                      dmc: bool = False):
+        """Follow a recorded trajectory on the counter-based stream and form, at every move,
+        this crowd's own proposal, ratio, gradients and decision from the shared state:
+        (trace_out with TR_POS = own proposal, TR_ACCEPT = own decision and TR_SELF = tau |xi|^2,
+        margin (u - P) / P).  dmc: fixed-node moves (a sign change of psi is rejected)."""
+        ti = _d(trace_in)
+        assert ti.shape[1:] == (self.ne, self.nw, TRACE_FIELDS)
+        to = np.zeros_like(ti)
+        margin = np.zeros(ti.shape[:3])
+        lib().orc_replay_trace_philox(self.h, seed, sweep0, ti.shape[0], tau, int(use_drift), int(dmc), _ptr(ti),
+                                      _ptr(to), _ptr(margin))
+        return to, margin
+
+    def copy_walkers(self, src):
+        """Walker i takes the state of walker src[i] (population control)."""
+        a = np.ascontiguousarray(src, np.int32)
+        lib().orc_copy_walkers(self.h, _ptr(a, _ip))
 
     def kinetic(self, with_gl: bool = False):
         """Kinetic energy per walker from the tracked state (call complete_updates first);

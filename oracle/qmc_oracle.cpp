@@ -76,6 +76,73 @@ struct Rng
 };
 
 // ---------------------------------------------------------------------------
+// The counter-based stream of the device sweeps (no reference counterpart: the
+// reference draws from mt19937 on the host).  Philox4x32-10 as published by
+// Salmon, Moraes, Dror and Shaw (SC'11, "Parallel random numbers: as easy as
+// 1, 2, 3"): ten rounds of two 32x32->64 multiplies with the Weyl key schedule.
+// Counter (walker, electron, sweep, j) under the key (seed low, seed high):
+// j = 0, 1 give four uniforms for the Box-Muller Gaussians of the proposal
+// (pairs as in assignGaussRand, RandomSeqGenerator.h:33-51), j = 2 the uniform of
+// the acceptance test.  A uniform is 53 bits of two words, in [0, 1).
+// ---------------------------------------------------------------------------
+struct P4
+{
+  uint32_t x, y, z, w;
+};
+
+inline P4 philox4x32_10(P4 c, uint32_t k0, uint32_t k1)
+{
+  for (int r = 0; r < 10; r++)
+  {
+    const uint64_t p0 = static_cast<uint64_t>(0xD2511F53u) * c.x;
+    const uint64_t p1 = static_cast<uint64_t>(0xCD9E8D57u) * c.z;
+    const uint32_t hi0 = static_cast<uint32_t>(p0 >> 32), lo0 = static_cast<uint32_t>(p0);
+    const uint32_t hi1 = static_cast<uint32_t>(p1 >> 32), lo1 = static_cast<uint32_t>(p1);
+    c = P4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+inline double philox_u01(uint32_t a, uint32_t b)
+{
+  const uint64_t v = (static_cast<uint64_t>(a) << 21) ^ static_cast<uint64_t>(b >> 11);
+  return static_cast<double>(v & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0);
+}
+
+struct PhiloxStream
+{
+  uint32_t k0, k1;
+  explicit PhiloxStream(uint64_t seed) : k0(static_cast<uint32_t>(seed)), k1(static_cast<uint32_t>(seed >> 32)) {}
+  // three unit Gaussians of the proposal of electron iat of walker w in sweep `sweep`
+  void gauss3(uint32_t w, uint32_t iat, uint32_t sweep, double out[3]) const
+  {
+    const P4 r0 = philox4x32_10(P4{w, iat, sweep, 0u}, k0, k1);
+    const P4 r1 = philox4x32_10(P4{w, iat, sweep, 1u}, k0, k1);
+    const double one_m = 1.0 - std::numeric_limits<double>::epsilon();
+    const double t1    = std::sqrt(-2.0 * std::log(1.0 - one_m * philox_u01(r0.x, r0.y)));
+    const double t2    = 2.0 * M_PI * philox_u01(r0.z, r0.w);
+    const double t3    = std::sqrt(-2.0 * std::log(1.0 - one_m * philox_u01(r1.x, r1.y)));
+    const double t4    = 2.0 * M_PI * philox_u01(r1.z, r1.w);
+    out[0]             = t1 * std::cos(t2);
+    out[1]             = t1 * std::sin(t2);
+    out[2]             = t3 * std::cos(t4);
+  }
+  double uniform(uint32_t w, uint32_t iat, uint32_t sweep) const
+  {
+    const P4 r2 = philox4x32_10(P4{w, iat, sweep, 2u}, k0, k1);
+    return philox_u01(r2.x, r2.y);
+  }
+};
+
+// fields of one move record (the layout of the library's move trace)
+enum : int
+{
+  TR_POS = 0, TR_RATIO = 3, TR_GRAD_NEW = 4, TR_GRAD_NOW = 7, TR_ACCEPT = 10, TR_SELF = 11, TRACE_FIELDS = 12
+};
+
+// ---------------------------------------------------------------------------
 // getSplineBound (src/Numerics/SplineBound.hpp:36-61)
 // ---------------------------------------------------------------------------
 template<typename T>
@@ -408,12 +475,7 @@ struct DelayEngine
     if (dc == 0)
       return;
     for (int c = 0; c < dc; c++)
-    {
-      T s = 0;
-      for (int j = 0; j < n; j++)
-        s += U[(size_t)c * n + j] * invRow[j];
-      p[c] = s;
-    }
+      p[c] = dot(U.data() + (size_t)c * n, invRow.data(), n);
     T* brow = Binv.data() + (size_t)dc * k;
     for (int i = 0; i < dc; i++)
     {
@@ -422,12 +484,12 @@ struct DelayEngine
         s += Binv[(size_t)c * k + i] * p[c];
       brow[i] = -s;
     }
-    for (int j = 0; j < n; j++)
+    for (int c = 0; c < dc; c++)
     {
-      T s = 0;
-      for (int c = 0; c < dc; c++)
-        s += V[(size_t)c * n + j] * brow[c];
-      invRow[j] += s;
+      const T b     = brow[c];
+      const T* vrow = V.data() + (size_t)c * n;
+      for (int j = 0; j < n; j++)
+        invRow[j] += vrow[j] * b;
     }
   }
   // mw_accept_rejectRow for one walker (DelayedUpdateBatched.h:542-670 and
@@ -438,12 +500,7 @@ struct DelayEngine
     if (accepted)
     {
       for (int c = 0; c < dc; c++)
-      {
-        T s = 0;
-        for (int j = 0; j < n; j++)
-          s += V[(size_t)c * n + j] * phi[j];
-        p[c] = -s;
-      }
+        p[c] = -dot(V.data() + (size_t)c * n, phi, n);
       const T sigma = T(1) / ratio;
       // y = sigma * Binv * p  -> column dc
       for (int i = 0; i < dc; i++)
@@ -472,7 +529,10 @@ struct DelayEngine
       delay_list[dc]            = -1;
     }
   }
-  // mw_updateInvMat (DelayedUpdateBatched.h:675-738): Ainv -= (Ainv U^T - E) (Binv V)
+  // mw_updateInvMat (DelayedUpdateBatched.h:675-738; the CPU engine's three GEMMs,
+  // DelayedUpdate.h:145-215): Ainv -= (Ainv U^T - E) (Binv V).  Loop orders keep every
+  // inner loop contiguous (dot products with eight partial sums, row updates as axpy)
+  // so the compiler vectorises them as a BLAS would.
   void update_inv(T* Ainv, int dc)
   {
     if (dc == 0)
@@ -480,34 +540,46 @@ struct DelayEngine
     // tempMat[j][c] = sum_i Ainv[j][i] U[c][i]
     for (int j = 0; j < n; j++)
       for (int c = 0; c < dc; c++)
-      {
-        T s = 0;
-        for (int i = 0; i < n; i++)
-          s += Ainv[(size_t)j * n + i] * U[(size_t)c * n + i];
-        tempMat[(size_t)j * k + c] = s;
-      }
+        tempMat[(size_t)j * k + c] = dot(Ainv + (size_t)j * n, U.data() + (size_t)c * n, n);
     for (int c = 0; c < dc; c++)
       if (delay_list[c] >= 0)
         tempMat[(size_t)delay_list[c] * k + c] -= T(1);
     // W = Binv V  (stored in U, k x n)
-    std::vector<T> W((size_t)dc * n);
+    std::vector<T> W((size_t)dc * n, T(0));
     for (int l = 0; l < dc; l++)
-      for (int i = 0; i < n; i++)
+      for (int c = 0; c < dc; c++)
       {
-        T s = 0;
-        for (int c = 0; c < dc; c++)
-          s += Binv[(size_t)l * k + c] * V[(size_t)c * n + i];
-        W[(size_t)l * n + i] = s;
+        const T b     = Binv[(size_t)l * k + c];
+        const T* vrow = V.data() + (size_t)c * n;
+        T* wrow       = W.data() + (size_t)l * n;
+        for (int i = 0; i < n; i++)
+          wrow[i] += b * vrow[i];
       }
     std::copy(W.begin(), W.end(), U.begin());
     for (int j = 0; j < n; j++)
-      for (int i = 0; i < n; i++)
+    {
+      T* arow = Ainv + (size_t)j * n;
+      for (int l = 0; l < dc; l++)
       {
-        T s = 0;
-        for (int l = 0; l < dc; l++)
-          s += tempMat[(size_t)j * k + l] * U[(size_t)l * n + i];
-        Ainv[(size_t)j * n + i] -= s;
+        const T t     = tempMat[(size_t)j * k + l];
+        const T* wrow = U.data() + (size_t)l * n;
+        for (int i = 0; i < n; i++)
+          arow[i] -= t * wrow[i];
       }
+    }
+  }
+  // sum_i a[i] b[i] with eight independent partial sums
+  static T dot(const T* a, const T* b, int n)
+  {
+    T acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int i = 0;
+    for (; i + 8 <= n; i += 8)
+      for (int q = 0; q < 8; q++)
+        acc[q] += a[i + q] * b[i + q];
+    T s = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+    for (; i < n; i++)
+      s += a[i] * b[i];
+    return s;
   }
 };
 
@@ -969,6 +1041,23 @@ struct Crowd
     }
   }
 
+  // ParticleSet::mw_makeMove with the proposed positions given directly
+  void make_move_to(int iat, const double* pos /*[nw][3]*/)
+  {
+#pragma omp parallel for schedule(static)
+    for (int iw = 0; iw < nw; iw++)
+    {
+      Walker& wk = w[iw];
+      for (int dd = 0; dd < 3; dd++)
+        wk.active_pos[dd] = pos[iw * 3 + dd];
+      ee_row(wk, wk.active_pos, wk.new_r.data(), wk.new_dr.data());
+      ee_row(wk, &wk.R[(size_t)iat * 3], wk.old_r.data(), wk.old_dr.data());
+      wk.old_r[iat] = std::numeric_limits<T>::max();
+      if (nions > 0)
+        ei_row(wk.active_pos, wk.ei_r.data(), wk.ei_dr.data());
+    }
+  }
+
   // ---------------- TrialWaveFunction::mw_calcRatioGrad --------------------
   // component order: determinant, J1, J2; ratios multiplied, grads summed
   // (TrialWaveFunction.cpp:685-772).
@@ -1161,7 +1250,12 @@ struct Crowd
           }
         }
         else
+        {
+          // the up-to-date inverse row of iat is formed here for the ratio (mw_getInvRow)
+          if (delay > 1)
+            eval_grad(iat, grads_now.data());
           std::copy_n(dl, (size_t)nw * 3, drift.data());
+        }
         make_move(iat, drift.data());
         if (use_drift)
         {
@@ -1206,6 +1300,207 @@ struct Crowd
     complete_updates();
   }
 };
+
+// ---------------------------------------------------------------------------
+// Sweeps on the counter-based stream, electron by electron as
+// VMCBatched::advanceWalkers (VMCBatched.cpp:106-177), one record per move in
+// trace [ne][nw][TRACE_FIELDS] (may be null).  Every walker draws its own numbers,
+// so the acceptance uniform of walker w does not depend on the other walkers.
+// ---------------------------------------------------------------------------
+template<typename T>
+void sweep_philox(Crowd<T>& c, const PhiloxStream& ps, uint32_t sweep, double tau, bool use_drift, long* n_accept,
+                  long* n_reject, double* trace)
+{
+  const int nw = c.nw, ne = c.ne;
+  const double sqrttau = std::sqrt(tau), oneover2tau = 0.5 / tau;
+  std::vector<double> grads_now((size_t)nw * 3), grads_new((size_t)nw * 3), drift((size_t)nw * 3), dl((size_t)nw * 3);
+  std::vector<double> ratios(nw), log_gf(nw), log_gb(nw);
+  std::vector<int> acc(nw);
+  const double eps = std::numeric_limits<T>::epsilon();
+  for (int iat = 0; iat < ne; iat++)
+  {
+    for (int iw = 0; iw < nw; iw++)
+    {
+      double g[3];
+      ps.gauss3((uint32_t)iw, (uint32_t)iat, sweep, g);
+      for (int k = 0; k < 3; k++)
+        dl[iw * 3 + k] = g[k] * sqrttau;
+    }
+    c.eval_grad(iat, grads_now.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      if (use_drift)
+      {
+        Crowd<T>::unr_drift(tau, &grads_now[iw * 3], &drift[iw * 3]);
+        for (int k = 0; k < 3; k++)
+          drift[iw * 3 + k] += dl[iw * 3 + k];
+      }
+      else
+        for (int k = 0; k < 3; k++)
+          drift[iw * 3 + k] = dl[iw * 3 + k];
+    }
+    c.make_move(iat, drift.data());
+    c.ratio_grad(iat, ratios.data(), grads_new.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      log_gf[iw] = log_gb[iw] = 0.0;
+      if (use_drift)
+      {
+        const double* d = &dl[iw * 3];
+        log_gf[iw]      = -oneover2tau * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        double dr[3];
+        Crowd<T>::unr_drift(tau, &grads_new[iw * 3], dr);
+        for (int k = 0; k < 3; k++)
+          dr[k] += drift[iw * 3 + k];
+        log_gb[iw] = -oneover2tau * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+      }
+      const double prob = ratios[iw] * ratios[iw];
+      acc[iw] = (prob >= eps && ps.uniform((uint32_t)iw, (uint32_t)iat, sweep) < prob * std::exp(log_gb[iw] - log_gf[iw]))
+          ? 1
+          : 0;
+      if (acc[iw])
+        (*n_accept)++;
+      else
+        (*n_reject)++;
+      if (trace)
+      {
+        double* tr = trace + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+        for (int k = 0; k < 3; k++)
+        {
+          tr[TR_POS + k]      = c.w[iw].active_pos[k];
+          tr[TR_GRAD_NEW + k] = grads_new[iw * 3 + k];
+          tr[TR_GRAD_NOW + k] = grads_now[iw * 3 + k];
+        }
+        tr[TR_RATIO]  = ratios[iw];
+        tr[TR_ACCEPT] = acc[iw];
+        tr[TR_SELF]   = 1.0;
+      }
+    }
+    c.accept_reject(iat, acc.data());
+  }
+  c.complete_updates();
+}
+
+// ---------------------------------------------------------------------------
+// Replay of a recorded trajectory: for every move the proposed positions and the
+// decisions of trace_in [ne][nw][TRACE_FIELDS] (from any implementation), this
+// crowd's own gradients and ratios on those positions into trace_out (same layout).
+// ---------------------------------------------------------------------------
+template<typename T>
+void replay(Crowd<T>& c, const double* trace_in, double* trace_out)
+{
+  const int nw = c.nw, ne = c.ne;
+  std::vector<double> pos((size_t)nw * 3), gnow((size_t)nw * 3), gnew((size_t)nw * 3), ratios(nw);
+  std::vector<int> acc(nw);
+  for (int iat = 0; iat < ne; iat++)
+  {
+    c.eval_grad(iat, gnow.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      const double* tr = trace_in + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+      for (int k = 0; k < 3; k++)
+        pos[iw * 3 + k] = tr[TR_POS + k];
+      acc[iw] = tr[TR_ACCEPT] != 0.0 ? 1 : 0;
+    }
+    c.make_move_to(iat, pos.data());
+    c.ratio_grad(iat, ratios.data(), gnew.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      double* o = trace_out + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+      for (int k = 0; k < 3; k++)
+      {
+        o[TR_POS + k]      = pos[iw * 3 + k];
+        o[TR_GRAD_NEW + k] = gnew[iw * 3 + k];
+        o[TR_GRAD_NOW + k] = gnow[iw * 3 + k];
+      }
+      o[TR_RATIO]  = ratios[iw];
+      o[TR_ACCEPT] = acc[iw];
+      o[TR_SELF]   = 1.0;
+    }
+    c.accept_reject(iat, acc.data());
+  }
+  c.complete_updates();
+}
+
+// ---------------------------------------------------------------------------
+// Step-by-step check of a recorded trajectory on the counter-based stream.  The
+// state follows trace_in (its proposed positions and decisions); at every move this
+// crowd also forms, independently, what the driver step would do from that state:
+// the gradient at R, its own proposal r + drift(R) + sqrt(tau) xi with the stream's
+// Gaussians, the ratio and gradient at the recorded R', and its own decision with
+// the stream's uniform, u < |ratio|^2 exp(log_gb - log_gf) (VMCBatched.cpp:125-158).
+// trace_out gets those (TR_POS = its own proposal, TR_ACCEPT = its own decision);
+// margin [ne][nw] = (u - P) / P, the relative distance of the decision from a tie;
+// TR_SELF of trace_out carries tau |xi|^2 of the move.  dmc: fixed-node moves.
+// ---------------------------------------------------------------------------
+template<typename T>
+void replay_philox(Crowd<T>& c, const PhiloxStream& ps, uint32_t sweep, double tau, bool use_drift, bool dmc,
+                   const double* trace_in, double* trace_out, double* margin)
+{
+  const int nw = c.nw, ne = c.ne;
+  const double sqrttau = std::sqrt(tau), oneover2tau = 0.5 / tau;
+  const double eps = std::numeric_limits<T>::epsilon();
+  std::vector<double> pos((size_t)nw * 3), gnow((size_t)nw * 3), gnew((size_t)nw * 3), ratios(nw);
+  std::vector<int> acc(nw);
+  for (int iat = 0; iat < ne; iat++)
+  {
+    c.eval_grad(iat, gnow.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      const double* tr = trace_in + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+      double* o        = trace_out + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+      double xi[3], drift[3] = {0, 0, 0};
+      ps.gauss3((uint32_t)iw, (uint32_t)iat, sweep, xi);
+      // tau |xi|^2 of the move (DMCBatched.cpp:165-167): the DMC r^2 of the step
+      o[TR_SELF] = tau * (xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2]);
+      if (use_drift)
+        Crowd<T>::unr_drift(tau, &gnow[iw * 3], drift);
+      for (int k = 0; k < 3; k++)
+      {
+        o[TR_POS + k]      = c.w[iw].R[(size_t)iat * 3 + k] + (drift[k] + xi[k] * sqrttau);
+        o[TR_GRAD_NOW + k] = gnow[iw * 3 + k];
+        pos[iw * 3 + k]    = tr[TR_POS + k];
+      }
+      acc[iw] = tr[TR_ACCEPT] != 0.0 ? 1 : 0;
+    }
+    c.make_move_to(iat, pos.data());
+    c.ratio_grad(iat, ratios.data(), gnew.data());
+    for (int iw = 0; iw < nw; iw++)
+    {
+      double* o = trace_out + ((size_t)iat * nw + iw) * TRACE_FIELDS;
+      double log_gf = 0, log_gb = 0;
+      if (use_drift)
+      {
+        // the recorded displacement, split into drift at R and diffusion
+        double dnow[3], dnew[3], disp[3], delta[3];
+        Crowd<T>::unr_drift(tau, &gnow[iw * 3], dnow);
+        Crowd<T>::unr_drift(tau, &gnew[iw * 3], dnew);
+        for (int k = 0; k < 3; k++)
+        {
+          disp[k]  = pos[iw * 3 + k] - c.w[iw].R[(size_t)iat * 3 + k];
+          delta[k] = disp[k] - dnow[k];
+          dnew[k] += disp[k];
+        }
+        log_gf = -oneover2tau * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2]);
+        log_gb = -oneover2tau * (dnew[0] * dnew[0] + dnew[1] * dnew[1] + dnew[2] * dnew[2]);
+      }
+      const double P = ratios[iw] * ratios[iw] * std::exp(log_gb - log_gf);
+      const double u = ps.uniform((uint32_t)iw, (uint32_t)iat, sweep);
+      // DMC: a move that changes the sign of psi is rejected (SFNBranch::phaseChanged
+      // for a real ratio, DMCBatched.cpp:203-215)
+      const bool phase_ok = !dmc || ratios[iw] > 0;
+      const int own       = (phase_ok && ratios[iw] * ratios[iw] >= eps && u < P) ? 1 : 0;
+      for (int k = 0; k < 3; k++)
+        o[TR_GRAD_NEW + k] = gnew[iw * 3 + k];
+      o[TR_RATIO]  = ratios[iw];
+      o[TR_ACCEPT] = own;
+      if (margin)
+        margin[(size_t)iat * nw + iw] = (u - P) / std::max(P, 1e-300);
+    }
+    c.accept_reject(iat, acc.data());
+  }
+  c.complete_updates();
+}
 
 template<typename T>
 Crowd<T>* make_crowd(int n_up, int n_dn, int norb, int npad, const double lattice[3], int n_ions, const double* ion_pos,
@@ -1503,6 +1798,65 @@ void orc_vmc_sweeps(void* hv, void* rng, int nsteps, double tau, int use_drift, 
     for (int s = 0; s < nsteps; s++)
       c->sweep(*r, tau, use_drift != 0, n_accept, n_reject,
                accept_log ? accept_log + (size_t)s * c->ne * c->nw : nullptr);
+  });
+}
+
+// ---- sweeps on the counter-based stream of the device (Philox4x32-10) --------
+// sweeps sweep0, sweep0 + 1, ...; trace [nsteps][ne][nw][TRACE_FIELDS] or null
+void orc_vmc_sweeps_philox(void* hv, uint64_t seed, unsigned sweep0, int nsteps, double tau, int use_drift,
+                           long* n_accept, long* n_reject, double* trace)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  const orc::PhiloxStream ps(seed);
+  dispatch(h, [&](auto* c) {
+    for (int s = 0; s < nsteps; s++)
+      orc::sweep_philox(*c, ps, sweep0 + (unsigned)s, tau, use_drift != 0, n_accept, n_reject,
+                        trace ? trace + (size_t)s * c->ne * c->nw * orc::TRACE_FIELDS : nullptr);
+  });
+}
+
+// replay of nsteps recorded sweeps: trace_in, trace_out [nsteps][ne][nw][TRACE_FIELDS]
+void orc_replay_trace(void* hv, int nsteps, const double* trace_in, double* trace_out)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  dispatch(h, [&](auto* c) {
+    const size_t per = (size_t)c->ne * c->nw * orc::TRACE_FIELDS;
+    for (int s = 0; s < nsteps; s++)
+      orc::replay(*c, trace_in + s * per, trace_out + s * per);
+  });
+}
+
+// step-by-step check of nsteps recorded sweeps (sweep indices sweep0, sweep0 + 1, ...):
+// trace_in, trace_out [nsteps][ne][nw][TRACE_FIELDS], margin [nsteps][ne][nw] or null
+void orc_replay_trace_philox(void* hv, uint64_t seed, unsigned sweep0, int nsteps, double tau, int use_drift, int dmc,
+                             const double* trace_in, double* trace_out, double* margin)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  const orc::PhiloxStream ps(seed);
+  dispatch(h, [&](auto* c) {
+    const size_t nrec = (size_t)c->ne * c->nw, per = nrec * orc::TRACE_FIELDS;
+    for (int s = 0; s < nsteps; s++)
+      orc::replay_philox(*c, ps, sweep0 + (unsigned)s, tau, use_drift != 0, dmc != 0, trace_in + s * per,
+                         trace_out + s * per, margin ? margin + s * nrec : nullptr);
+  });
+}
+
+// population control: walker i takes the state of walker src[i] (Walker::makeCopy);
+// call after complete_updates
+void orc_copy_walkers(void* hv, const int* src)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  dispatch(h, [&](auto* c) {
+    auto old = c->w;
+    auto dg  = c->dgrad;
+    auto dl  = c->dlap;
+    const size_t gpw = (size_t)2 * c->norb * 3 * c->norb, lpw = (size_t)2 * c->norb * c->norb;
+    for (int i = 0; i < c->nw; i++)
+    {
+      c->w[i] = old[src[i]];
+      std::copy_n(dg.begin() + src[i] * gpw, gpw, c->dgrad.begin() + i * gpw);
+      std::copy_n(dl.begin() + src[i] * lpw, lpw, c->dlap.begin() + i * lpw);
+    }
   });
 }
 

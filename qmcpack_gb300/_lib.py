@@ -23,7 +23,10 @@ EXPORTS = [
     "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
     "qmcg_proposal_backward", "qmcg_proposal_features", "qmcg_vmc_sweeps_learned",
     "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info", "qmcg_crowd_set_threads",
+    "qmcg_mw_evaluate_gl", "qmcg_vmc_sweeps_trace", "qmcg_profile_recompute",
+    "qmcg_dmc_init", "qmcg_dmc_step", "qmcg_dmc_copy_walkers", "qmcg_dmc_comb", "qmcg_dmc_reconfigure",
 ]
+TRACE_FIELDS = 12
 PROPOSAL_NUM_PARAMS = 43408
 _fp = C.POINTER(C.c_float)
 
@@ -42,6 +45,11 @@ class SystemDesc(C.Structure):
 class SweepParams(C.Structure):
     _fields_ = [("tau", C.c_double), ("use_drift", C.c_int), ("rng_mode", C.c_int), ("seed", C.c_uint64),
                 ("recompute_every", C.c_int), ("path", C.c_int), ("flush", C.c_int)]
+
+
+class BranchParams(C.Structure):
+    _fields_ = [("e_trial", C.c_double), ("e_ref", C.c_double), ("tau_eff", C.c_double),
+                ("branch_cutoff", C.c_double), ("branch_max", C.c_double)]
 
 
 class SweepStats(C.Structure):
@@ -109,6 +117,15 @@ def load(path: str = LIB_PATH):
         "qmcg_group_sweeps": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats)],
         "qmcg_group_info": [vp, _ip],
         "qmcg_crowd_set_threads": [vp, C.c_int],
+        "qmcg_mw_evaluate_gl": [vp, _dp, _dp, _dp],
+        "qmcg_vmc_sweeps_trace": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats), _dp],
+        "qmcg_profile_recompute": [vp, _dp],
+        "qmcg_dmc_init": [vp, _dp],
+        "qmcg_dmc_step": [vp, C.POINTER(SweepParams), C.POINTER(BranchParams), _dp, _dp, _ip, _dp,
+                          C.POINTER(SweepStats), _dp],
+        "qmcg_dmc_copy_walkers": [vp, _ip],
+        "qmcg_dmc_comb": [C.c_int, _dp, C.c_double, _ip, _ip],
+        "qmcg_dmc_reconfigure": [vp, C.c_double, _ip],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

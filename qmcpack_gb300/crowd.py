@@ -14,7 +14,7 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from ._lib import QmcgError, SweepParams, SweepStats, SystemDesc, check
+from ._lib import BranchParams, QmcgError, SweepParams, SweepStats, SystemDesc, check
 from .system import System
 
 _dp = C.POINTER(C.c_double)
@@ -179,6 +179,63 @@ class Crowd:
         self.last_repaired = st.repaired
         return st.accepted, st.rejected, acc
 
+    def mw_evaluateGL(self):
+        """(log|psi| [nw], G [nw][ne][3], L [nw][ne]) from the tracked state (after mw_completeUpdates)."""
+        lp = np.zeros(self.nw)
+        G = np.zeros((self.nw, self.ne, 3))
+        L = np.zeros((self.nw, self.ne))
+        check(self.L.qmcg_mw_evaluate_gl(self.handle, _p(lp), _p(G), _p(L)))
+        return lp, G, L
+
+    def vmc_sweeps_trace(self, nsweeps: int, tau: float, seed: int, use_drift: bool = True, recompute_every: int = 0,
+                         flush: int = 0):
+        """Walker-resident sweeps with one record per move: (accepted, rejected,
+        trace [nsweeps][ne][nw][TRACE_FIELDS]); fields as QMCG_TRACE_FIELDS in the header."""
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
+                        recompute_every=recompute_every, path=0, flush=flush)
+        st = SweepStats()
+        tr = np.zeros((nsweeps, self.ne, self.nw, _lib.TRACE_FIELDS))
+        check(self.L.qmcg_vmc_sweeps_trace(self.handle, C.byref(p), nsweeps, C.byref(st), _p(tr)))
+        self.last_repaired = st.repaired
+        return st.accepted, st.rejected, tr
+
+    # ---- diffusion Monte Carlo
+    def dmc_init(self):
+        """Weights 1, ages 0; returns the local energy of every walker (the first E_old)."""
+        el = np.zeros(self.nw)
+        check(self.L.qmcg_dmc_init(self.handle, _p(el)))
+        return el
+
+    def dmc_step(self, tau: float, seed: int, e_trial: float, e_ref: float, tau_eff: float, branch_cutoff: float,
+                 branch_max: float, use_drift: bool = True, recompute_every: int = 0, flush: int = 0,
+                 trace: bool = False):
+        """One fixed-node DMC step with branch weights: dict of weights [nw], e_local [nw],
+        age [nw], sums [5] (sum w, sum w E, sum w E^2, sum r2 accepted, sum r2 proposed),
+        accepted, rejected and the move trace (if asked)."""
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
+                        recompute_every=recompute_every, path=0, flush=flush)
+        b = BranchParams(e_trial=e_trial, e_ref=e_ref, tau_eff=tau_eff, branch_cutoff=branch_cutoff,
+                         branch_max=branch_max)
+        w, el, sums = np.zeros(self.nw), np.zeros(self.nw), np.zeros(5)
+        age = np.zeros(self.nw, np.int32)
+        st = SweepStats()
+        tr = np.zeros((1, self.ne, self.nw, _lib.TRACE_FIELDS)) if trace else None
+        check(self.L.qmcg_dmc_step(self.handle, C.byref(p), C.byref(b), _p(w), _p(el), _p(age, _ip), _p(sums),
+                                   C.byref(st), _p(tr) if tr is not None else None))
+        self.last_repaired = st.repaired
+        return {"weights": w, "e_local": el, "age": age, "sums": sums, "accepted": st.accepted,
+                "rejected": st.rejected, "trace": tr}
+
+    def dmc_copy_walkers(self, src):
+        a = np.ascontiguousarray(np.asarray(src, dtype=np.int32).reshape(self.nw))
+        check(self.L.qmcg_dmc_copy_walkers(self.handle, _p(a, _ip)))
+
+    def dmc_reconfigure(self, u: float):
+        """Comb of the current weights (fixed walker count) and the device copies; returns the sources."""
+        src = np.zeros(self.nw, np.int32)
+        check(self.L.qmcg_dmc_reconfigure(self.handle, float(u), _p(src, _ip)))
+        return src
+
     def mw_evaluate_local_energy(self):
         """(E_L, kinetic, potential) per walker; needs all delayed updates completed."""
         el, ke, vp = np.zeros(self.nw), np.zeros(self.nw), np.zeros(self.nw)
@@ -272,10 +329,26 @@ class Crowd:
         check(self.L.qmcg_profile_sweep(self.handle, nsweeps, _p(out)))
         return float(out[0]), float(out[1]), int(out[2]), int(out[3])
 
+    def profile_recompute(self) -> float:
+        """Device ms of one periodic FP64 recompute of every walker."""
+        ms = C.c_double()
+        check(self.L.qmcg_profile_recompute(self.handle, C.byref(ms)))
+        return ms.value
+
     def stream(self) -> int:
         p = C.c_void_p()
         check(self.L.qmcg_crowd_stream(self.handle, C.byref(p)))
         return p.value or 0
+
+
+def dmc_comb(weights, u: float):
+    """Population control with a fixed walker count (no GPU needed): (sources, walkers kept)."""
+    w = np.ascontiguousarray(weights, np.float64)
+    src = np.zeros(w.size, np.int32)
+    kept = C.c_int()
+    L = _lib.load()
+    check(L.qmcg_dmc_comb(w.size, _p(w), float(u), _p(src, _ip), C.byref(kept)))
+    return src, kept.value
 
 
 def group_seed(seed: int, index: int) -> int:

@@ -468,7 +468,71 @@ struct qmcg_crowd_s
   virtual int sweeps_learned(const qmcg_sweep_params* p, int n, int train, double lr, double* el,
                              qmcg_sweep_stats* st, double* tstats) = 0;
   virtual int sweeps_measure(const qmcg_sweep_params* p, int n, double* el, double* ke, qmcg_sweep_stats* st) = 0;
+  virtual int sweeps_trace(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, double* trace) = 0;
+  virtual int evaluate_gl(double* lp, double* grads, double* laps) = 0;
+  virtual int profile_recompute(double* ms) = 0;
+  virtual int dmc_init(double* el) = 0;
+  virtual int dmc_step(const qmcg_sweep_params* p, const qmcg_branch_params* b, double* w, double* el, int* age,
+                       double* sums, qmcg_sweep_stats* st, double* trace) = 0;
+  virtual int dmc_copy(const int* src) = 0;
+  virtual int dmc_reconfigure(double u, int* src) = 0;
 };
+
+// The comb of population control with a fixed walker count
+// (WalkerReconfiguration::getIndexPermutation, WalkerReconfiguration.cpp:30-107): nw
+// teeth at W (u + i) / nw, W = sum |w|, u in [0, 1); walker iw gets one copy per tooth in
+// [sum_{j<iw} |w_j|, sum_{j<=iw} |w_j|).  Slots of walkers with no copy take the extra
+// copies of the others in order; every other slot keeps its walker.  Returns the number
+// of walkers with at least one copy.
+static int comb_sources(int nw, const double* weights, double u, int* src)
+{
+  double wtot = 0;
+  for (int iw = 0; iw < nw; iw++)
+    wtot += std::fabs(weights[iw]);
+  std::vector<double> zeta(nw + 1);
+  const double nw_inv = 1.0 / static_cast<double>(nw), dstep = u * nw_inv;
+  for (int iw = 0; iw < nw; iw++)
+    zeta[iw] = wtot * (dstep + static_cast<double>(iw) * nw_inv);
+  zeta[nw] = wtot + 1.0;
+  std::vector<int> plus, minus;
+  int ind = 0, kept = 0;
+  double wcur = 0;
+  for (int iw = 0; iw < nw; iw++)
+  {
+    const double tryp = wcur + std::fabs(weights[iw]);
+    int ni            = 0;
+    while (zeta[ind] < tryp && zeta[ind] >= wcur)
+    {
+      ind++;
+      ni++;
+    }
+    wcur += std::fabs(weights[iw]);
+    kept += ni ? 1 : 0;
+    if (ni > 1)
+      plus.insert(plus.end(), ni - 1, iw);
+    else if (ni == 0)
+      minus.push_back(iw);
+    src[iw] = iw;
+  }
+  // a tooth lost to rounding at the end of the comb leaves a walker without a copy in its slot
+  const size_t ncopy = std::min(plus.size(), minus.size());
+  for (size_t i = 0; i < ncopy; i++)
+    src[minus[i]] = plus[i];
+  return kept;
+}
+
+extern "C" int qmcg_dmc_comb(int nw, const double* weights, double u, int* src, int* num_kept)
+{
+  if (nw <= 0 || !weights || !src || !(u >= 0.0 && u < 1.0))
+    return fail(QMCG_ERR_ARG, "need num_walkers > 0, weights, src and 0 <= u < 1");
+  for (int i = 0; i < nw; i++)
+    if (!std::isfinite(weights[i]))
+      return fail(QMCG_ERR_ARG, "non-finite walker weight");
+  const int kept = comb_sources(nw, weights, u, src);
+  if (num_kept)
+    *num_kept = kept;
+  return QMCG_OK;
+}
 
 template<typename T>
 struct Crowd final : qmcg_crowd_s
@@ -515,6 +579,25 @@ struct Crowd final : qmcg_crowd_s
     float g_lr = 0;
   } ln;
   EwaldDev<T> ew{};
+  double* trace_d = nullptr; // [ne][nw][TRACE_FIELDS] move records of a traced resident sweep
+  // diffusion Monte Carlo: weights, previous local energies, ages, branch parameters,
+  // ensemble sums, the branch kernel's copy of the weights, population-control sources
+  struct Dmc
+  {
+    bool ready     = false;
+    double* weight = nullptr;
+    double* e_old  = nullptr;
+    int* age       = nullptr;
+    double* par    = nullptr; // [5]
+    double* sums   = nullptr; // [5]
+    double* w_out  = nullptr;
+    int* src       = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int g_drift = -1, g_flush = -1, g_nt = -1;
+    double g_tau   = 0;
+    uint64_t g_seed = 0;
+  } dm;
+  double* gl_d    = nullptr; // [nw][ne][4] per-electron gradient and Laplacian of log psi
   double* e_out  = nullptr; // [3][nw] local energy, kinetic, potential
   double* e_hist = nullptr; // [e_hist_cap][2][nw] per-sweep local and kinetic energies
   size_t e_hist_cap = 0;
@@ -531,6 +614,8 @@ struct Crowd final : qmcg_crowd_s
       cudaFree(e_hist);
     if (ln.graph)
       cudaGraphExecDestroy(ln.graph);
+    if (dm.graph)
+      cudaGraphExecDestroy(dm.graph);
     if (stream)
       cudaStreamDestroy(stream);
   }
@@ -1046,6 +1131,261 @@ struct Crowd final : qmcg_crowd_s
     return run_sweeps(p, n, st, acc_log, false);
   }
 
+  // one sweep of the walker-resident path launched outside the graph with the move
+  // record switched on; trace_h [ne][nw][TRACE_FIELDS] and acc_log [ne][nw] may be null
+  int resident_traced_sweep(double* trace_h, int* acc_log)
+  {
+    const size_t nrec = (size_t)sys->ne * nw;
+    if (!trace_d)
+      CUDA_TRY(mem.alloc(&trace_d, nrec * TRACE_FIELDS));
+    s.trace = trace_d;
+    const int rc = enqueue_sweep_resident();
+    s.trace = nullptr;
+    if (rc)
+      return rc;
+    std::vector<double> h;
+    double* dst = trace_h;
+    if (!dst)
+    {
+      h.resize(nrec * TRACE_FIELDS);
+      dst = h.data();
+    }
+    CUDA_TRY(cudaMemcpyAsync(dst, trace_d, nrec * TRACE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (acc_log)
+      for (size_t r = 0; r < nrec; r++)
+        acc_log[r] = dst[r * TRACE_FIELDS + TR_ACCEPT] != 0.0 ? 1 : 0;
+    return QMCG_OK;
+  }
+
+  int sweeps_trace(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, double* trace) override
+  {
+    if (!p || !trace)
+      return fail(QMCG_ERR_ARG, "null arguments");
+    if (!resident(p))
+      return fail(QMCG_ERR_ARG, "move records come from the walker-resident path: rng_mode 1 and path 0");
+    return run_sweeps(p, n, st, nullptr, false, trace);
+  }
+
+  // ------------------------------------------------------------------ diffusion Monte Carlo
+  int dmc_init(double* el) override
+  {
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "DMC needs mw_completeUpdates first");
+    if (!dm.ready)
+    {
+      CUDA_TRY(mem.alloc(&dm.weight, (size_t)nw));
+      CUDA_TRY(mem.alloc(&dm.e_old, (size_t)nw));
+      CUDA_TRY(mem.alloc(&dm.age, (size_t)nw));
+      CUDA_TRY(mem.alloc(&dm.par, 5));
+      CUDA_TRY(mem.alloc(&dm.sums, 5));
+      CUDA_TRY(mem.alloc(&dm.w_out, (size_t)nw));
+      CUDA_TRY(mem.alloc(&dm.src, (size_t)nw));
+      CUDA_TRY(mem.alloc(&s.rr, 2 * (size_t)nw));
+      dm.ready = true;
+    }
+    std::vector<double> ones(nw, 1.0);
+    CUDA_TRY(cudaMemcpyAsync(dm.weight, ones.data(), nw * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(dm.age, 0, nw * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(s.rr, 0, 2 * nw * sizeof(double), stream));
+    CUDA_TRY(launch_local_energy<T>(s, ew, e_out, stream));
+    CUDA_TRY(cudaMemcpyAsync(dm.e_old, e_out, nw * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    if (el)
+      CUDA_TRY(cudaMemcpyAsync(el, e_out, nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return status_check();
+  }
+
+  // one DMC step: fixed-node sweep, local energy, branch weights (DMCBatched::advanceWalkers)
+  int enqueue_dmc_step()
+  {
+    s.dmc      = 1;
+    int rc     = enqueue_sweep_resident();
+    s.dmc      = 0;
+    if (rc)
+      return rc;
+    CUDA_TRY(launch_local_energy<T>(s, ew, e_out, stream));
+    CUDA_TRY(launch_dmc_branch(nw, e_out, dm.e_old, dm.weight, dm.age, s.rr, dm.par, dm.sums, dm.w_out, stream));
+    return QMCG_OK;
+  }
+
+  int dmc_step(const qmcg_sweep_params* p, const qmcg_branch_params* b, double* w, double* el, int* age,
+               double* sums, qmcg_sweep_stats* st, double* trace) override
+  {
+    if (!p || !b || !(p->tau > 0))
+      return fail(QMCG_ERR_ARG, "bad DMC parameters");
+    if (!dm.ready)
+      return fail(QMCG_ERR_STATE, "call qmcg_dmc_init first");
+    if (!resident(p))
+      return fail(QMCG_ERR_ARG, "DMC runs on the walker-resident path: rng_mode 1 and path 0");
+    if (!(b->branch_max > b->branch_cutoff))
+      return fail(QMCG_ERR_ARG, "branch_max must exceed branch_cutoff");
+    if (dc[0] || dc[1])
+    {
+      const int rc = complete();
+      if (rc)
+        return rc;
+    }
+    s.rng_mode  = 1;
+    s.use_drift = p->use_drift;
+    s.tau       = p->tau;
+    s.seed      = p->seed;
+    flush_kind  = p->flush;
+    const double par[5] = {b->e_trial, b->e_ref, b->tau_eff, b->branch_cutoff, b->branch_max};
+    CUDA_TRY(cudaMemcpyAsync(dm.par, par, sizeof(par), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(s.counters, 0, 3 * sizeof(unsigned long long), stream));
+    if (trace)
+    {
+      const size_t nrec = (size_t)sys->ne * nw;
+      if (!trace_d)
+        CUDA_TRY(mem.alloc(&trace_d, nrec * TRACE_FIELDS));
+      s.trace = trace_d;
+      const int rc = enqueue_dmc_step();
+      s.trace      = nullptr;
+      if (rc)
+        return rc;
+      CUDA_TRY(cudaMemcpyAsync(trace, trace_d, nrec * TRACE_FIELDS * sizeof(double), cudaMemcpyDeviceToHost,
+                               stream));
+    }
+    else
+    {
+      if (!dm.graph || dm.g_drift != p->use_drift || dm.g_tau != p->tau || dm.g_seed != p->seed ||
+          dm.g_flush != p->flush || dm.g_nt != sweep_nt)
+      {
+        if (dm.graph)
+          cudaGraphExecDestroy(dm.graph);
+        dm.graph = nullptr;
+        cudaGraph_t g;
+        CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        const int rc        = enqueue_dmc_step();
+        const cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (rc)
+          return rc;
+        if (e != cudaSuccess)
+          return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&dm.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess)
+          return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ei));
+        dm.g_drift = p->use_drift;
+        dm.g_tau   = p->tau;
+        dm.g_seed  = p->seed;
+        dm.g_flush = p->flush;
+        dm.g_nt    = sweep_nt;
+      }
+      CUDA_TRY(cudaGraphLaunch(dm.graph, stream));
+    }
+    if (w)
+      CUDA_TRY(cudaMemcpyAsync(w, dm.w_out, nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (el)
+      CUDA_TRY(cudaMemcpyAsync(el, e_out, nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (age)
+      CUDA_TRY(cudaMemcpyAsync(age, dm.age, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    if (sums)
+      CUDA_TRY(cudaMemcpyAsync(sums, dm.sums, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    sweeps_since_recompute++;
+    if (p->recompute_every > 0 && sweeps_since_recompute >= p->recompute_every)
+    {
+      const int rc = recompute_device();
+      if (rc)
+        return rc;
+      sweeps_since_recompute = 0;
+    }
+    return sync(st);
+  }
+
+  // population control on the device: slot i takes walker src[i]
+  int dmc_copy(const int* src) override
+  {
+    if (!src)
+      return fail(QMCG_ERR_ARG, "null source list");
+    if (!dm.ready)
+      return fail(QMCG_ERR_STATE, "call qmcg_dmc_init first");
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "delayed updates pending: call qmcg_mw_complete_updates first");
+    for (int i = 0; i < nw; i++)
+    {
+      if (src[i] < 0 || src[i] >= nw)
+        return fail(QMCG_ERR_ARG, "source walker out of range");
+      if (src[src[i]] != src[i])
+        return fail(QMCG_ERR_ARG, "a walker copied elsewhere must keep its own slot (src[src[i]] == src[i])");
+    }
+    CUDA_TRY(cudaMemcpyAsync(dm.src, src, nw * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(launch_copy_walkers<T>(s, dm.src, dm.weight, dm.e_old, dm.age, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    invrow_iat = -1;
+    return QMCG_OK;
+  }
+
+  // fixed-count population control: comb of the current weights, then the device copies
+  int dmc_reconfigure(double u, int* src_out) override
+  {
+    if (!dm.ready)
+      return fail(QMCG_ERR_STATE, "call qmcg_dmc_init first");
+    std::vector<double> w;
+    int rc = d2h(w, static_cast<const double*>(dm.weight), (size_t)nw);
+    if (rc)
+      return rc;
+    std::vector<int> src(nw);
+    rc = qmcg_dmc_comb(nw, w.data(), u, src.data(), nullptr);
+    if (rc)
+      return rc;
+    rc = dmc_copy(src.data());
+    if (rc)
+      return rc;
+    if (src_out)
+      std::copy(src.begin(), src.end(), src_out);
+    return QMCG_OK;
+  }
+
+  // device time of one periodic FP64 recompute of every walker (CUDA events on the stream)
+  int profile_recompute(double* ms) override
+  {
+    if (!ms)
+      return fail(QMCG_ERR_ARG, "null output");
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "delayed updates pending: call qmcg_mw_complete_updates first");
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    CUDA_TRY(cudaEventRecord(a, stream));
+    int rc = recompute_device();
+    CUDA_TRY(cudaEventRecord(b, stream));
+    CUDA_TRY(cudaEventSynchronize(b));
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc)
+      return rc;
+    *ms = t;
+    return status_check();
+  }
+
+  // TrialWaveFunction::mw_evaluateGL on the tracked state
+  int evaluate_gl(double* lp, double* grads, double* laps) override
+  {
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "mw_evaluateGL needs mw_completeUpdates first");
+    const size_t n = (size_t)nw * sys->ne;
+    if (!gl_d)
+      CUDA_TRY(mem.alloc(&gl_d, n * 4));
+    CUDA_TRY(launch_evaluate_gl<T>(s, gl_d, stream));
+    std::vector<double> h;
+    int rc = d2h(h, static_cast<const double*>(gl_d), n * 4);
+    if (rc)
+      return rc;
+    for (size_t e = 0; e < n; e++)
+    {
+      if (grads)
+        for (int d = 0; d < 3; d++)
+          grads[e * 3 + d] = h[e * 4 + d];
+      if (laps)
+        laps[e] = h[e * 4 + 3];
+    }
+    return lp ? get_log(lp, nullptr, nullptr) : QMCG_OK;
+  }
+
   // QMCHamiltonian::mw_evaluate for kinetic + Coulomb after all delayed updates
   int local_energy(double* el, double* ke, double* vp) override
   {
@@ -1458,7 +1798,8 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 
-  int run_sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log, bool measure)
+  int run_sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log, bool measure,
+                 double* trace = nullptr)
   {
     if (!p || n < 0 || !(p->tau > 0) || (p->rng_mode != 0 && p->rng_mode != 1))
       return fail(QMCG_ERR_ARG, "bad sweep parameters");
@@ -1490,7 +1831,16 @@ struct Crowd final : qmcg_crowd_s
         CUDA_TRY(cudaMemcpyAsync(gauss_d, gauss_h, ng * sizeof(double), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(unif_d, unif_h, nu * sizeof(double), cudaMemcpyHostToDevice, stream));
       }
-      if (acc_log)
+      if (resident(p) && (acc_log || trace))
+      {
+        // the walker-resident kernel records its own moves
+        const size_t nrec = (size_t)sys->ne * nw;
+        rc = resident_traced_sweep(trace ? trace + (size_t)it * nrec * TRACE_FIELDS : nullptr,
+                                   acc_log ? acc_log + (size_t)it * nrec : nullptr);
+        if (rc)
+          return rc;
+      }
+      else if (acc_log)
       {
         // electron-by-electron launches so the decisions can be logged
         rc = sweep_logged(acc_log + (size_t)it * sys->ne * nw);
@@ -2127,6 +2477,25 @@ extern "C" int qmcg_vmc_sweeps_measure(qmcg_crowd c, const qmcg_sweep_params* p,
   CROWD_CALL(c, sweeps_measure(p, n, el, ke, st));
 }
 extern "C" int qmcg_crowd_sync(qmcg_crowd c, qmcg_sweep_stats* st) { CROWD_CALL(c, sync(st)); }
+extern "C" int qmcg_vmc_sweeps_trace(qmcg_crowd c, const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st,
+                                     double* trace)
+{
+  static_assert(QMCG_TRACE_FIELDS == TRACE_FIELDS, "trace record layout");
+  CROWD_CALL(c, sweeps_trace(p, n, st, trace));
+}
+extern "C" int qmcg_profile_recompute(qmcg_crowd c, double* ms) { CROWD_CALL(c, profile_recompute(ms)); }
+extern "C" int qmcg_dmc_init(qmcg_crowd c, double* el) { CROWD_CALL(c, dmc_init(el)); }
+extern "C" int qmcg_dmc_step(qmcg_crowd c, const qmcg_sweep_params* p, const qmcg_branch_params* b, double* w,
+                             double* el, int* age, double* sums, qmcg_sweep_stats* st, double* trace)
+{
+  CROWD_CALL(c, dmc_step(p, b, w, el, age, sums, st, trace));
+}
+extern "C" int qmcg_dmc_copy_walkers(qmcg_crowd c, const int* src) { CROWD_CALL(c, dmc_copy(src)); }
+extern "C" int qmcg_dmc_reconfigure(qmcg_crowd c, double u, int* src) { CROWD_CALL(c, dmc_reconfigure(u, src)); }
+extern "C" int qmcg_mw_evaluate_gl(qmcg_crowd c, double* lp, double* grads, double* laps)
+{
+  CROWD_CALL(c, evaluate_gl(lp, grads, laps));
+}
 extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
 extern "C" int qmcg_profile_sweep(qmcg_crowd c, int n, double* ms) { CROWD_CALL(c, profile_sweep(n, ms)); }
 

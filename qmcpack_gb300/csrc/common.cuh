@@ -115,6 +115,25 @@ struct DevState
   // learned proposal (walker-resident path): SIMT weight image and FP32 master parameters
   const void* mlp_simt;
   const float* mlp_params;
+  // optional per-move record of the walker-resident drift-diffusion sweep, [ne][nw][TRACE_FIELDS]
+  // (null: nothing recorded)
+  double* trace;
+  // fixed-node DMC moves (walker-resident path): a move that changes the sign of psi is
+  // rejected, and rr [nw][2] accumulates tau |xi|^2 over the proposed and the accepted moves
+  int dmc;
+  double* rr;
+};
+
+// fields of one move record of the walker-resident sweep (qmcg_vmc_sweeps_trace)
+enum : int
+{
+  TR_POS      = 0,  // proposed position x, y, z
+  TR_RATIO    = 3,  // psi(R') / psi(R)
+  TR_GRAD_NEW = 4,  // grad log psi at the proposed position, x, y, z
+  TR_GRAD_NOW = 7,  // grad log psi at the current position, x, y, z
+  TR_ACCEPT   = 10, // 1 accepted, 0 rejected
+  TR_SELF     = 11, // Ainv[row] . phi(r_row): 1 for an exact inverse (the health check's value)
+  TRACE_FIELDS = 12,
 };
 
 // Ewald tables of a system for the local-energy kernel (energy.cu)

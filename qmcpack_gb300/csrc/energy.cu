@@ -271,6 +271,75 @@ cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, dou
 }
 
 // ---------------------------------------------------------------------------
+// Per-electron gradient and Laplacian of log psi from the tracked state
+// (TrialWaveFunction::mw_evaluateGL, TrialWaveFunction.cpp:869-919, over the
+// components' mw_evaluateGL: DiracDeterminantBatched.cpp:594-603,
+// TwoBodyJastrow.cpp:774-775, J1OrbitalSoA.h:119-120):
+//   G_i = Ainv[r].dphi_i + dUat_i + Grad1_i
+//   L_i = Ainv[r].d2phi_i - |Ainv[r].dphi_i|^2 + d2Uat_i - Lap1_i
+// The same sums as the kinetic term of local_energy_kernel.  One CTA of 256
+// threads covers 8 electrons (a warp each) of one walker: grid (ceil(ne / 8), nw).
+// gl: [nw][ne][4] FP64 = G xyz, L.
+// ---------------------------------------------------------------------------
+template<typename T>
+__global__ void __launch_bounds__(256) evaluate_gl_kernel(DevState<T> s, double* __restrict__ gl)
+{
+  const int iw = blockIdx.y, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= s.ne)
+    return;
+  const int N = s.norb, lda = s.lda;
+  const int sp    = i < s.nup ? 0 : 1;
+  const size_t rb = ((size_t)sp * s.nw + iw) * N + (i - sp * s.nup);
+  const T* a      = s.Ainv + rb * lda;
+  const T* g      = s.dgrad + rb * 3 * lda;
+  const T* l      = s.dlap + rb * lda;
+  T gx = 0, gy = 0, gz = 0, lp = 0;
+  for (int o = lane; o < N; o += 32)
+  {
+    const T av = a[o];
+    gx += av * g[o];
+    gy += av * g[lda + o];
+    gz += av * g[2 * lda + o];
+    lp += av * l[o];
+  }
+  double G[3] = {static_cast<double>(warp_sum(gx)), static_cast<double>(warp_sum(gy)),
+                 static_cast<double>(warp_sum(gz))};
+  double L    = static_cast<double>(warp_sum(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+  if (lane != 0)
+    return;
+  if (s.has_j2)
+  {
+    const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + i;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      G[d] += static_cast<double>(j2[(1 + d) * s.ne_pad]);
+    L += static_cast<double>(j2[4 * s.ne_pad]);
+  }
+  if (s.has_j1)
+  {
+    const T* j1 = s.J1 + (size_t)iw * 5 * s.ne_pad + i;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      G[d] += static_cast<double>(j1[(1 + d) * s.ne_pad]);
+    L -= static_cast<double>(j1[4 * s.ne_pad]);
+  }
+  double* o = gl + ((size_t)iw * s.ne + i) * 4;
+  o[0]      = G[0];
+  o[1]      = G[1];
+  o[2]      = G[2];
+  o[3]      = L;
+}
+
+template<typename T>
+cudaError_t launch_evaluate_gl(const DevState<T>& s, double* gl, cudaStream_t st)
+{
+  const dim3 grid((s.ne + 7) / 8, s.nw);
+  evaluate_gl_kernel<T><<<grid, 256, 0, st>>>(s, gl);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // host: G vectors, ion structure factor and constants
 // ---------------------------------------------------------------------------
 int ewald_build(const double L[3], int ne, int nions, const double* ion_pos, const double* ion_q, double eps,
@@ -351,5 +420,7 @@ template cudaError_t setup_local_energy<double>();
 template cudaError_t launch_local_energy<float>(const DevState<float>&, const EwaldDev<float>&, double*, cudaStream_t);
 template cudaError_t launch_local_energy<double>(const DevState<double>&, const EwaldDev<double>&, double*,
                                                  cudaStream_t);
+template cudaError_t launch_evaluate_gl<float>(const DevState<float>&, double*, cudaStream_t);
+template cudaError_t launch_evaluate_gl<double>(const DevState<double>&, double*, cudaStream_t);
 
 } // namespace qmcg

@@ -110,6 +110,15 @@ cudaError_t setup_local_energy();
 // out: [3][nw] doubles = local energy, kinetic, potential
 template<typename T>
 cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st);
+// diffusion Monte Carlo (dmc.cu)
+cudaError_t launch_dmc_branch(int nw, const double* e_new, double* e_old, double* weight, int* age, double* rr,
+                              const double* par, double* sums, double* w_out, cudaStream_t st);
+template<typename T>
+cudaError_t launch_copy_walkers(const DevState<T>& s, const int* src, double* weight, double* e_old, int* age,
+                                cudaStream_t st);
+// per-electron gradient and Laplacian of log psi, gl: [nw][ne][4] (G xyz, L)
+template<typename T>
+cudaError_t launch_evaluate_gl(const DevState<T>& s, double* gl, cudaStream_t st);
 
 // learned MH proposal (learned.cu): MLP 51 -> 128 -> 128 -> 128 -> 6, inputs padded
 // to 64 and outputs to 16 for the tensor cores

@@ -204,6 +204,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       J2s[e] = s.J2[(size_t)w * 5 * s.ne_pad + e];
     prefetch_rows(s, slot, i0 - first, pre, threadIdx.x, NT);
     int dc = 0;
+    // DMC: tau |xi|^2 of this segment's proposed and accepted moves (thread 0)
+    double rr_prop = 0, rr_acc = 0;
     // product of the accepted determinant ratios (thread 0), one log per segment
     double det_mant = 1.0;
     int det_exp     = 0;
@@ -359,6 +361,13 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
               gs += J2s[(1 + d) * s.ne_pad + iat];
             gn[d] = gs;
           }
+          if (s.trace)
+          {
+            double* tr = s.trace + ((size_t)iat * s.nw + w) * TRACE_FIELDS;
+            for (int d = 0; d < 3; d++)
+              tr[TR_GRAD_NOW + d] = static_cast<double>(gn[d]);
+            tr[TR_SELF] = static_cast<double>(g[3]);
+          }
           const T sqrttau = sqrt(tau);
           T delta[3], drift[3];
           for (int d = 0; d < 3; d++)
@@ -507,9 +516,20 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           log_gb = -(T(0.5) / tau) * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
         }
         int a = 0;
-        if (p >= Eps<T>::v)
+        // DMC: a move that changes the sign of psi is rejected (fixed node,
+        // DMCBatched.cpp:203-210 with SFNBranch::phaseChanged for real ratios)
+        if (p >= Eps<T>::v && (!s.dmc || detr > T(0)))
         {
           a = sh.runif[jj] < p * exp(log_gb - sh.loggf) ? 1 : 0;
+        }
+        if (s.dmc)
+        {
+          const double r2 = static_cast<double>(tau) *
+              static_cast<double>(sh.rgauss[jj][0] * sh.rgauss[jj][0] + sh.rgauss[jj][1] * sh.rgauss[jj][1] +
+                                  sh.rgauss[jj][2] * sh.rgauss[jj][2]);
+          rr_prop += r2;
+          if (a)
+            rr_acc += r2;
         }
         if (a)
         {
@@ -523,6 +543,17 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         else
           n_rej++;
         sh.acc = a;
+        if (s.trace)
+        {
+          double* tr = s.trace + ((size_t)iat * s.nw + w) * TRACE_FIELDS;
+          for (int d = 0; d < 3; d++)
+          {
+            tr[TR_POS + d]      = sh.pos[d];
+            tr[TR_GRAD_NEW + d] = static_cast<double>(g[d]);
+          }
+          tr[TR_RATIO]  = static_cast<double>(detr) * exp(static_cast<double>(logj));
+          tr[TR_ACCEPT] = a;
+        }
         }
       }
       __syncthreads();
@@ -734,6 +765,11 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       s.log_abs[slot] += log(det_mant) + det_exp * 0.69314718055994530942;
       if (det_neg)
         s.sign[slot] = -s.sign[slot];
+      if (s.dmc)
+      {
+        s.rr[2 * w] += rr_prop;
+        s.rr[2 * w + 1] += rr_acc;
+      }
     }
     // hand the segment's Binv to the batched flush, positions and J2 state back to HBM
     if (K > 1)

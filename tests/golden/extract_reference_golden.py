@@ -34,7 +34,7 @@ def checks(text, lhs_pat):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QMCPACK_REFERENCE_DIR", "/root/reference")
     g = {"source": "QMCPACK unit tests (read as text)"}
 
     # --- spline2 prefactors and VGH: src/spline2/tests/test_multi_spline.cpp

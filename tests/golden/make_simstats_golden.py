@@ -14,7 +14,7 @@ import numpy as np
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QMCPACK_REFERENCE_DIR", "/root/reference")
     sys.path.insert(0, os.path.join(root, "nexus"))
     from nexus.numerics import simstats
 

@@ -102,3 +102,99 @@ def test_fp32_crowd_tracks_fp64():
         np.testing.assert_allclose(r4, r8, rtol=1e-3)
         c8.accept_reject(iat, [1, 0, 1])
         c4.accept_reject(iat, [1, 0, 1])
+
+
+@pytest.mark.parametrize("delay,drift", [(1, True), (3, True), (3, False)])
+def test_philox_sweep_state_matches_recompute(delay, drift):
+    """Sweeps on the counter-based stream keep the tracked state equal to a recompute."""
+    s = small_system(delay)
+    R = make_walkers(s, 3, seed=4)
+    c = orc.Crowd(s, 3, delay, 8)
+    c.load_walkers(R)
+    c.evaluate_log()
+    na, nr, tr = c.vmc_sweeps_philox(seed=77, nsteps=3, tau=0.3, use_drift=drift, trace=True)
+    assert na > 0 and nr > 0 and na + nr == 3 * s.n_elec * 3
+    assert int(tr[..., 10].sum()) == na
+    lp_tracked, _, _ = c.get_log()
+    j2_tracked, _ = c.jastrow_state()
+    lp_fresh, _ = c.evaluate_log()
+    np.testing.assert_allclose(lp_tracked, lp_fresh, rtol=1e-10, atol=1e-10)
+    j2_fresh, _ = c.jastrow_state()
+    np.testing.assert_allclose(j2_tracked, j2_fresh, rtol=1e-9, atol=1e-11)
+
+
+def test_philox_sweeps_deterministic_and_sweep_indexed():
+    """The stream depends only on (seed, walker, electron, sweep): two sweeps in one call
+    equal one sweep at sweep index 0 followed by one at sweep index 1."""
+    s = small_system(3)
+    R = make_walkers(s, 3, seed=5)
+    a, b = orc.Crowd(s, 3, 3, 8), orc.Crowd(s, 3, 3, 8)
+    for c in (a, b):
+        c.load_walkers(R)
+        c.evaluate_log()
+    _, _, ta = a.vmc_sweeps_philox(seed=9, nsteps=2, tau=0.3, trace=True)
+    _, _, t0 = b.vmc_sweeps_philox(seed=9, nsteps=1, tau=0.3, sweep0=0, trace=True)
+    _, _, t1 = b.vmc_sweeps_philox(seed=9, nsteps=1, tau=0.3, sweep0=1, trace=True)
+    np.testing.assert_array_equal(ta, np.concatenate([t0, t1]))
+    np.testing.assert_array_equal(a.positions(), b.positions())
+
+
+def test_replay_reproduces_trajectory():
+    """Replaying a recorded trajectory on a fresh crowd gives the same ratios, gradients
+    and final state as the run that recorded it."""
+    s = small_system(3)
+    R = make_walkers(s, 3, seed=6)
+    a, b = orc.Crowd(s, 3, 3, 8), orc.Crowd(s, 3, 3, 8)
+    for c in (a, b):
+        c.load_walkers(R)
+        c.evaluate_log()
+    _, _, ta = a.vmc_sweeps_philox(seed=21, nsteps=2, tau=0.3, trace=True)
+    tb = b.replay(ta)
+    np.testing.assert_allclose(tb, ta, rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_allclose(a.get_log()[0], b.get_log()[0], rtol=1e-13)
+
+
+def test_philox_proposals_are_unit_gaussians():
+    """Proposal displacements without drift are sqrt(tau) times unit Gaussians: first
+    moves of many walkers have mean 0 and variance tau per axis."""
+    spec = scaled_spec("c0_32e", n_up=2, n_dn=2, grid=8, walkers=4000, delay=1, precision=8)
+    s = make_system(spec, seed=3)
+    nw = 4000
+    R = make_walkers(s, nw, seed=8)
+    c = orc.Crowd(s, nw, 1, 8)
+    c.load_walkers(R)
+    c.evaluate_log()
+    tau = 0.3
+    _, _, tr = c.vmc_sweeps_philox(seed=5, nsteps=1, tau=tau, use_drift=False, trace=True)
+    d = tr[0, 0, :, 0:3] - R[:, 0, :]
+    d -= s.lattice * np.round(d / s.lattice)
+    z = d.ravel() / np.sqrt(tau)
+    assert abs(z.mean()) < 4 / np.sqrt(z.size)
+    assert abs(z.var() - 1) < 5 * np.sqrt(2 / z.size)
+
+
+@pytest.mark.parametrize("delay", [1, 3])
+def test_replay_philox_reproduces_own_chain(delay):
+    """Following its own recorded chain, the step-by-step check forms the same proposals
+    and the same decisions (every decision away from a tie)."""
+    s = small_system(delay)
+    R = make_walkers(s, 3, seed=9)
+    a, b = orc.Crowd(s, 3, delay, 8), orc.Crowd(s, 3, delay, 8)
+    for c in (a, b):
+        c.load_walkers(R)
+        c.evaluate_log()
+    _, _, ta = a.vmc_sweeps_philox(seed=31, nsteps=2, tau=0.3, trace=True)
+    tb, margin = b.replay_philox(ta, seed=31, tau=0.3)
+    np.testing.assert_allclose(tb[..., 0:3], ta[..., 0:3], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(tb[..., 3:10], ta[..., 3:10], rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(tb[..., 10], ta[..., 10])
+    assert np.all(np.abs(margin) > 0)
+    # a decision that differs from the recorded one is caught
+    tc = ta.copy()
+    tc[0, 2, 1, 10] = 1 - tc[0, 2, 1, 10]
+    d = orc.Crowd(s, 3, delay, 8)
+    d.load_walkers(R)
+    d.evaluate_log()
+    td, _ = d.replay_philox(tc, seed=31, tau=0.3)
+    assert td[0, 2, 1, 10] != tc[0, 2, 1, 10]

@@ -33,3 +33,19 @@ def test_energy_statistics_shapes():
     assert st["sweeps"] == 180 and st["walkers"] == 16
     assert abs(st["energy"] + 10) < 5 * st["error"] + 1e-12
     assert 0.5 < st["kappa"] < 2.0
+
+
+def test_walker_kappa_matches_ar1():
+    """Independent AR(1) chains x_t = a x_{t-1} + noise have kappa = (1 + a) / (1 - a)."""
+    from qmcpack_gb300.stats import ensemble_statistics, walker_kappa
+    rng = np.random.default_rng(4)
+    a, n, nw = 0.8, 2000, 256
+    x = np.zeros((n, nw))
+    x[0] = rng.normal(size=nw) / np.sqrt(1 - a * a)
+    for t in range(1, n):
+        x[t] = a * x[t - 1] + rng.normal(size=nw)
+    k = walker_kappa(x)
+    assert abs(k - (1 + a) / (1 - a)) < 0.5
+    st = ensemble_statistics(x + 3.0)
+    assert abs(st["energy"] - 3.0) < 4 * st["error"]
+    assert abs(st["variance"] - 1 / (1 - a * a)) < 4 * st["variance_error"]

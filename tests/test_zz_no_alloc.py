@@ -2,10 +2,13 @@
 
 It serves callers that cannot allocate device memory themselves or through a
 stream-ordered pool (their device memory belongs to another allocator, or they
-cannot take the synchronisation that freeing implies); its scratch is a fixed
-16 MiB device array instead.  Two calls in a row, with different data and sizes,
-must each give the same result as the allocating entry point
-qmcg_mw_update_inv_mat on the same inputs, within the tolerances of
+cannot take the synchronisation that freeing implies).  Shapes whose tiles fit in
+shared memory need no scratch; the others use a fixed 16 MiB device array instead.
+Per precision, three calls in a row: a large batch on the scratch path with every
+delay slot used, then a smaller one on the scratch path with fewer slots used than
+the delay rank (so stale scratch from the first call would show), then a shape
+that needs no scratch.  Each must give the same result as the allocating entry
+point qmcg_mw_update_inv_mat on the same inputs, within the tolerances of
 tests/test_gpu_det_engine.py (1e-12 FP64, 2e-5 FP32, relative to the largest
 element), and the second call must not change the free device memory.
 This file is collected last so that a run stopping at the first failure has
@@ -51,27 +54,32 @@ def _call(L, name, prec, dev, dc):
                             C.c_void_p(tV.data_ptr()), C.c_void_p(tB.data_ptr()), C.c_void_p(tD.data_ptr()), None)
 
 
+# (num_walkers, n, lda, delay_rank, delay_count): scratch path with dc = k, scratch path with
+# dc < k, then a shape whose shared-memory tiles fit (no scratch)
+CASES = {
+    8: [(256, 192, 192, 32, 32), (64, 192, 208, 32, 20), (4, 40, 48, 8, 6)],
+    4: [(80, 768, 768, 64, 64), (16, 768, 784, 64, 40), (512, 192, 192, 32, 32)],
+}
+
+
 @pytest.mark.parametrize("prec,tol", [(8, 1e-12), (4, 2e-5)])
-def test_noalloc_flush_matches_allocating_flush_twice(prec, tol):
+def test_noalloc_flush_matches_allocating_flush(prec, tol):
     import torch
     from qmcpack_gb300 import _lib
     L = _lib.load()
-    # second case: the production shape (384 electrons, delay rank 32); 12.6 MB of scratch either way
-    cases = [((4, 40, 48, 8, 6), 1), ((512 if prec == 4 else 256, 192, 192, 32, 32), 2)]
     results = []
-    free_before_second = None
-    for i, (shape, seed) in enumerate(cases):
-        arrays = _case(*shape, seed=seed)
+    for i, shape in enumerate(CASES[prec]):
+        arrays = _case(*shape, seed=i + 1)
         dev = _device(arrays, prec)
         torch.cuda.synchronize()
-        if i == 1:
-            free_before_second = torch.cuda.mem_get_info()[0]
+        free_before = torch.cuda.mem_get_info()[0]
         rc = _call(L, "qmcg_mw_update_inv_mat_noalloc", prec, dev, shape[4])
         torch.cuda.synchronize()
         assert rc == 0, L.qmcg_last_error()
         if i == 1:
-            assert torch.cuda.mem_get_info()[0] == free_before_second
+            assert torch.cuda.mem_get_info()[0] == free_before
         results.append((arrays, dev[0].double().cpu().numpy(), shape))
+        del dev
     # the allocating entry point on the same inputs, after the allocation-free calls
     for arrays, got, shape in results:
         dev = _device(arrays, prec)
@@ -81,7 +89,8 @@ def test_noalloc_flush_matches_allocating_flush_twice(prec, tol):
         ref = dev[0].double().cpu().numpy()
         n = shape[1]
         err = np.max(np.abs(got[:, :, :n] - ref[:, :, :n])) / np.max(np.abs(ref[:, :, :n]))
-        assert err <= tol, err
+        assert err <= tol, (shape, err)
+        del dev
 
 
 def test_noalloc_flush_rejects_oversized_batches():
