@@ -211,6 +211,11 @@ def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4, R=None):
             "walkers": label}
 
 
+def monotonic(x) -> bool:
+    d = np.diff(np.asarray(x, np.float64))
+    return bool(np.all(d > 0) or np.all(d < 0))
+
+
 def effective_samples(args, system, dsys32, seed: int):
     """Effective independent samples/s = walker-sweeps/s / kappa for
       plain_fp64:   drift-diffusion, FP64 move loop (the comparator the metric names)
@@ -219,9 +224,10 @@ def effective_samples(args, system, dsys32, seed: int):
                     (staged kernels, BF16 network on the tensor cores, hand-written backward
                     and Adam), then run frozen on the walker-resident kernel.
     Protocol: one FP32 drift-diffusion crowd is equilibrated in blocks of args.eff_block
-    sweeps, at least args.eff_min_blocks of them, until the last block's mean energy agrees
-    with the previous block's within 2 combined standard errors twice in a row (at most
-    args.eff_max_blocks blocks); the three methods then start from that configuration and
+    sweeps, at least args.eff_min_blocks of them, until twice in a row the last block's
+    mean energy agrees with the previous block's within 2 combined standard errors and the
+    last four block means show no monotonic trend (at most args.eff_max_blocks blocks; the
+    record says whether the test passed); the three methods then start from that configuration and
     run the same number of sweeps (args.eff_sweeps), so their kappa estimates see series
     of equal length.  Each method's kappa is its own: the autocorrelation function averaged
     over the walkers' own E_L series (independent chains, simstats truncation rule);
@@ -265,7 +271,8 @@ def effective_samples(args, system, dsys32, seed: int):
                                                                 flush=args.flush))
         t_eq += dt
         blocks.append(ensemble_statistics(el))
-        if len(blocks) >= max(2, args.eff_min_blocks) and agree_within(blocks[-1], blocks[-2], "energy", "error"):
+        if len(blocks) >= max(4, args.eff_min_blocks) and agree_within(blocks[-1], blocks[-2], "energy", "error") \
+                and not monotonic([b["energy"] for b in blocks[-4:]]):
             passes += 1
             if passes >= 2:
                 break
@@ -274,8 +281,9 @@ def effective_samples(args, system, dsys32, seed: int):
     out["equilibration"] = {"method": "plain FP32 drift-diffusion", "block_sweeps": args.eff_block,
                             "blocks": len(blocks), "sweeps": len(blocks) * args.eff_block, "seconds": t_eq,
                             "stationary": passes >= 2,
-                            "test": f"at least {args.eff_min_blocks} blocks, then the last block mean within 2 "
-                                    "sigma of the previous block, twice in a row",
+                            "test": f"at least {args.eff_min_blocks} blocks, then twice in a row: the last block "
+                                    "mean within 2 sigma of the previous block and the last four block means not "
+                                    "monotonic (no trend)",
                             "block_energies": [b["energy"] for b in blocks],
                             "block_errors": [b["error"] for b in blocks]}
     Req = g.positions()

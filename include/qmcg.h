@@ -225,6 +225,18 @@ int qmcg_vmc_sweeps_measure(qmcg_crowd crowd, const qmcg_sweep_params* params, i
  * updates are pending. */
 int qmcg_mw_evaluate_gl(qmcg_crowd crowd, double* log_psi, double* grads, double* laplacians);
 
+/* Ratios of virtual moves: ratios[v] = psi(R with electron electron[v] at pos[v]) / psi(R)
+ * for walker walker[v] — the quadrature points of a non-local pseudopotential
+ * (TrialWaveFunction::mw_evaluateRatios, TrialWaveFunction.cpp:1079-1110, over the
+ * VirtualParticleSets of NonLocalECPotential; per component SplineR2R::mw_evaluateDetRatios,
+ * SplineR2R.cpp:204-335, TwoBodyJastrow::mw_evaluateRatios, TwoBodyJastrow.cpp:174-206, and
+ * J1OrbitalSoA::evaluateRatios, J1OrbitalSoA.h:295-299).  The virtual moves of every walker
+ * form one flat list of num_moves entries: walker [num_moves], electron [num_moves],
+ * pos [num_moves][3] (bohr, FP64 host arrays); ratios [num_moves] FP64.  Nothing of the
+ * walkers changes.  Returns QMCG_ERR_STATE while delayed updates are pending. */
+int qmcg_mw_evaluate_ratios(qmcg_crowd crowd, int num_moves, const int* walker, const int* electron, const double* pos,
+                            double* ratios);
+
 /* Verification helper (no reference counterpart; it exposes what the driver loop of
  * VMCBatched::advanceWalkers sees for every move): qmcg_vmc_sweeps on the
  * walker-resident path (rng_mode 1, path 0, drift-diffusion) with one record per move,

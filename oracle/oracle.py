@@ -66,6 +66,7 @@ def lib():
         L.orc_replay_trace_philox.argtypes = [C.c_void_p, C.c_uint64, C.c_uint, C.c_int, C.c_double, C.c_int,
                                               C.c_int, _dp, _dp, _dp]
         L.orc_copy_walkers.argtypes = [C.c_void_p, _ip]
+        L.orc_evaluate_ratios.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp]
         L.orc_prefactors.argtypes = [C.c_double, _dp, _dp, _dp]
         L.orc_spline_vgh.argtypes = [_ip, C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp]
         L.orc_functor_eval.argtypes = [C.c_int, C.c_double, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
@@ -353,6 +354,15 @@ class Crowd:
         lib().orc_replay_trace_philox(self.h, seed, sweep0, ti.shape[0], tau, int(use_drift), int(dmc), _ptr(ti),
                                       _ptr(to), _ptr(margin))
         return to, margin
+
+    def evaluate_ratios(self, walker, electron, pos):
+        """Ratios psi(R, electron at pos) / psi(R) of a flat list of virtual moves."""
+        wk = np.ascontiguousarray(walker, np.int32).ravel()
+        el = np.ascontiguousarray(electron, np.int32).ravel()
+        ps = _d(pos).reshape(-1, 3)
+        r = np.zeros(wk.size)
+        lib().orc_evaluate_ratios(self.h, wk.size, _ptr(wk, _ip), _ptr(el, _ip), _ptr(ps), _ptr(r))
+        return r
 
     def copy_walkers(self, src):
         """Walker i takes the state of walker src[i] (population control)."""

@@ -1423,6 +1423,47 @@ void replay(Crowd<T>& c, const double* trace_in, double* trace_out)
 }
 
 // ---------------------------------------------------------------------------
+// Ratio of one virtual move: psi(R with electron e at pos) / psi(R) of walker iw, after
+// every delayed update (TrialWaveFunction::mw_evaluateRatios over a VirtualParticleSet,
+// TrialWaveFunction.cpp:1079-1110): the determinant Ainv[row] . phi(pos)
+// (SplineR2R::evaluateDetRatios, SplineR2R.cpp:184-196), the J2 factor
+// exp(Uat[e] - sum_{j != e} u(|r_j - pos|)) (TwoBodyJastrow::evaluateRatios,
+// TwoBodyJastrow.cpp:166-171) and the J1 factor exp(Vat[e] - sum_I u1(|R_I - pos|))
+// (J1OrbitalSoA::evaluateRatios, J1OrbitalSoA.h:295-299).
+// ---------------------------------------------------------------------------
+template<typename T>
+double vp_ratio(const Crowd<T>& c, int iw, int e, const double pos[3])
+{
+  const int s   = c.group_of(e);
+  const int row = e - c.first_of(s);
+  std::vector<T> v(c.norb), g((size_t)3 * c.norb), l(c.norb);
+  c.spo_vgl(pos, v.data(), g.data(), l.data());
+  const T* inv = c.w[iw].det[s].Ainv.data() + (size_t)row * c.norb;
+  T det        = 0;
+  for (int o = 0; o < c.norb; o++)
+    det += v[o] * inv[o];
+  double logj = 0;
+  const auto& wk = c.w[iw];
+  if (c.has_j2)
+  {
+    std::vector<T> dist(c.ne), dr((size_t)3 * c.ne);
+    c.ee_row(wk, pos, dist.data(), dr.data());
+    T vgl[5];
+    c.j2_vgl(e, dist.data(), dr.data(), vgl, nullptr, nullptr, nullptr);
+    logj += static_cast<double>(wk.Uat[e] - vgl[0]);
+  }
+  if (c.has_j1)
+  {
+    std::vector<T> dist(c.nions), dr((size_t)3 * c.nions);
+    c.ei_row(pos, dist.data(), dr.data());
+    T U, gr[3], lap;
+    c.j1_vgl(dist.data(), dr.data(), U, gr, lap);
+    logj += static_cast<double>(wk.Vat[e] - U);
+  }
+  return static_cast<double>(det) * std::exp(logj);
+}
+
+// ---------------------------------------------------------------------------
 // Step-by-step check of a recorded trajectory on the counter-based stream.  The
 // state follows trace_in (its proposed positions and decisions); at every move this
 // crowd also forms, independently, what the driver step would do from that state:
@@ -1838,6 +1879,18 @@ void orc_replay_trace_philox(void* hv, uint64_t seed, unsigned sweep0, int nstep
     for (int s = 0; s < nsteps; s++)
       orc::replay_philox(*c, ps, sweep0 + (unsigned)s, tau, use_drift != 0, dmc != 0, trace_in + s * per,
                          trace_out + s * per, margin ? margin + s * nrec : nullptr);
+  });
+}
+
+// ratios of virtual moves (call after complete_updates): ratios[v] for walker[v],
+// electron elec[v] at pos[v] (pos [nvp][3])
+void orc_evaluate_ratios(void* hv, int nvp, const int* walker, const int* elec, const double* pos, double* ratios)
+{
+  auto* h = static_cast<OrcHandle*>(hv);
+  dispatch(h, [&](auto* c) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int v = 0; v < nvp; v++)
+      ratios[v] = orc::vp_ratio(*c, walker[v], elec[v], pos + 3 * (size_t)v);
   });
 }
 

@@ -199,6 +199,17 @@ class Crowd:
         self.last_repaired = st.repaired
         return st.accepted, st.rejected, tr
 
+    def mw_evaluateRatios(self, walker, electron, pos):
+        """Ratios psi(R, electron at pos) / psi(R) of a flat list of virtual moves
+        (non-local pseudopotential quadrature points); needs mw_completeUpdates first."""
+        wk = np.ascontiguousarray(walker, np.int32).ravel()
+        el = np.ascontiguousarray(electron, np.int32).ravel()
+        ps = _d(pos).reshape(-1, 3)
+        assert wk.size == el.size == ps.shape[0]
+        r = np.zeros(wk.size)
+        check(self.L.qmcg_mw_evaluate_ratios(self.handle, wk.size, _p(wk, _ip), _p(el, _ip), _p(ps), _p(r)))
+        return r
+
     # ---- diffusion Monte Carlo
     def dmc_init(self):
         """Weights 1, ages 0; returns the local energy of every walker (the first E_old)."""

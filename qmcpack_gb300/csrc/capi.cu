@@ -476,6 +476,7 @@ struct qmcg_crowd_s
                        double* sums, qmcg_sweep_stats* st, double* trace) = 0;
   virtual int dmc_copy(const int* src) = 0;
   virtual int dmc_reconfigure(double u, int* src) = 0;
+  virtual int evaluate_ratios(int nvp, const int* walker, const int* elec, const double* pos, double* ratios) = 0;
 };
 
 // The comb of population control with a fixed walker count
@@ -597,6 +598,25 @@ struct Crowd final : qmcg_crowd_s
     double g_tau   = 0;
     uint64_t g_seed = 0;
   } dm;
+  // virtual moves (non-local pseudopotential quadrature points): inputs and ratios on the device
+  struct VirtualMoves
+  {
+    size_t cap     = 0;
+    int* walker    = nullptr;
+    int* elec      = nullptr;
+    double* pos    = nullptr;
+    double* ratios = nullptr;
+    void release()
+    {
+      cudaFree(walker);
+      cudaFree(elec);
+      cudaFree(pos);
+      cudaFree(ratios);
+      walker = elec = nullptr;
+      pos = ratios = nullptr;
+      cap          = 0;
+    }
+  } vp;
   double* gl_d    = nullptr; // [nw][ne][4] per-electron gradient and Laplacian of log psi
   double* e_out  = nullptr; // [3][nw] local energy, kinetic, potential
   double* e_hist = nullptr; // [e_hist_cap][2][nw] per-sweep local and kinetic energies
@@ -616,6 +636,7 @@ struct Crowd final : qmcg_crowd_s
       cudaGraphExecDestroy(ln.graph);
     if (dm.graph)
       cudaGraphExecDestroy(dm.graph);
+    vp.release();
     if (stream)
       cudaStreamDestroy(stream);
   }
@@ -1335,6 +1356,41 @@ struct Crowd final : qmcg_crowd_s
       return rc;
     if (src_out)
       std::copy(src.begin(), src.end(), src_out);
+    return QMCG_OK;
+  }
+
+  // TrialWaveFunction::mw_evaluateRatios over virtual moves (flat list across walkers)
+  int evaluate_ratios(int nvp, const int* walker, const int* elec, const double* pos, double* ratios) override
+  {
+    if (nvp < 0 || (nvp > 0 && (!walker || !elec || !pos || !ratios)))
+      return fail(QMCG_ERR_ARG, "bad virtual-move arguments");
+    if (dc[0] || dc[1])
+      return fail(QMCG_ERR_STATE, "virtual-move ratios need mw_completeUpdates first");
+    for (int v = 0; v < nvp; v++)
+    {
+      if (walker[v] < 0 || walker[v] >= nw || elec[v] < 0 || elec[v] >= sys->ne)
+        return fail(QMCG_ERR_ARG, "virtual move " + std::to_string(v) + ": walker or electron out of range");
+      if (!std::isfinite(pos[3 * v]) || !std::isfinite(pos[3 * v + 1]) || !std::isfinite(pos[3 * v + 2]))
+        return fail(QMCG_ERR_ARG, "virtual move " + std::to_string(v) + ": non-finite position");
+    }
+    if (nvp == 0)
+      return QMCG_OK;
+    if ((size_t)nvp > vp.cap)
+    {
+      CUDA_TRY(cudaStreamSynchronize(stream));
+      vp.release();
+      CUDA_TRY(cudaMalloc(&vp.walker, nvp * sizeof(int)));
+      CUDA_TRY(cudaMalloc(&vp.elec, nvp * sizeof(int)));
+      CUDA_TRY(cudaMalloc(&vp.pos, 3 * (size_t)nvp * sizeof(double)));
+      CUDA_TRY(cudaMalloc(&vp.ratios, nvp * sizeof(double)));
+      vp.cap = nvp;
+    }
+    CUDA_TRY(cudaMemcpyAsync(vp.walker, walker, nvp * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(vp.elec, elec, nvp * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(vp.pos, pos, 3 * (size_t)nvp * sizeof(double), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, stream));
+    CUDA_TRY(cudaMemcpyAsync(ratios, vp.ratios, nvp * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
     return QMCG_OK;
   }
 
@@ -2492,6 +2548,11 @@ extern "C" int qmcg_dmc_step(qmcg_crowd c, const qmcg_sweep_params* p, const qmc
 }
 extern "C" int qmcg_dmc_copy_walkers(qmcg_crowd c, const int* src) { CROWD_CALL(c, dmc_copy(src)); }
 extern "C" int qmcg_dmc_reconfigure(qmcg_crowd c, double u, int* src) { CROWD_CALL(c, dmc_reconfigure(u, src)); }
+extern "C" int qmcg_mw_evaluate_ratios(qmcg_crowd c, int nvp, const int* walker, const int* elec, const double* pos,
+                                       double* ratios)
+{
+  CROWD_CALL(c, evaluate_ratios(nvp, walker, elec, pos, ratios));
+}
 extern "C" int qmcg_mw_evaluate_gl(qmcg_crowd c, double* lp, double* grads, double* laps)
 {
   CROWD_CALL(c, evaluate_gl(lp, grads, laps));

@@ -110,6 +110,10 @@ cudaError_t setup_local_energy();
 // out: [3][nw] doubles = local energy, kinetic, potential
 template<typename T>
 cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st);
+// ratios of virtual moves (nlpp.cu): out[v] = psi(R, electron elec[v] at pos[v]) / psi(R) of walker walker[v]
+template<typename T>
+cudaError_t launch_vp_ratios(const DevState<T>& s, int nvp, const int* walker, const int* elec, const double* pos,
+                             double* out, cudaStream_t st);
 // diffusion Monte Carlo (dmc.cu)
 cudaError_t launch_dmc_branch(int nw, const double* e_new, double* e_old, double* weight, int* age, double* rr,
                               const double* par, double* sums, double* w_out, cudaStream_t st);

@@ -1,0 +1,104 @@
+"""Ratios of virtual moves (non-local pseudopotential quadrature points) on the GPU
+against the oracle.
+
+FP64: every ratio within 1e-10 relative of the oracle's, 1e-8 near a node of psi
+(|ratio| < 1e-2, where the determinant ratio is a cancelling sum); a virtual move onto
+the electron's own position gives 1 and one onto a proposed position gives the
+mw_calcRatioGrad ratio of that move.  FP32 (the 384-electron system): errors against
+the FP64 oracle on the same positions and coefficients are measured and bounded.
+Set QMCG_ERROR_TABLE to append the FP32 error statistics.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from qmcpack_gb300.nlpp import quadrature_moves
+from qmcpack_gb300.system import make_system, make_walkers, scaled_spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu():
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem
+    return Crowd, DeviceSystem
+
+
+def rel_errors(a, b, floor=1e-12):
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+@pytest.mark.parametrize("delay", [1, 4])
+def test_virtual_move_ratios_fp64(delay):
+    Crowd, DeviceSystem = _gpu()
+    nw = 8
+    spec = scaled_spec("c0_32e", n_up=16, n_dn=16, grid=16, walkers=nw, delay=delay, precision=8)
+    s = make_system(spec, seed=71)
+    g = Crowd(DeviceSystem(s), nw, delay)
+    g.load_walkers(make_walkers(s, nw, seed=72))
+    g.mw_evaluateLog()
+    g.vmc_sweeps(3, 0.3, 5, rng_mode=1)
+    R = g.positions()
+    o = orc.Crowd(s, nw, delay, 8)
+    o.load_walkers(R)
+    o.evaluate_log()
+    # the GPU's tracked state against the oracle's fresh one: compare after a GPU recompute
+    g.mw_evaluateLog()
+    w, e, pos, _ = quadrature_moves(s, R, 2.5, np.random.default_rng(3))
+    assert len(w) > 100
+    rg = g.mw_evaluateRatios(w, e, pos)
+    ro = o.evaluate_ratios(w, e, pos)
+    err = rel_errors(rg, ro)
+    near = np.abs(ro) < 1e-2
+    assert np.all(err[~near] <= 1e-10), np.max(err[~near])
+    assert np.all(err[near] <= 1e-8), np.max(err[near])
+    # onto the electron's own position: ratio 1
+    ee = np.arange(s.n_elec)
+    ones = g.mw_evaluateRatios(np.repeat(np.arange(nw), s.n_elec), np.tile(ee, nw), R.reshape(-1, 3))
+    np.testing.assert_allclose(ones, 1.0, rtol=1e-9)
+    # onto a proposed position: the ratio of the move
+    iat = 3
+    target = R[:, iat, :] + np.random.default_rng(4).normal(size=(nw, 3)) * 0.3
+    vr = g.mw_evaluateRatios(np.arange(nw), np.full(nw, iat), target)
+    g.mw_evalGrad(iat)
+    g.mw_makeMove(iat, target - R[:, iat, :])
+    r, _ = g.mw_calcRatioGrad(iat)
+    np.testing.assert_allclose(vr, r, rtol=1e-10, atol=1e-13)
+
+
+def test_virtual_move_ratios_fp32_c1():
+    """The 384-electron system in FP32 against the FP64 oracle (fresh inverses on both)."""
+    Crowd, DeviceSystem = _gpu()
+    nw = 4
+    s = make_system("c1_384e")
+    g = Crowd(DeviceSystem(s), nw, s.spec.delay)
+    g.load_walkers(make_walkers(s, nw, seed=73))
+    g.mw_evaluateLog()
+    g.vmc_sweeps(20, 0.3, 6, rng_mode=1, flush=3)
+    R = g.positions()
+    g.load_walkers(R)
+    g.mw_evaluateLog()
+    orc.set_threads(os.cpu_count() or 1)
+    o = orc.Crowd(s, nw, s.spec.delay, 8)
+    o.load_walkers(R)
+    o.evaluate_log(nthreads=os.cpu_count() or 1)
+    w, e, pos, _ = quadrature_moves(s, R, 2.0, np.random.default_rng(5))
+    rg = g.mw_evaluateRatios(w, e, pos)
+    ro = o.evaluate_ratios(w, e, pos)
+    err = rel_errors(rg, ro, floor=1e-300)
+    away = np.abs(ro) > 1e-2
+    table = {"moves": int(len(w)), "walkers": nw,
+             "ratio_rel": {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
+                           "max": float(err.max())},
+             "ratio_rel_away_from_nodes": {"median": float(np.median(err[away])),
+                                           "p99": float(np.percentile(err[away], 99)),
+                                           "max": float(err[away].max())}}
+    print("c1_384e_nlpp", json.dumps(table))
+    path = os.environ.get("QMCG_ERROR_TABLE")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps({"workload": "c1_384e_virtual_moves", **table}) + "\n")
+    assert table["ratio_rel"]["median"] < 1e-4
+    assert table["ratio_rel_away_from_nodes"]["p99"] < 1e-2

@@ -198,3 +198,44 @@ def test_replay_philox_reproduces_own_chain(delay):
     d.evaluate_log()
     td, _ = d.replay_philox(tc, seed=31, tau=0.3)
     assert td[0, 2, 1, 10] != tc[0, 2, 1, 10]
+
+
+def test_virtual_move_ratio_equals_real_move():
+    """The ratio of a virtual move equals mw_calcRatioGrad's ratio of the same move, and a
+    virtual move onto the electron's own position has ratio 1."""
+    s = small_system(3)
+    R = make_walkers(s, 3, seed=12)
+    c = orc.Crowd(s, 3, 3, 8)
+    c.load_walkers(R)
+    c.evaluate_log()
+    c.vmc_sweeps_philox(seed=5, nsteps=1, tau=0.3)
+    Rn = c.positions()
+    iat = 6
+    rng = np.random.default_rng(1)
+    target = Rn[:, iat, :] + rng.normal(size=(3, 3)) * 0.4
+    vr = c.evaluate_ratios(np.arange(3), np.full(3, iat), target)
+    same = c.evaluate_ratios(np.arange(3), np.full(3, iat), Rn[:, iat, :])
+    np.testing.assert_allclose(same, 1.0, rtol=1e-10)
+    c.eval_grad(iat)
+    c.make_move(iat, target - Rn[:, iat, :])
+    r, _ = c.ratio_grad(iat)
+    np.testing.assert_allclose(vr, r, rtol=1e-10)
+
+
+def test_quadrature_moves_geometry():
+    from qmcpack_gb300.nlpp import icosahedron, quadrature_moves
+    u = icosahedron()
+    assert u.shape == (12, 3)
+    np.testing.assert_allclose(np.linalg.norm(u, axis=1), 1.0)
+    np.testing.assert_allclose(u.sum(axis=0), 0.0, atol=1e-12)
+    s = small_system(1)
+    R = make_walkers(s, 2, seed=3)
+    w, e, pos, ion = quadrature_moves(s, R, 3.0, np.random.default_rng(0))
+    assert len(w) % 12 == 0 and len(w) > 0
+    # every point lies on the sphere through its electron around its ion
+    L = s.lattice
+    d_e = R[w, e] - s.ion_pos[ion]
+    d_e -= L * np.round(d_e / L)
+    d_p = pos - s.ion_pos[ion]
+    d_p -= L * np.round(d_p / L)
+    np.testing.assert_allclose(np.linalg.norm(d_p, axis=1), np.linalg.norm(d_e, axis=1), rtol=1e-12)
