@@ -211,6 +211,56 @@ def ratio_error(system, dsys32, nw: int, k: int, nelec: int = 4, R=None):
             "walkers": label}
 
 
+def virtual_moves(crowd, system, peak: float, rcut: float = 2.0, seed: int = 5):
+    """Non-local pseudopotential ratios at the crowd's current configurations: the 12-point
+    quadrature points of every electron within rcut of an ion (qmcg_mw_evaluate_ratios).
+    Device time of the ratio kernel alone (CUDA events, inputs resident) and end to end
+    through the C ABI (host lists in, ratios out)."""
+    from qmcpack_gb300.nlpp import quadrature_moves
+    R = crowd.positions()
+    w, e, pos, _ = quadrature_moves(system, R, rcut, np.random.default_rng(seed))
+    n = len(w)
+    ms = crowd.profile_ratios(w, e, pos, reps=10)
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        crowd.mw_evaluateRatios(w, e, pos)
+    e2e_s = (time.perf_counter() - t0) / reps
+    sz = 4 if system.spec.precision == 4 else 8
+    per = (65 * system.npad + 3 * system.n_elec) * sz
+    achieved = per * n / (ms / 1e3) / 1e9
+    return {"moves": int(n), "per_walker": n / crowd.nw, "cutoff_bohr": rcut, "rule": "12-point icosahedral",
+            "kernel": "vp_ratio_kernel", "ms_per_launch": ms, "moves_per_s": n / (ms / 1e3),
+            "e2e_moves_per_s": n / e2e_s, "algorithmic_bytes_per_move": per,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak}}
+
+
+def dmc_rate(dsys, system, R, flush: int, steps: int = 20, warmup: int = 10, tau: float = 0.02):
+    """Fixed-node DMC steps of the production crowd through the host driver (device step,
+    comb population control, SFNBranch parameters): wall clock of `steps` steps after
+    `warmup` warm-up steps."""
+    from qmcpack_gb300.crowd import Crowd
+    from qmcpack_gb300.dmc import DMCDriver
+    spec = system.spec
+    g = Crowd(dsys, spec.walkers, spec.delay)
+    g.load_walkers(R)
+    g.mw_evaluateLog()
+    d = DMCDriver(g, tau=tau, seed=77, warmup_steps=warmup, flush=flush, recompute_every=spec.recompute_every)
+    d.run(warmup)
+    torch_sync()
+    t0 = time.perf_counter()
+    hist = d.run(steps)
+    dt = time.perf_counter() - t0
+    moves = steps * spec.walkers * system.n_elec
+    acc = sum(h["accepted"] for h in hist) / max(sum(h["accepted"] + h["rejected"] for h in hist), 1)
+    return {"tau": tau, "steps": steps, "warmup_steps": warmup, "ms_per_step": dt / steps * 1e3,
+            "walker_moves_per_s": moves / dt, "acceptance": acc,
+            "e_now_last": hist[-1]["e_now"], "e_trial_last": hist[-1]["e_trial"],
+            "walkers_copied_per_step": float(np.mean([h["copied"] for h in hist])),
+            "step": "fixed-node sweep + local energy + branch weights on the device, comb population control "
+                    "and SFNBranch updates on the host"}
+
+
 def monotonic(x) -> bool:
     d = np.diff(np.asarray(x, np.float64))
     return bool(np.all(d > 0) or np.all(d < 0))
@@ -604,6 +654,10 @@ def run_ours(args, rank: int, world: int):
     base = cpu_baseline(args.workload) if world == 1 and not args.no_cpu_baseline else None
     eff = None
     rerr = None
+    extras = {}
+    if world == 1 and not args.no_extras:
+        extras["virtual_moves"] = virtual_moves(crowd, system, peak)
+        extras["dmc"] = dmc_rate(dsys, system, crowd.positions(), args.flush)
     if world == 1 and not args.no_effective and args.workload == "c1_384e":
         Req = crowd.positions()[:64]
         rerr = {"uniform_start": ratio_error(system, dsys, 64, k),
@@ -646,6 +700,7 @@ def run_ours(args, rank: int, world: int):
         "walker_sweeps_per_s": value / system.n_elec,
         "effective_samples": eff,
         "ratio_error_fp32": rerr,
+        **extras,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -664,6 +719,7 @@ def main():
     ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
                     help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
     ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
+    ap.add_argument("--no-extras", action="store_true", help="skip the virtual-move and DMC measurements")
     ap.add_argument("--eff-sweeps", type=int, default=500, help="measured sweeps per method in the comparison")
     ap.add_argument("--eff-block", type=int, default=250, help="sweeps per equilibration block")
     ap.add_argument("--eff-min-blocks", type=int, default=8, help="fewest equilibration blocks")

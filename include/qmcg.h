@@ -445,6 +445,12 @@ int qmcg_profile_sweep(qmcg_crowd crowd, int num_sweeps, double* out4);
  * crowd freshly recomputed; returns QMCG_ERR_STATE while delayed updates are pending. */
 int qmcg_profile_recompute(qmcg_crowd crowd, double* ms);
 
+/* Measurement helper (no reference counterpart): device time in ms of one launch of the
+ * virtual-move ratio kernel of qmcg_mw_evaluate_ratios on these moves (inputs uploaded once,
+ * reps launches timed with CUDA events on the crowd's stream). */
+int qmcg_profile_ratios(qmcg_crowd crowd, int num_moves, const int* walker, const int* electron, const double* pos,
+                        int reps, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -210,6 +210,15 @@ class Crowd:
         check(self.L.qmcg_mw_evaluate_ratios(self.handle, wk.size, _p(wk, _ip), _p(el, _ip), _p(ps), _p(r)))
         return r
 
+    def profile_ratios(self, walker, electron, pos, reps: int = 10) -> float:
+        """Device ms of one launch of the virtual-move ratio kernel on these moves."""
+        wk = np.ascontiguousarray(walker, np.int32).ravel()
+        el = np.ascontiguousarray(electron, np.int32).ravel()
+        ps = _d(pos).reshape(-1, 3)
+        ms = C.c_double()
+        check(self.L.qmcg_profile_ratios(self.handle, wk.size, _p(wk, _ip), _p(el, _ip), _p(ps), reps, C.byref(ms)))
+        return ms.value
+
     # ---- diffusion Monte Carlo
     def dmc_init(self):
         """Weights 1, ages 0; returns the local energy of every walker (the first E_old)."""

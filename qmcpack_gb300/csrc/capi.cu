@@ -477,6 +477,8 @@ struct qmcg_crowd_s
   virtual int dmc_copy(const int* src) = 0;
   virtual int dmc_reconfigure(double u, int* src) = 0;
   virtual int evaluate_ratios(int nvp, const int* walker, const int* elec, const double* pos, double* ratios) = 0;
+  virtual int profile_ratios(int nvp, const int* walker, const int* elec, const double* pos, int reps,
+                             double* ms) = 0;
 };
 
 // The comb of population control with a fixed walker count
@@ -678,6 +680,7 @@ struct Crowd final : qmcg_crowd_s
     d.grid_scale[2] = static_cast<T>(sys->grid[2] / sys->L[2]);
     d.ions        = static_cast<const T*>(sys->ions);
     d.ion_species = sys->ion_species;
+    d.j1_nspecies = sys->nion_species;
     d.j1c         = static_cast<const T*>(sys->j1c);
     d.j1_ncoef    = sys->j1_ncoef;
     d.j1_maxidx   = sys->j1_ncoef - 4;
@@ -737,7 +740,8 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&unif_d, nu));
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
-    sweep_nt = sweep_default_threads<T>(d);
+    sweep_nt   = sweep_default_threads<T>(d);
+    d.seg_smem = sweep_seg_smem<T>(d) ? 1 : 0;
     CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size, false, sweep_nt));
     CUDA_TRY(setup_local_energy<T>());
     CUDA_TRY(mem.alloc(&e_out, 3 * (size_t)nw));
@@ -799,6 +803,8 @@ struct Crowd final : qmcg_crowd_s
     if (any)
     {
       CUDA_TRY(cudaMemsetAsync(s.status, 0, nw * sizeof(int), stream));
+      if (any & ST_TIMEOUT)
+        return fail(QMCG_ERR_CUDA, "walker-resident sweep: a bounded wait on an asynchronous copy timed out");
       if (any & ST_SINGULAR)
         return fail(QMCG_ERR_SINGULAR, "singular Slater matrix");
       if (any & ST_NONFINITE)
@@ -1391,6 +1397,32 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, stream));
     CUDA_TRY(cudaMemcpyAsync(ratios, vp.ratios, nvp * sizeof(double), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
+  }
+
+  // device time of the virtual-move ratio kernel alone: inputs uploaded once, reps launches
+  // timed with CUDA events on the crowd's stream
+  int profile_ratios(int nvp, const int* walker, const int* elec, const double* pos, int reps, double* ms) override
+  {
+    if (nvp <= 0 || reps <= 0 || !ms)
+      return fail(QMCG_ERR_ARG, "bad profile arguments");
+    std::vector<double> r(nvp);
+    int rc = evaluate_ratios(nvp, walker, elec, pos, r.data()); // validates, uploads, warms up
+    if (rc)
+      return rc;
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    CUDA_TRY(cudaEventRecord(a, stream));
+    for (int i = 0; i < reps; i++)
+      CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, stream));
+    CUDA_TRY(cudaEventRecord(b, stream));
+    CUDA_TRY(cudaEventSynchronize(b));
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = t / reps;
     return QMCG_OK;
   }
 
@@ -2133,6 +2165,8 @@ struct Crowd final : qmcg_crowd_s
       CUDA_TRY(cudaMemsetAsync(tc_err, 0, sizeof(int), stream));
       return fail(QMCG_ERR_CUDA, "tensor-core flush: an mbarrier wait timed out");
     }
+    if (any & ST_TIMEOUT)
+      return fail(QMCG_ERR_CUDA, "walker-resident sweep: a bounded wait on an asynchronous copy timed out");
     if (any & ST_SINGULAR)
       return fail(QMCG_ERR_SINGULAR, "singular Slater matrix");
     if (any & ST_NONFINITE)
@@ -2548,6 +2582,11 @@ extern "C" int qmcg_dmc_step(qmcg_crowd c, const qmcg_sweep_params* p, const qmc
 }
 extern "C" int qmcg_dmc_copy_walkers(qmcg_crowd c, const int* src) { CROWD_CALL(c, dmc_copy(src)); }
 extern "C" int qmcg_dmc_reconfigure(qmcg_crowd c, double u, int* src) { CROWD_CALL(c, dmc_reconfigure(u, src)); }
+extern "C" int qmcg_profile_ratios(qmcg_crowd c, int nvp, const int* walker, const int* elec, const double* pos,
+                                   int reps, double* ms)
+{
+  CROWD_CALL(c, profile_ratios(nvp, walker, elec, pos, reps, ms));
+}
 extern "C" int qmcg_mw_evaluate_ratios(qmcg_crowd c, int nvp, const int* walker, const int* elec, const double* pos,
                                        double* ratios)
 {

@@ -25,6 +25,7 @@ enum : int
   ST_ILLCOND     = 8,  // the tracked inverse lost accuracy: |Ainv[row] . phi(r_row) - 1| above tolerance
   ST_ILLCOND_UP  = 16, // the same, found in the spin-up determinant only
   ST_ILLCOND_DN  = 32, // the same, found in the spin-down determinant only
+  ST_TIMEOUT     = 64, // a bounded wait on an asynchronous copy ran out (the walker was skipped)
   ST_REPAIR_MASK = ST_NONFINITE | ST_ILLCOND | ST_ILLCOND_UP | ST_ILLCOND_DN,
 };
 
@@ -122,6 +123,10 @@ struct DevState
   // rejected, and rr [nw][2] accumulates tau |xi|^2 over the proposed and the accepted moves
   int dmc;
   double* rr;
+  // the walker-resident sweep keeps a segment's inverse rows in shared memory (set by the host
+  // when that does not enlarge the kernel's shared-memory footprint)
+  int seg_smem;
+  int j1_nspecies; // ion species of the one-body functors (rows of j1c)
 };
 
 // fields of one move record of the walker-resident sweep (qmcg_vmc_sweeps_trace)
@@ -272,6 +277,11 @@ __device__ __forceinline__ T functor_eval(const T* __restrict__ c, T dri, int ma
       c3 * (((T(1.0 / 6.0) * t + T(0.0)) * t + T(0.0)) * t + T(0.0));
 }
 
+// 1/sqrt(x): one special-function instruction in FP32 (rsqrtf, at most 2 ulp), the
+// library rsqrt in FP64
+__device__ __forceinline__ float inv_sqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double inv_sqrt(double x) { return rsqrt(x); }
+
 // orthorhombic minimum image of d = R_j - r (DTD_BConds<T,3,PPPO>)
 template<typename T>
 __device__ __forceinline__ T min_image(T d, T L, T Linv)
@@ -319,10 +329,10 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T* scratch)
 // Inside a warp a reduce-scatter halves the values a lane keeps at every step (16
 // shuffles for 16 values instead of 5 per value) until lane l holds the warp's total of
 // value l / 2; warp 0 then adds the warps' totals and broadcasts them to its lanes.
-// scratch: 16 * 32 elements.  No trailing barrier: the caller synchronises before scratch
-// is written again.
+// scratch: 16 * stride elements, stride >= the number of warps.  No trailing barrier: the
+// caller synchronises before scratch is written again.
 template<typename T, int NV>
-__device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch)
+__device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch, int stride = 32)
 {
   static_assert(NV <= 16, "up to 16 values");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
@@ -344,14 +354,14 @@ __device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch)
   }
   x[0] += __shfl_xor_sync(0xffffffffu, x[0], 1);
   if ((lane & 1) == 0 && (lane >> 1) < NV)
-    scratch[(lane >> 1) * 32 + wid] = x[0];
+    scratch[(lane >> 1) * stride + wid] = x[0];
   __syncthreads();
   if (wid == 0)
   {
     T t = T(0);
     if (lane < NV)
       for (int w = 0; w < nwarp; w++)
-        t += scratch[lane * 32 + w];
+        t += scratch[lane * stride + w];
 #pragma unroll
     for (int q = 0; q < NV; q++)
       v[q] = __shfl_sync(0xffffffffu, t, q);

@@ -33,7 +33,10 @@ cudaError_t setup_recompute_kernels();
 template<typename T>
 cudaError_t setup_sweep_kernel();
 template<typename T>
-size_t sweep_smem_bytes(const DevState<T>& s);
+size_t sweep_smem_bytes(const DevState<T>& s, bool learned = false);
+// whether a segment's inverse rows can be staged in shared memory without enlarging the footprint
+template<typename T>
+bool sweep_seg_smem(const DevState<T>& s);
 template<typename T>
 cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned = false, int threads = 128);
 template<typename T>

@@ -10,14 +10,21 @@
 // the state update (mw_accept_rejectMove).  Segments end where the delayed
 // update fills its window (DelayedUpdateBatched::mw_updateInvMat,
 // DelayedUpdateBatched.h:675-738); that flush runs batched over all walkers in
-// flush_kernels.cu.
+// flush_kernels.cu / flush_tc.cu.
 //
 // Per CTA the walker's positions, two-body Jastrow state and the delayed-update
-// matrix Binv stay in shared memory for the segment; the next electron's inverse
-// row, orbital-gradient rows and orbital values are prefetched with cp.async
-// while the current electron is evaluated.  Driver arithmetic (Box-Muller
-// Gaussians, drift, Green's functions) runs in the move-loop precision, as the
-// reference's mixed-precision build does in RealType.
+// matrix Binv stay in shared memory for the segment.  Where it does not enlarge the
+// kernel's shared-memory footprint, the segment's inverse rows (the rows of its k
+// electrons, which the delayed update reads as V and the accepted moves read against
+// the new orbital row) arrive in shared memory at the start of the segment by one
+// bulk asynchronous copy completing on an mbarrier; the next electron's orbital
+// gradient and value rows are prefetched with cp.async while the current one is
+// evaluated.  The evaluation at the proposed position is split by warps: the first
+// warps own orbital pairs and read all 64 coefficient rows of the grid cell for them
+// (8-byte loads contiguous over orbitals, the value, gradient and Laplacian formed in
+// registers), the remaining warp(s) compute the one- and two-body Jastrow rows at the
+// same time.  Driver arithmetic (Box-Muller Gaussians, drift, Green's functions) runs
+// in the move-loop precision, as the reference's mixed-precision build does in RealType.
 #include <algorithm>
 #include <type_traits>
 
@@ -25,6 +32,7 @@
 #include "launch.h"
 #include "learned.cuh"
 #include "spline.cuh"
+#include "tc.cuh"
 
 namespace qmcg
 {
@@ -36,18 +44,67 @@ struct SweepCfg
   static constexpr int MINB = sizeof(T) == 4 ? 4 : 2;
 };
 
-template<typename T>
-static size_t sweep_smem_elems(const DevState<T>& s)
+// network scratch of the learned proposal: features, activations, reduction scratch, outputs
+constexpr int ML_SCRATCH_FLOATS = ML_IN + 2 * ML_H + ML_NOUT * 4 + 8;
+
+// shared-memory layout of the resident sweep (offsets in elements of T, every region on a
+// 16-byte boundary)
+struct SweepLayout
 {
-  return (size_t)28 * s.lda    // spline partials
-      + (size_t)10 * s.lda     // prefetch double buffer (inverse row, dgrad xyz, orbital values)
-      + 2 * (size_t)s.lda      // up-to-date inverse row, spare row (keeps 16-byte alignment)
-      + 5 * (size_t)s.lda      // orbital VGL at the proposed position
-      + 8 * (size_t)s.ne_pad   // positions, J2 state
-      + (size_t)s.k * s.k      // Binv
-      + 3 * (size_t)s.k        // p, t, y
-      + 16 * 32                // block reductions
-      + (size_t)s.k * (s.k - 1) / 2; // U_c . Ainv[row_x] of the segment, c < x
+  int npre; // rows per prefetch buffer: dgrad xyz, values (+ the inverse row when the segment rows are not staged)
+  int pre, invrow, phi, Rs, J2s, Bs, pv, tv, yv, red, tri, seg, ml, coef, total;
+};
+
+template<typename T>
+__host__ __device__ inline SweepLayout sweep_layout(int lda, int ne_pad, int K, bool seg_smem, bool learned,
+                                                   int ncoef)
+{
+  constexpr int a = 16 / (int)sizeof(T);
+  auto up         = [](int x) { return (x + a - 1) / a * a; };
+  SweepLayout L;
+  int o    = 0;
+  L.npre   = seg_smem ? 4 : 5;
+  L.pre    = o, o += up(2 * L.npre * lda);
+  L.invrow = o, o += up(lda);
+  L.phi    = o, o += up(5 * lda);
+  L.Rs     = o, o += up(3 * ne_pad);
+  L.J2s    = o, o += up(5 * ne_pad);
+  L.Bs     = o, o += up(K * K);
+  L.pv     = o, o += up(K);
+  L.tv     = o, o += up(K);
+  L.yv     = o, o += up(K);
+  L.red    = o, o += up(16 * 16); // block reductions of up to 16 values over up to 16 warps
+  L.tri    = o, o += up(K * (K - 1) / 2);
+  L.seg    = o, o += up(seg_smem ? K * lda : (K == 1 ? lda : 0)); // the segment's rows, or the rank-1 scratch
+  L.ml     = o, o += learned ? up((ML_SCRATCH_FLOATS * 4 + (int)sizeof(T) - 1) / (int)sizeof(T)) : 0;
+  L.coef   = o, o += up(ncoef); // the J2 (same, opposite spin) and J1 (per species) functor coefficients
+  L.total  = o;
+  return L;
+}
+
+// the footprint of the previous design (spline partials in shared memory, every row
+// from global memory): the segment rows are staged only where they fit inside it
+template<typename T>
+static size_t sweep_smem_reference(int lda, int ne_pad, int K)
+{
+  return sizeof(T) * ((size_t)45 * lda + 8 * (size_t)ne_pad + (size_t)K * K + 3 * (size_t)K + 512 +
+                      (size_t)K * (K - 1) / 2);
+}
+
+// functor coefficients staged per CTA
+template<typename T>
+__host__ __device__ inline int sweep_ncoef(const DevState<T>& s)
+{
+  return (s.has_j2 ? 2 * s.j2_ncoef : 0) + (s.has_j1 ? s.j1_nspecies * s.j1_ncoef : 0);
+}
+
+template<typename T>
+bool sweep_seg_smem(const DevState<T>& s)
+{
+  if (s.k <= 1)
+    return false;
+  const SweepLayout L = sweep_layout<T>(s.lda, s.ne_pad, s.k, true, false, sweep_ncoef(s));
+  return sizeof(T) * (size_t)L.total <= sweep_smem_reference<T>(s.lda, s.ne_pad, s.k);
 }
 
 // cp.async of n_elems elements (a multiple of 16 bytes) from global to shared
@@ -65,19 +122,35 @@ __device__ __forceinline__ void async_copy(T* dst, const T* src, int n_elems, in
 __device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// rows of electron `row` of spin slot into pre[5][lda]: inverse row, dgrad xyz, orbital values
+// rows of electron `row` of spin slot into pre: [inverse row,] dgrad xyz, orbital values
 template<typename T>
-__device__ __forceinline__ void prefetch_rows(const DevState<T>& s, size_t slot, int row, T* pre, int tid, int nt)
+__device__ __forceinline__ void prefetch_rows(const DevState<T>& s, size_t slot, int row, T* pre, bool with_inv,
+                                              int tid, int nt)
 {
   const int n = s.norb;
-  async_copy(pre, s.Ainv + (slot * n + row) * s.lda, s.lda, tid, nt);
-  async_copy(pre + s.lda, s.dgrad + ((slot * n + row) * 3) * s.lda, 3 * s.lda, tid, nt);
-  async_copy(pre + 4 * s.lda, s.psiv + (slot * n + row) * s.lda, s.lda, tid, nt);
+  if (with_inv)
+  {
+    async_copy(pre, s.Ainv + (slot * n + row) * s.lda, s.lda, tid, nt);
+    pre += s.lda;
+  }
+  async_copy(pre, s.dgrad + ((slot * n + row) * 3) * s.lda, 3 * s.lda, tid, nt);
+  async_copy(pre + 3 * s.lda, s.psiv + (slot * n + row) * s.lda, s.lda, tid, nt);
   async_commit();
 }
 
-// out[c] = scale * (rows[c] . x) for c < nrows (rows in global memory, stride ld,
-// x in shared memory): every warp owns up to 8 rows and issues the loads of four
+// bulk asynchronous copy global -> shared completing on an mbarrier (16-byte aligned, size a
+// multiple of 16); issued by one thread after it announced the byte count on the barrier
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint32_t mbar)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+// out[c] = scale * (rows[c] . x) for c < nrows (rows in shared or global memory, stride
+// ld, x in shared memory): every warp owns up to 8 rows and issues the loads of four
 // 32-column strips of all of them (32 loads in flight) before the first product
 template<typename T, int NT>
 __device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const T* x, int n, T* out, T scale)
@@ -123,6 +196,65 @@ __device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const
   }
 }
 
+// Orbital values, gradients and Laplacians of the orbital pair starting at orbital o0 at
+// the grid cell (ix, iy, iz): all 64 coefficient rows of the cell for these two orbitals,
+// read plane by plane (16 loads in flight), the tricubic sums in registers
+// (spline2::evaluate_vgh_impl, MultiBsplineVGLH.hpp:120-230, and SplineR2R::assign_vgl,
+// SplineR2R.cpp:338-374, for an orthorhombic cell).  out[q][w]: q = value, gradient xyz,
+// Laplacian of orbital o0 + w.
+template<typename T>
+__device__ __forceinline__ void spline_pair_vgl(const DevState<T>& s, const T* origin, int o0, const T a[4],
+                                                const T da[4], const T d2a[4], const T b[4], const T db[4],
+                                                const T d2b[4], const T c[4], const T dc[4], const T d2c[4],
+                                                T (&out)[5][2])
+{
+  T acc[7][2];
+#pragma unroll
+  for (int q = 0; q < 7; q++)
+    acc[q][0] = acc[q][1] = T(0);
+  const T* base = origin + o0;
+#pragma unroll 1
+  for (int i = 0; i < 4; i++)
+  {
+    T v[4][4][2];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        Vec<T>::load(base + i * s.xs + j * s.ys + k * s.zs, v[j][k]);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+    {
+      const T pre00 = a[i] * b[j], pre10 = da[i] * b[j], pre01 = a[i] * db[j], pre20 = d2a[i] * b[j],
+              pre02 = a[i] * d2b[j];
+#pragma unroll
+      for (int w = 0; w < 2; w++)
+      {
+        const T s0 = c[0] * v[j][0][w] + c[1] * v[j][1][w] + c[2] * v[j][2][w] + c[3] * v[j][3][w];
+        const T s1 = dc[0] * v[j][0][w] + dc[1] * v[j][1][w] + dc[2] * v[j][2][w] + dc[3] * v[j][3][w];
+        const T s2 = d2c[0] * v[j][0][w] + d2c[1] * v[j][1][w] + d2c[2] * v[j][2][w] + d2c[3] * v[j][3][w];
+        acc[0][w] += pre00 * s0;
+        acc[1][w] += pre10 * s0;
+        acc[2][w] += pre01 * s0;
+        acc[3][w] += pre00 * s1;
+        acc[4][w] += pre20 * s0;
+        acc[5][w] += pre02 * s0;
+        acc[6][w] += pre00 * s2;
+      }
+    }
+  }
+  const T fx = s.grid_scale[0], fy = s.grid_scale[1], fz = s.grid_scale[2];
+#pragma unroll
+  for (int w = 0; w < 2; w++)
+  {
+    out[0][w] = acc[0][w];
+    out[1][w] = acc[1][w] * fx;
+    out[2][w] = acc[2][w] * fy;
+    out[3][w] = acc[3][w] * fz;
+    out[4][w] = acc[4][w] * (fx * fx) + acc[5][w] * (fy * fy) + acc[6][w] * (fz * fz);
+  }
+}
+
 // shared scratch of the learned proposal (empty for the drift-diffusion kernel)
 template<typename T, bool LEARNED>
 struct LearnedSmem
@@ -134,11 +266,6 @@ struct LearnedSmem<T, true>
   T g[3];
   T p;
 };
-// the network's features, activations, reduction scratch and outputs live in the spline
-// partials buffer, which is free while the network runs (before the spline partials of
-// the proposed position are formed, and after they are combined)
-constexpr int ML_SCRATCH_FLOATS = ML_IN + 2 * ML_H + ML_NOUT * 4 + 8;
-static_assert(ML_SCRATCH_FLOATS * 4 <= 28 * 16 * 4, "the network scratch fits the partials of the smallest padding");
 
 // per-CTA scalars of the resident sweep in shared memory
 template<typename T, bool LEARNED>
@@ -155,7 +282,20 @@ struct SweepShared
   T det;
   T cur[10];
   LearnedSmem<T, LEARNED> lsm;
+  unsigned long long seg_bar; // mbarrier of the segment rows' bulk copy
+  int seg_phase;              // its parity
 };
+
+template<typename T, bool LEARNED>
+__device__ __forceinline__ void sweep_shared_init(SweepShared<T, LEARNED>& sh)
+{
+  if (threadIdx.x == 0)
+  {
+    mbar_init(smem_u32(&sh.seg_bar));
+    sh.seg_phase = 0;
+  }
+  __syncthreads();
+}
 
 // The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.
 template<typename T, int NT, bool LEARNED>
@@ -164,25 +304,30 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
                                              unsigned long long& n_rej)
 {
   const int lda = s.lda, n = s.norb, K = s.k;
-  T* part   = reinterpret_cast<T*>(smem_raw); // 28 x lda
-  T* pre    = part + 28 * lda;                // 2 x 5 x lda prefetch buffers
-  T* invrow = pre + 10 * lda;                 // lda
-  T* spare  = invrow + lda;                   // lda
-  T* phi    = spare + lda;                    // 5 x lda
-  T* Rs     = phi + 5 * lda;                  // 3 x ne_pad
-  T* J2s    = Rs + 3 * s.ne_pad;              // 5 x ne_pad
-  T* Bs     = J2s + 5 * s.ne_pad;             // K x K
-  T* pv     = Bs + K * K;                     // K
-  T* tv     = pv + K;                         // K
-  T* yv     = tv + K;                         // K
-  T* red    = yv + K;                         // 16 x 32
-  T* tri    = red + 16 * 32;                  // K (K - 1) / 2: entry x (x - 1) / 2 + c = U_c . Ainv[row_x]
+  const bool seg_smem  = K > 1 && s.seg_smem != 0;
+  const SweepLayout Ly = sweep_layout<T>(lda, s.ne_pad, K, seg_smem, LEARNED, sweep_ncoef(s));
+  T* sm     = reinterpret_cast<T*>(smem_raw);
+  T* pre    = sm + Ly.pre;    // 2 x npre x lda prefetch buffers
+  T* invrow = sm + Ly.invrow; // lda
+  T* phi    = sm + Ly.phi;    // 5 x lda
+  T* Rs     = sm + Ly.Rs;     // 3 x ne_pad
+  T* J2s    = sm + Ly.J2s;    // 5 x ne_pad
+  T* Bs     = sm + Ly.Bs;     // K x K
+  T* pv     = sm + Ly.pv;     // K
+  T* tv     = sm + Ly.tv;     // K
+  T* yv     = sm + Ly.yv;     // K
+  T* red    = sm + Ly.red;    // 16 x NT/32
+  T* tri    = sm + Ly.tri;    // K (K - 1) / 2: entry x (x - 1) / 2 + c = U_c . Ainv[row_x]
+  T* seg    = sm + Ly.seg;    // the segment's inverse rows (K x lda), or the rank-1 scratch
+  constexpr int NW = NT / 32;
   const __nv_bfloat162* ml_pairs = reinterpret_cast<const __nv_bfloat162*>(s.mlp_simt);
   const __nv_bfloat16* ml_w4 = reinterpret_cast<const __nv_bfloat16*>(ml_pairs + MS_NPAIRS);
-  float* ml_x   = reinterpret_cast<float*>(part); // ML_SCRATCH_FLOATS <= 28 * lda elements of part
+  float* ml_x   = reinterpret_cast<float*>(sm + Ly.ml);
   float* ml_h   = ml_x + ML_IN;
   float* ml_red = ml_h + 2 * ML_H;
   float* ml_out = ml_red + ML_NOUT * 4;
+  (void)ml_w4;
+  (void)ml_out;
 
   const uint32_t sweep = static_cast<uint32_t>(*s.sweep_counter);
   const uint32_t k0 = static_cast<uint32_t>(s.seed), k1 = static_cast<uint32_t>(s.seed >> 32);
@@ -192,17 +337,61 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   const int spin    = i0 >= s.nup ? 1 : 0;
   const int first   = spin ? s.nup : 0;
   const int lane    = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  (void)spare;
-  (void)ml_w4;
-  (void)ml_out;
+  // warps [0, spw) evaluate the orbitals (orbital pairs, one or more per thread), the others the
+  // Jastrow rows; every thread reads the functor coefficients from shared memory
+  const int pairs   = lda / 2;
+  const int spw     = max(1, min(NW - 1, (pairs + 31) / 32));
+  const bool spline_thread = wid < spw;
+  T* coef           = sm + Ly.coef;
+  const T* j2c      = coef;                                   // [2][j2_ncoef]
+  const T* j1c      = coef + (s.has_j2 ? 2 * s.j2_ncoef : 0); // [species][j1_ncoef]
 
   {
     const size_t slot = (size_t)spin * s.nw + w;
+    const T* ainv_seg = s.Ainv + (slot * n + (i0 - first)) * lda; // rows of this segment's electrons
+    if (seg_smem && threadIdx.x == 0)
+    {
+      // the previous walker's reads of seg (generic proxy) precede this copy (async proxy)
+      fence_async_smem();
+      bulk_copy_g2s(seg, ainv_seg, (uint32_t)((i1 - i0) * lda * sizeof(T)), smem_u32(&sh.seg_bar));
+    }
     for (int e = threadIdx.x; e < 3 * s.ne_pad; e += NT)
       Rs[e] = s.Rt[(size_t)w * 3 * s.ne_pad + e];
     for (int e = threadIdx.x; e < 5 * s.ne_pad; e += NT)
       J2s[e] = s.J2[(size_t)w * 5 * s.ne_pad + e];
-    prefetch_rows(s, slot, i0 - first, pre, threadIdx.x, NT);
+    if (s.has_j2)
+      for (int e = threadIdx.x; e < 2 * s.j2_ncoef; e += NT)
+        coef[e] = s.j2c[e];
+    if (s.has_j1)
+      for (int e = threadIdx.x; e < s.j1_nspecies * s.j1_ncoef; e += NT)
+        coef[(s.has_j2 ? 2 * s.j2_ncoef : 0) + e] = s.j1c[e];
+    prefetch_rows(s, slot, i0 - first, pre, !seg_smem, threadIdx.x, NT);
+    if (seg_smem)
+    {
+      const int phase = sh.seg_phase;
+      bool ok         = mbar_wait(smem_u32(&sh.seg_bar), (uint32_t)phase);
+      if (__syncthreads_or(!ok))
+      {
+        // a copy that did not complete in time: record it, let the copy finish (bounded)
+        // before the shared memory is used again, and skip this walker's segment
+        if (!ok)
+          mbar_wait(smem_u32(&sh.seg_bar), (uint32_t)phase);
+        if (threadIdx.x == 0)
+        {
+          atomicOr(s.status + w, ST_TIMEOUT);
+          sh.seg_phase = phase ^ 1;
+        }
+        async_wait_all();
+        __syncthreads();
+        return;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0)
+        sh.seg_phase = phase ^ 1;
+    }
+    // the segment's rows: V (the inverse rows of the earlier electrons, fixed during a
+    // segment) and the rows the accepted moves are multiplied with
+    const T* segrows = seg_smem ? seg : ainv_seg;
     int dc = 0;
     // DMC: tau |xi|^2 of this segment's proposed and accepted moves (thread 0)
     double rr_prop = 0, rr_acc = 0;
@@ -213,9 +402,11 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
     for (int iat = i0; iat < i1; iat++)
     {
       const int row = iat - first;
-      T* arow       = pre + ((iat - i0) & 1) * 5 * lda; // this electron's prefetched rows
-      const T* dg   = arow + lda;
-      const T* pv0  = arow + 4 * lda;
+      T* pb         = pre + ((iat - i0) & 1) * Ly.npre * lda; // this electron's prefetched rows
+      const T* arow = seg_smem ? segrows + (size_t)(iat - i0) * lda : pb;
+      const T* dg   = seg_smem ? pb : pb + lda;
+      const T* pv0  = dg + 3 * lda;
+      T* pnext      = pre + ((iat + 1 - i0) & 1) * Ly.npre * lda;
       // the random numbers of the next 32 electrons, one electron per thread (counter-based:
       // the same values the single-electron calls would draw)
       const int jj = (iat - i0) & 31;
@@ -226,16 +417,19 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         const u4 r2            = philox4x32_10(u4{(uint32_t)w, e, sweep, 2u}, k0, k1);
         sh.runif[threadIdx.x]  = T(u01(r2.x, r2.y));
       }
-      // thread 0's operands of the proposal and the decision, loaded ahead of their use
-      double r_now[3] = {0, 0, 0};
-      T j1_now[4]     = {0, 0, 0, 0}; // Vat, Grad xyz of this electron
-      if (threadIdx.x == 0)
+      // operands of the proposal (lanes 0-2 of warp 0: component `lane` of the position and of
+      // the one-body gradient) and of the decision (thread 0: the one-body value), loaded
+      // ahead of their use
+      double r_me = 0;
+      T j1g_me = 0, j1v_now = 0;
+      if (threadIdx.x < 3)
       {
-        for (int d = 0; d < 3; d++)
-          r_now[d] = s.R[((size_t)w * 3 + d) * s.ne_pad + iat];
+        r_me = s.R[((size_t)w * 3 + threadIdx.x) * s.ne_pad + iat];
         if (s.has_j1)
-          for (int q = 0; q < 4; q++)
-            j1_now[q] = s.J1[((size_t)w * 5 + q) * s.ne_pad + iat];
+        {
+          j1g_me  = s.J1[((size_t)w * 5 + 1 + threadIdx.x) * s.ne_pad + iat];
+          j1v_now = s.J1[((size_t)w * 5) * s.ne_pad + iat];
+        }
       }
       async_wait_all();
       __syncthreads();
@@ -245,7 +439,6 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       T g[4]       = {0, 0, 0, 0};
       if (K > 1 && dc > 0)
       {
-        const T* V = s.V + slot * K * lda;
         // pv_c = U_c . Ainv[row] of the earlier slots of this segment, formed when slot c
         // was decided (zero for a rejected move), read straight from the table
         const T* pvt = tri + dc * (dc - 1) / 2;
@@ -260,7 +453,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         __syncthreads();
         // the next electron's rows arrive while this one is evaluated
         if (iat + 1 < i1)
-          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
+          prefetch_rows(s, slot, row + 1, pnext, !seg_smem, threadIdx.x, NT);
+        const T* V = segrows;
         for (int j = threadIdx.x; j < n; j += NT)
         {
           T a[4] = {0, 0, 0, 0};
@@ -287,8 +481,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
       else
       {
-        if (iat + 1 < i1)
-          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
+        if (iat + 1 < i1 && K > 1)
+          prefetch_rows(s, slot, row + 1, pnext, !seg_smem, threadIdx.x, NT);
         for (int j = threadIdx.x; j < n; j += NT)
         {
           const T x = arow[j];
@@ -297,10 +491,11 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           g[2] += x * dg[2 * lda + j];
           g[3] += x * pv0[j];
         }
+        // rank-1 updates: the next rows are fetched after this electron's update
       }
       // ------------------------------------------------ gradient, health check, proposal
       {
-        block_sum_to0<T, 4>(g, red); // thread 0 uses the sums
+        block_sum_to0<T, 4>(g, red, NW); // thread 0 uses the sums
         if constexpr (LEARNED)
         {
           // the network at the current position: (mu, s) of the proposal
@@ -308,15 +503,17 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           {
             if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
               atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
-            for (int d = 0; d < 3; d++)
-            {
-              T gs = g[d];
-              if (s.has_j1)
-                gs += j1_now[1 + d];
-              if (s.has_j2)
-                gs += J2s[(1 + d) * s.ne_pad + iat];
-              sh.lsm.g[d] = gs;
-            }
+          }
+          if (threadIdx.x < 3)
+          {
+            const int d = threadIdx.x;
+            T gs        = d == 0 ? g[0] : (d == 1 ? g[1] : g[2]);
+            if (s.has_j1)
+              gs += j1g_me;
+            if (s.has_j2)
+              gs += J2s[(1 + d) * s.ne_pad + iat];
+            sh.lsm.g[d] = gs;
+            sh.pos[d]   = r_me; // the current position, read back by thread 0 below
           }
           __syncthreads();
           const T pc[3] = {Rs[iat], Rs[s.ne_pad + iat], Rs[2 * s.ne_pad + iat]};
@@ -337,7 +534,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
               x2 += sh.rgauss[jj][d] * sh.rgauss[jj][d];
               const T dd = drift[d] + st * mu + st * exp(sd) * sh.rgauss[jj][d];
               sh.disp[d]  = dd;
-              sh.pos[d]   = r_now[d] + static_cast<double>(dd);
+              sh.pos[d]   = sh.pos[d] + static_cast<double>(dd);
               sh.posT[d]  = static_cast<T>(sh.pos[d]);
             }
             spline_frac(s, sh.pos, sh.ru);
@@ -347,78 +544,121 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         }
         else
         {
-        if (threadIdx.x == 0)
+        if (threadIdx.x < 32)
         {
-          if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
-            atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
-          T gn[3];
-          for (int d = 0; d < 3; d++)
-          {
-            T gs = g[d];
-            if (s.has_j1)
-              gs += j1_now[1 + d];
-            if (s.has_j2)
-              gs += J2s[(1 + d) * s.ne_pad + iat];
-            gn[d] = gs;
-          }
-          if (s.trace)
-          {
-            double* tr = s.trace + ((size_t)iat * s.nw + w) * TRACE_FIELDS;
-            for (int d = 0; d < 3; d++)
-              tr[TR_GRAD_NOW + d] = static_cast<double>(gn[d]);
-            tr[TR_SELF] = static_cast<double>(g[3]);
-          }
-          const T sqrttau = sqrt(tau);
-          T delta[3], drift[3];
-          for (int d = 0; d < 3; d++)
-            delta[d] = sh.rgauss[jj][d] * sqrttau;
+          // drift-diffusion proposal (DriftModifierUNR::getDrift and the Gaussian step of
+          // VMCBatched::advanceWalkers): lane d < 3 forms component d; |grad|^2 and |delta|^2
+          // are gathered across the three lanes
+          const int d = lane < 3 ? lane : 0;
+          T gs = d == 0 ? g[0] : (d == 1 ? g[1] : g[2]);
+          if (s.has_j1)
+            gs += j1g_me;
+          if (s.has_j2)
+            gs += J2s[(1 + d) * s.ne_pad + iat];
+          const T g2  = gs * gs;
+          const T vsq = __shfl_sync(0xffffffffu, g2, 0) + __shfl_sync(0xffffffffu, g2, 1) +
+              __shfl_sync(0xffffffffu, g2, 2);
+          const T delta = sh.rgauss[jj][d] * sqrt(tau);
+          T drift       = delta;
           if (s.use_drift)
           {
-            unr_drift_t(tau, gn, drift);
-            for (int d = 0; d < 3; d++)
-              drift[d] += delta[d];
+            const T sc = vsq < Eps<T>::v ? tau : ((T(-1) + sqrt(T(1) + T(2) * tau * vsq)) / vsq);
+            drift      = gs * sc + delta;
           }
-          else
-            for (int d = 0; d < 3; d++)
-              drift[d] = delta[d];
-          for (int d = 0; d < 3; d++)
+          const T d2  = delta * delta;
+          const T dsq = __shfl_sync(0xffffffffu, d2, 0) + __shfl_sync(0xffffffffu, d2, 1) +
+              __shfl_sync(0xffffffffu, d2, 2);
+          if (lane < 3)
           {
-            sh.disp[d] = drift[d];
-            sh.pos[d]  = r_now[d] + static_cast<double>(drift[d]);
-            sh.posT[d] = static_cast<T>(sh.pos[d]);
+            const double pos = r_me + static_cast<double>(drift);
+            sh.disp[d]       = drift;
+            sh.pos[d]        = pos;
+            sh.posT[d]       = static_cast<T>(pos);
+            // fractional coordinate (spline_frac) of this component
+            const double Gd = d == 0 ? s.G[0] : (d == 1 ? s.G[1] : s.G[2]);
+            T u             = static_cast<T>(pos * Gd);
+            if (-Eps<T>::v < u && u < T(0))
+              u = T(0);
+            else
+              u -= floor(u);
+            sh.ru[d] = u;
+            if (s.trace)
+              s.trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_GRAD_NOW + d] = static_cast<double>(gs);
           }
-          spline_frac(s, sh.pos, sh.ru);
-          sh.loggf = s.use_drift
-              ? -(T(0.5) / tau) * (delta[0] * delta[0] + delta[1] * delta[1] + delta[2] * delta[2])
-              : T(0);
+          if (lane == 0)
+          {
+            if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
+              atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
+            if (s.trace)
+              s.trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_SELF] = static_cast<double>(g[3]);
+            sh.loggf = s.use_drift ? -(T(0.5) / tau) * dsq : T(0);
+          }
         }
         __syncthreads();
         }
       }
       // ------------------------------------------------ evaluation at the proposed position
-      // the FP64 position and its fractional coordinates were converted once, by thread 0
+      // the FP64 position and its fractional coordinates were converted once, by thread 0;
+      // spline warps: orbital pairs; the other warps: Jastrow rows
       T acc[14];
 #pragma unroll
       for (int q = 0; q < 14; q++)
         acc[q] = T(0);
       const T x0 = sh.posT[0], y0 = sh.posT[1], z0 = sh.posT[2];
-      // Jastrow rows against the positions in shared memory, threads t0, t0 + stride, ...
-      auto jastrow_rows = [&](int t0, int stride) {
+      if (spline_thread)
+      {
+        int ix, iy, iz;
+        T tx, ty, tz;
+        spline_bound(sh.ru[0] * T(s.gx), s.gx - 1, ix, tx);
+        spline_bound(sh.ru[1] * T(s.gy), s.gy - 1, iy, ty);
+        spline_bound(sh.ru[2] * T(s.gz), s.gz - 1, iz, tz);
+        T a[4], da[4], d2a[4], b[4], db[4], d2b[4], c[4], dcw[4], d2c[4];
+        bspline_weights(tx, a, da, d2a);
+        bspline_weights(ty, b, db, d2b);
+        bspline_weights(tz, c, dcw, d2c);
+        const T* origin = s.coefs + ix * s.xs + iy * s.ys + iz * s.zs;
+        for (int p = threadIdx.x; p < pairs; p += spw * 32)
+        {
+          T vgl[5][2];
+          spline_pair_vgl(s, origin, 2 * p, a, da, d2a, b, db, d2b, c, dcw, d2c, vgl);
+#pragma unroll
+          for (int w2 = 0; w2 < 2; w2++)
+          {
+            const int o = 2 * p + w2;
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+              phi[q * lda + o] = vgl[q][w2];
+            if (o < n)
+            {
+              const T x = inv[o];
+              acc[0] += x * vgl[0][w2];
+              acc[1] += x * vgl[1][w2];
+              acc[2] += x * vgl[2][w2];
+              acc[3] += x * vgl[3][w2];
+            }
+          }
+        }
+      }
+      else
+      {
+        const int t0 = threadIdx.x - spw * 32, stride = NT - spw * 32;
         if (s.has_j2)
           for (int j = t0; j < s.ne; j += stride)
           {
             if (j == iat)
               continue;
-            const T dx = min_image(Rs[j] - x0, L0, Li0);
-            const T dy = min_image(Rs[s.ne_pad + j] - y0, L1, Li1);
-            const T dz = min_image(Rs[2 * s.ne_pad + j] - z0, L2, Li2);
-            const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+            const T dx   = min_image(Rs[j] - x0, L0, Li0);
+            const T dy   = min_image(Rs[s.ne_pad + j] - y0, L1, Li1);
+            const T dz   = min_image(Rs[2 * s.ne_pad + j] - z0, L2, Li2);
+            const T r2   = dx * dx + dy * dy + dz * dz;
+            const T rinv = inv_sqrt(r2);
+            const T r    = r2 * rinv;
             if (r < s.j2_rcut)
             {
               const int same = (j < s.nup) == (iat < s.nup);
               T du, d2u;
-              const T u = functor_eval(s.j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
-              du *= T(1) / r;
+              const T u = functor_eval(j2c + (same ? 0 : s.j2_ncoef), s.j2_dri, s.j2_maxidx, r, du, d2u);
+              du *= rinv;
               acc[5] += u;
               acc[6] += du * dx;
               acc[7] += du * dy;
@@ -429,16 +669,18 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         if (s.has_j1)
           for (int j = t0; j < s.nions; j += stride)
           {
-            const T dx = min_image(s.ions[j] - x0, L0, Li0);
-            const T dy = min_image(s.ions[s.nions_pad + j] - y0, L1, Li1);
-            const T dz = min_image(s.ions[2 * s.nions_pad + j] - z0, L2, Li2);
-            const T r  = sqrt(dx * dx + dy * dy + dz * dz);
+            const T dx   = min_image(s.ions[j] - x0, L0, Li0);
+            const T dy   = min_image(s.ions[s.nions_pad + j] - y0, L1, Li1);
+            const T dz   = min_image(s.ions[2 * s.nions_pad + j] - z0, L2, Li2);
+            const T r2   = dx * dx + dy * dy + dz * dz;
+            const T rinv = inv_sqrt(r2);
+            const T r    = r2 * rinv;
             if (r < s.j1_rcut)
             {
               T du, d2u;
               const T u =
-                  functor_eval(s.j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
-              du *= T(1) / r;
+                  functor_eval(j1c + (size_t)s.ion_species[j] * s.j1_ncoef, s.j1_dri, s.j1_maxidx, r, du, d2u);
+              du *= rinv;
               acc[10] += u;
               acc[11] += du * dx;
               acc[12] += du * dy;
@@ -446,24 +688,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
               acc[4] += d2u + T(2) * du;
             }
           }
-      };
-      spline_partials_frac(s, sh.ru, part);
-      jastrow_rows(threadIdx.x, NT);
-      __syncthreads();
-      for (int o = threadIdx.x; o < n; o += NT)
-      {
-        T vgl[5];
-        spline_combine(s, part, o, vgl);
-#pragma unroll
-        for (int q = 0; q < 5; q++)
-          phi[q * lda + o] = vgl[q];
-        const T x = inv[o];
-        acc[0] += x * vgl[0];
-        acc[1] += x * vgl[1];
-        acc[2] += x * vgl[2];
-        acc[3] += x * vgl[3];
       }
-      block_sum_to0<T, 14>(acc, red);
+      block_sum_to0<T, 14>(acc, red, NW);
       if (threadIdx.x == 0)
       {
         const T detr = acc[0];
@@ -471,7 +697,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         T logj       = T(0);
         if (s.has_j1)
         {
-          logj += j1_now[0] - acc[10];
+          logj += j1v_now - acc[10];
           g[0] += acc[11];
           g[1] += acc[12];
           g[2] += acc[13];
@@ -616,7 +842,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           const T sigma = T(1) / sh.det;
           // phi . Ainv[row_x] for every electron x of the segment: x < dc are the V_x . phi
           // of the Binv update (V_x is Ainv[row_x]), x > dc the U . invRow terms of later slots
-          rows_dot<T, NT>(s.Ainv + (slot * n + (i0 - first)) * lda, lda, m, phi, n, pv, T(1));
+          rows_dot<T, NT>(segrows, lda, m, phi, n, pv, T(1));
           __syncthreads();
           for (int x = dc + 1 + threadIdx.x; x < m; x += NT)
             tri[x * (x - 1) / 2 + dc] = pv[x];
@@ -666,7 +892,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       {
         // rank-1 Sherman-Morrison on the whole inverse (arow holds the old row)
         T* Aw  = s.Ainv + slot * n * lda;
-        T* tmp = part;
+        T* tmp = seg;
         for (int j = wid; j < n; j += NT / 32)
         {
           T a = 0;
@@ -683,14 +909,13 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           const int j = e / n, i = e % n;
           Aw[(size_t)j * lda + i] += c * arow[i] * tmp[j];
         }
-        // the prefetched rows of the next electron predate this update: fetch them again
         __syncthreads();
-        if (iat + 1 < i1)
-        {
-          async_wait_all();
-          __syncthreads();
-          prefetch_rows(s, slot, row + 1, pre + ((iat + 1 - i0) & 1) * 5 * lda, threadIdx.x, NT);
-        }
+      }
+      if (K == 1 && iat + 1 < i1)
+      {
+        // rank-1 updates change the whole inverse: the next electron's rows are read after it
+        __syncthreads();
+        prefetch_rows(s, slot, row + 1, pnext, true, threadIdx.x, NT);
       }
       if (accd)
       {
@@ -708,29 +933,31 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         if (s.has_j2)
         {
           const T xo = Rs[iat], yo = Rs[s.ne_pad + iat], zo = Rs[2 * s.ne_pad + iat];
+#pragma unroll 2
           for (int j = threadIdx.x; j < s.ne; j += NT)
           {
             if (j == iat)
               continue;
             const int same = (j < s.nup) == (iat < s.nup);
-            const T* fc    = s.j2c + (same ? 0 : s.j2_ncoef);
+            const T* fc    = j2c + (same ? 0 : s.j2_ncoef);
             const T xj = Rs[j], yj = Rs[s.ne_pad + j], zj = Rs[2 * s.ne_pad + j];
             const T odx = min_image(xj - xo, L0, Li0), ody = min_image(yj - yo, L1, Li1),
                     odz = min_image(zj - zo, L2, Li2);
             const T ndx = min_image(xj - x0, L0, Li0), ndy = min_image(yj - y0, L1, Li1),
                     ndz = min_image(zj - z0, L2, Li2);
-            const T ro = sqrt(odx * odx + ody * ody + odz * odz);
-            const T rn = sqrt(ndx * ndx + ndy * ndy + ndz * ndz);
+            const T ro2 = odx * odx + ody * ody + odz * odz, rn2 = ndx * ndx + ndy * ndy + ndz * ndz;
+            const T roinv = inv_sqrt(ro2), rninv = inv_sqrt(rn2);
+            const T ro = ro2 * roinv, rn = rn2 * rninv;
             T u = 0, du = 0, d2u = 0, cu = 0, cdu = 0, cd2u = 0;
             if (ro < s.j2_rcut)
             {
               u = functor_eval(fc, s.j2_dri, s.j2_maxidx, ro, du, d2u);
-              du *= T(1) / ro;
+              du *= roinv;
             }
             if (rn < s.j2_rcut)
             {
               cu = functor_eval(fc, s.j2_dri, s.j2_maxidx, rn, cdu, cd2u);
-              cdu *= T(1) / rn;
+              cdu *= rninv;
             }
             J2s[j] += cu - u;
             J2s[1 * s.ne_pad + j] -= ndx * cdu - odx * du;
@@ -791,6 +1018,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ SweepShared<T, LEARNED> sh;
+  sweep_shared_init(sh);
   unsigned long long n_acc = 0, n_rej = 0;
   for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
     sweep_walker<T, NT, LEARNED>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
@@ -816,6 +1044,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_multi_kernel(const DevState<T>
   __shared__ SweepShared<T, false> sh;
   __shared__ __align__(16) DevState<T> ds;
   __shared__ int s_item;
+  sweep_shared_init(sh);
   unsigned long long n_acc = 0, n_rej = 0;
   int cur = -1;
   const int total = st.begin[st.nactive];
@@ -934,9 +1163,10 @@ cudaError_t setup_sweep_kernel()
 }
 
 template<typename T>
-size_t sweep_smem_bytes(const DevState<T>& s)
+size_t sweep_smem_bytes(const DevState<T>& s, bool learned)
 {
-  return sizeof(T) * sweep_smem_elems(s);
+  return sizeof(T) * (size_t)sweep_layout<T>(s.lda, s.ne_pad, s.k, s.k > 1 && s.seg_smem, learned, sweep_ncoef(s))
+                         .total;
 }
 
 // electrons [i0, i1) of every walker, inside one spin group; with delayed updates
@@ -953,12 +1183,12 @@ cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1,
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
     if (!s.mlp_simt || !s.mlp_params)
       return cudaErrorInvalidValue;
-    sweep_kernel<T, NT, MINB, true><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+    sweep_kernel<T, NT, MINB, true><<<grid, NT, sweep_smem_bytes(s, true), st>>>(s, i0, i1);
     return cudaGetLastError();
   }
   return with_threads<T>(nt, [&](auto c) {
     constexpr int NT = decltype(c)::value;
-    sweep_kernel<T, NT, SweepMinb<T, NT>::v, false><<<grid, NT, sweep_smem_bytes(s), st>>>(s, i0, i1);
+    sweep_kernel<T, NT, SweepMinb<T, NT>::v, false><<<grid, NT, sweep_smem_bytes(s, false), st>>>(s, i0, i1);
     return cudaGetLastError();
   });
 }
@@ -977,13 +1207,13 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
   {
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, true>, NT,
-                                                      sweep_smem_bytes(s));
+                                                      sweep_smem_bytes(s, true));
   }
   else
     e = with_threads<T>(nt, [&](auto c) {
       constexpr int NT = decltype(c)::value;
       return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, SweepMinb<T, NT>::v, false>,
-                                                           NT, sweep_smem_bytes(s));
+                                                           NT, sweep_smem_bytes(s, false));
     });
   if (e != cudaSuccess)
     return e;
@@ -997,7 +1227,7 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
 template<typename T>
 int sweep_default_threads(const DevState<T>& s)
 {
-  const size_t sm = sweep_smem_bytes(s);
+  const size_t sm = sweep_smem_reference<T>(s.lda, s.ne_pad, s.k);
   if (sm > 114 * 1024)
     return sizeof(T) == 4 ? 512 : 256;
   if (sm > 76 * 1024)
@@ -1007,8 +1237,10 @@ int sweep_default_threads(const DevState<T>& s)
 
 template cudaError_t setup_sweep_kernel<float>();
 template cudaError_t setup_sweep_kernel<double>();
-template size_t sweep_smem_bytes<float>(const DevState<float>&);
-template size_t sweep_smem_bytes<double>(const DevState<double>&);
+template size_t sweep_smem_bytes<float>(const DevState<float>&, bool);
+template size_t sweep_smem_bytes<double>(const DevState<double>&, bool);
+template bool sweep_seg_smem<float>(const DevState<float>&);
+template bool sweep_seg_smem<double>(const DevState<double>&);
 template cudaError_t launch_sweep_segment<float>(const DevState<float>&, int, int, int, cudaStream_t, bool, int);
 template cudaError_t launch_sweep_segment<double>(const DevState<double>&, int, int, int, cudaStream_t, bool, int);
 template cudaError_t sweep_grid<float>(const DevState<float>&, int*, bool, int);

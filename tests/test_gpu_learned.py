@@ -153,6 +153,9 @@ def test_learned_sampling_is_unbiased():
 
 
 def test_training_lowers_the_objective():
+    """Paired comparison: the training objective of the untrained and the trained network,
+    each measured from the same configurations with the same counter-based random numbers
+    (a fresh crowd per measurement, so the stream restarts at sweep 0)."""
     Crowd, DeviceSystem = _gpu()
     s = _small(prec=8, n=8, nw=128, delay=4, seed=25)
     ds = DeviceSystem(s)
@@ -160,11 +163,24 @@ def test_training_lowers_the_objective():
     g.load_walkers(make_walkers(s, 128, seed=26))
     g.mw_evaluateLog()
     g.proposal_init(seed=1)
-    g.vmc_sweeps(10, 0.3, 1, rng_mode=1)
-    # lr = 0: the statistics of the untrained (drift-diffusion) proposal
-    _, _, _, (esjd0, acc0, obj0) = g.vmc_sweeps_learned(12, 0.3, 2, train=True, lr=0.0)
+    g.vmc_sweeps(30, 0.3, 1, rng_mode=1)
+    R0 = g.positions()
+    p_untrained = g.proposal_params()
     g.vmc_sweeps_learned(60, 0.3, 3, train=True, lr=2e-3)
-    _, _, _, (esjd1, acc1, obj1) = g.vmc_sweeps_learned(12, 0.3, 4, train=True, lr=0.0)
+    p_trained = g.proposal_params()
+
+    def measure(params):
+        m = Crowd(ds, 128, 4)
+        m.load_walkers(R0)
+        m.mw_evaluateLog()
+        m.proposal_init(seed=1)
+        m.set_proposal_params(params)
+        # lr = 0: the statistics of the moves without changing the parameters
+        _, _, _, stats = m.vmc_sweeps_learned(12, 0.3, 4, train=True, lr=0.0)
+        return stats
+
+    esjd0, acc0, obj0 = measure(p_untrained)
+    esjd1, acc1, obj1 = measure(p_trained)
     print("training objective per move: before", obj0, "after", obj1, "; expected squared jump", esjd0, "->",
           esjd1, "; acceptance", acc0, "->", acc1)
     assert np.isfinite(obj1) and obj1 < obj0
