@@ -80,6 +80,24 @@ def launches_per_sweep(system, k: int) -> int:
     return 1 + 5
 
 
+def flush_kernel_name(n: int, k: int, flush: int) -> str:
+    """The flush kernel the library takes for n orbitals and delay rank k (flush_tc_variant:
+    one pass while the whole product fits one MMA and 200 KB of shared memory, else column
+    tiles)."""
+    if flush == 0:
+        return "flush_fused_kernel (SIMT)"
+    terms = "TF32" if flush == 1 else "3xTF32"
+    k1, npad = (k + 31) // 32 * 32, (n + 15) // 16 * 16
+    al = lambda x: (x + 1023) & ~1023
+    first = 2 * al(128 * 64 * 4) + 2 * al(k1 * 64 * 4)
+    later = 2 * al(128 * k1 * 4) + 2 * al(npad * k1 * 4)
+    o = max(first, later)
+    tail = max(al(o + k * n * 4), al(al(o + k1 * k1 * 4) + k1 * k1 * 4))
+    one_pass = k <= 32 and npad <= 256 and al(al(tail + k * 4) + 32) <= 200 * 1024
+    name = "flush_tc_kernel" if one_pass else "flush_tc_tiled_kernel"
+    return f"{name} (tcgen05 {terms})"
+
+
 def read_traffic(workload: str):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", f"sweep_kernel_{workload}.md")
@@ -232,7 +250,10 @@ def virtual_moves(crowd, system, peak: float, rcut: float = 2.0, seed: int = 5):
     return {"moves": int(n), "per_walker": n / crowd.nw, "cutoff_bohr": rcut, "rule": "12-point icosahedral",
             "kernel": "vp_ratio_kernel", "ms_per_launch": ms, "moves_per_s": n / (ms / 1e3),
             "e2e_moves_per_s": n / e2e_s, "algorithmic_bytes_per_move": per,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak}}
+            "gathered_gbs": achieved,
+            "bound": "L2: the points of one quadrature sphere and the spheres of nearby electrons share grid "
+                     "cells, so most coefficient rows are L2 hits and the gathered bytes per second exceed the "
+                     "HBM copy bandwidth; no HBM fraction is claimed"}
 
 
 def dmc_rate(dsys, system, R, flush: int, steps: int = 20, warmup: int = 10, tau: float = 0.02):
@@ -571,6 +592,9 @@ def run_ours(args, rank: int, world: int):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     spec = SPECS[args.workload]
+    if args.walkers:
+        import dataclasses
+        spec = dataclasses.replace(spec, walkers=args.walkers)
     system = make_system(spec)
     nw, k = spec.walkers, spec.delay
     dsys = DeviceSystem(system)
@@ -685,8 +709,7 @@ def run_ours(args, rank: int, world: int):
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                      else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": seg_ms,
                      "algorithmic_bytes_per_launch": algo, "launches_per_sweep": seg_per_sweep,
-                     "flush": {"kernel": {0: "flush_fused_kernel (SIMT)", 1: "flush_tc_kernel (tcgen05 TF32)",
-                                          3: "flush_tc_kernel (tcgen05 3xTF32)"}[args.flush],
+                     "flush": {"kernel": flush_kernel_name(system.spec.n_up, k, args.flush),
                                "ms_per_launch": flush_ms,
                                "launches_per_sweep": flush_per_sweep, "algorithmic_bytes_per_launch": flush_bytes,
                                "achieved_gbs": flush_bytes / (flush_ms / 1e3) / 1e9 if flush_ms else None}},
@@ -720,6 +743,8 @@ def main():
                     help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
     ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
     ap.add_argument("--no-extras", action="store_true", help="skip the virtual-move and DMC measurements")
+    ap.add_argument("--walkers", type=int, default=0, help="walkers of the crowd (0: the workload's own count; "
+                                                           "smaller counts size profiler captures)")
     ap.add_argument("--eff-sweeps", type=int, default=500, help="measured sweeps per method in the comparison")
     ap.add_argument("--eff-block", type=int, default=250, help="sweeps per equilibration block")
     ap.add_argument("--eff-min-blocks", type=int, default=8, help="fewest equilibration blocks")
