@@ -637,8 +637,11 @@ def run_ours(args, rank: int, world: int):
     value = moves / (ms / 1e3)
 
     # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
+    # (the caller's buffers are pinned and reused every step, as a driver's walker buffers are)
     Rh = torch.from_numpy(crowd.positions()).pin_memory()
     Rnp = Rh.numpy()
+    log_out = tuple(torch.from_numpy(a).pin_memory().numpy()
+                    for a in (np.zeros(nw), np.zeros(nw, np.int32), np.zeros((nw, 4))))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -646,8 +649,8 @@ def run_ours(args, rank: int, world: int):
     for _ in range(args.steps):
         crowd.load_walkers(Rnp)
         crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=0, flush=args.flush)
-        Rnp[...] = crowd.positions()
-        lp, _, _ = crowd.get_log()
+        crowd.positions(out=Rnp)
+        lp, _, _ = crowd.get_log(out=log_out)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0 + n_rec * rec_ms / 1e3
     _, e2e_s = aggregate_timing(0.0, e2e_s)

@@ -99,8 +99,11 @@ class Crowd:
         assert R.shape == (self.nw, self.ne, 3)
         check(self.L.qmcg_load_walkers(self.handle, _p(R)))
 
-    def positions(self):
-        R = np.zeros((self.nw, self.ne, 3))
+    def positions(self, out: Optional[np.ndarray] = None):
+        """Positions [nw][ne][3] (float64), written into `out` when given (a C-contiguous
+        float64 array of that shape, e.g. in pinned memory) instead of a new array."""
+        R = np.empty((self.nw, self.ne, 3)) if out is None else out
+        assert R.shape == (self.nw, self.ne, 3) and R.dtype == np.float64 and R.flags.c_contiguous
         check(self.L.qmcg_get_positions(self.handle, _p(R)))
         return R
 
@@ -144,10 +147,12 @@ class Crowd:
         check(self.L.qmcg_mw_complete_updates(self.handle))
 
     # ---- state readback
-    def get_log(self):
-        lp = np.zeros(self.nw)
-        sg = np.zeros(self.nw, np.int32)
-        parts = np.zeros((self.nw, 4))
+    def get_log(self, out: Optional[tuple] = None):
+        """(log|psi| [nw], sign [nw], parts [nw][4]); `out` may supply the three arrays."""
+        if out is None:
+            lp, sg, parts = np.zeros(self.nw), np.zeros(self.nw, np.int32), np.zeros((self.nw, 4))
+        else:
+            lp, sg, parts = out
         check(self.L.qmcg_get_log(self.handle, _p(lp), _p(sg, _ip), _p(parts)))
         return lp, sg, parts
 

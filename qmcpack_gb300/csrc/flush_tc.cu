@@ -466,13 +466,15 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 // with each V^T tile staged from global V, so neither N nor k is bounded by TMEM or
 // by a full V in shared memory.  TMEM: T1 and then X in columns [0, KM), the
 // product tile in [KM, KM + TN).
-// Two instances: delay ranks up to 64 with 128-column tiles (256 TMEM columns, one CTA
-// per SM by shared memory), and delay ranks up to 32 with 96-column tiles (128 TMEM
-// columns and 70 KB of shared memory: three CTAs per SM).
+// Two instances: delay ranks up to 64 with 64-column tiles (128 TMEM columns and 97 KB
+// of shared memory: two CTAs per SM), and delay ranks up to 32 with 96-column tiles
+// (128 TMEM columns and 70 KB: three CTAs per SM).  The loads of the next K chunk and of
+// the next V^T tile are issued before the current chunk's MMAs and tile's epilogue, so
+// their latency overlaps the work in flight.
 // ---------------------------------------------------------------------------
 constexpr int TT_KC = 32;  // K chunk of the first product
 // epilogue chunk (columns) of a product tile of TN columns
-__host__ __device__ constexpr int TT_EW(int TN) { return TN % 64 == 0 ? 64 : 32; }
+__host__ __device__ constexpr int TT_EW(int TN) { return TN % 64 == 0 && TN > 64 ? 64 : 32; }
 constexpr int TT_KMAX = 64;
 
 struct TtPlan
@@ -480,7 +482,7 @@ struct TtPlan
   int k1;                            // delay rank padded to 16
   uint32_t a_hi, a_lo, u_hi, u_lo;   // first product: 128 x KC and k1 x KC
   uint32_t a2_hi, a2_lo, w_hi, w_lo; // later products: 128 x k1 (T1 - E, then X) and TN x k1 (V^T tile)
-  uint32_t bt_hi, bt_lo;             // Binv^T: k1 x k1
+  uint32_t bt_hi, bt_lo;             // Binv^T: k1 x k1, over the V^T tile (read before the first tile)
   uint32_t dl, bar, total;
 };
 
@@ -499,9 +501,12 @@ __host__ __device__ inline TtPlan tt_plan(int k, int TN)
   p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.w_hi  = o2; o2 = al(o2 + TN * p.k1 * 4);
   p.w_lo  = o2; o2 = al(o2 + TN * p.k1 * 4);
-  p.bt_hi = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
-  p.bt_lo = o2; o2 = al(o2 + p.k1 * p.k1 * 4);
-  // the epilogue's staging of the product tile overlays the V^T tile and Binv^T
+  // the X product (Binv^T) completes before the first V^T tile is staged
+  p.bt_hi = p.w_hi;
+  p.bt_lo = al(p.bt_hi + p.k1 * p.k1 * 4);
+  const uint32_t btend = al(p.bt_lo + p.k1 * p.k1 * 4);
+  o2 = o2 > btend ? o2 : btend;
+  // the epilogue's staging of the product tile overlays the V^T tile
   const uint32_t eend = al(p.w_hi + TC_M * (TT_EW(TN) + 4) * 4);
   o2 = o2 > eend ? o2 : eend;
   o = o > o2 ? o : o2;
@@ -569,25 +574,42 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
 #pragma unroll
   for (int q = 0; q < KM; q++)
     t1[q] = 0.f;
-  constexpr int AV = TC_M * (TT_KC / 4) / TC_NT; // 8 float4 per thread
+  constexpr int AV = TC_M * (TT_KC / 4) / TC_NT;  // 8 float4 per thread
+  constexpr int UV = KM * (TT_KC / 4) / TC_NT;    // float4 of the U chunk per thread (k1 <= KM)
   const int ub = k1 * (TT_KC / 4);
-  for (int k0 = 0; k0 < n && ok; k0 += TT_KC)
-  {
+  float4 ra[AV], ru[UV];
+  auto load_chunk = [&](int k0) {
 #pragma unroll
     for (int q = 0; q < AV; q++)
     {
       const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e);
       const int gr = r0 + r, gc = k0 + c4;
-      const float4 x = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
-                                          : make_float4(0.f, 0.f, 0.f, 0.f);
-      split_store(x, P.a_hi, P.a_lo, cm_off(r, c4, TT_KC));
+      ra[q] = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int e = tid; e < ub; e += TC_NT)
+#pragma unroll
+    for (int q = 0; q < UV; q++)
     {
-      const int r = slot_row(e), c4 = slot_col(e), gc = k0 + c4;
-      const float4 x = (r < dc && gc < n) ? *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc)
-                                          : make_float4(0.f, 0.f, 0.f, 0.f);
-      split_store(x, P.u_hi, P.u_lo, cm_off(r, c4, TT_KC));
+      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e), gc = k0 + c4;
+      ru[q] = (e < ub && r < dc && gc < n) ? *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc)
+                                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  };
+  load_chunk(0);
+  for (int k0 = 0; k0 < n && ok; k0 += TT_KC)
+  {
+#pragma unroll
+    for (int q = 0; q < AV; q++)
+    {
+      const int e = tid + q * TC_NT;
+      split_store(ra[q], P.a_hi, P.a_lo, cm_off(slot_row(e), slot_col(e), TT_KC));
+    }
+#pragma unroll
+    for (int q = 0; q < UV; q++)
+    {
+      const int e = tid + q * TC_NT;
+      if (e < ub)
+        split_store(ru[q], P.u_hi, P.u_lo, cm_off(slot_row(e), slot_col(e), TT_KC));
     }
     fence_async_smem();
     tc_fence_before();
@@ -611,6 +633,9 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
       }
       mma_commit(bar);
     }
+    // the next chunk's loads are in flight while this chunk's products run
+    if (k0 + TT_KC < n)
+      load_chunk(k0 + TT_KC);
     ok = wait_mma();
     if (TERMS > 1 && ok)
     {
@@ -689,18 +714,31 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
           split_store(make_float4(t[q], t[q + 1], t[q + 2], t[q + 3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
     }
   }
-  // ---------------- column tiles: P_tile = X V[:, tile], Ainv -= P
-  for (int t0 = 0; t0 < n && ok; t0 += TN)
-  {
-    // V^T tile: element (i, l) = V[l][t0 + i], consecutive threads on consecutive columns
-    for (int e = tid; e < TN * (k1 / 4); e += TC_NT)
+  // ---------------- column tiles: P_tile = X V[:, tile], Ainv -= P.  V^T tile: element
+  // (i, l) = V[l][t0 + i], consecutive threads on consecutive columns; the next tile's
+  // values are read while this tile's epilogue runs
+  constexpr int VV = TN * (KM / 4) / TC_NT; // slots of a V^T tile per thread (k1 <= KM)
+  float vq[VV][4];
+  auto load_vt = [&](int t0) {
+#pragma unroll
+    for (int h = 0; h < VV; h++)
     {
-      const int i = e % TN, l4 = (e / TN) * 4, col = t0 + i;
-      float x[4];
+      const int e = tid + h * TC_NT, i = e % TN, l4 = (e / TN) * 4, col = t0 + i;
 #pragma unroll
       for (int q = 0; q < 4; q++)
-        x[q] = (l4 + q < dc && col < n) ? V[(size_t)(l4 + q) * lda + col] : 0.f;
-      split_store(make_float4(x[0], x[1], x[2], x[3]), P.w_hi, P.w_lo, cm_off(i, l4, k1));
+        vq[h][q] = (l4 + q < dc && l4 + q < k1 && col < n) ? V[(size_t)(l4 + q) * lda + col] : 0.f;
+    }
+  };
+  if (ok)
+    load_vt(0);
+  for (int t0 = 0; t0 < n && ok; t0 += TN)
+  {
+#pragma unroll
+    for (int h = 0; h < VV; h++)
+    {
+      const int e = tid + h * TC_NT, i = e % TN, l4 = (e / TN) * 4;
+      if (l4 < k1)
+        split_store(make_float4(vq[h][0], vq[h][1], vq[h][2], vq[h][3]), P.w_hi, P.w_lo, cm_off(i, l4, k1));
     }
     fence_async_smem();
     tc_fence_before();
@@ -711,6 +749,8 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
       mma_k1<TERMS>(d2, sm, P.a2_hi, P.a2_lo, P.w_hi, P.w_lo, k1, idesc_tf32(TC_M, TN));
       mma_commit(bar);
     }
+    if (t0 + TN < n)
+      load_vt(t0 + TN);
     ok = wait_mma();
     if (!ok)
       break;
@@ -738,10 +778,10 @@ static bool flush_tc_compact_ok(int n, int k)
 bool flush_tc_supported(int n, int k, int lda)
 {
   // 16-byte aligned rows; delay rank up to 64 (the tiled kernels cover any N)
-  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k, 128).total <= 200 * 1024;
+  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k, 64).total <= 200 * 1024;
 }
 
-#define QMCG_TILED_BIG(TERMS) flush_tc_tiled_kernel<TERMS, 128, 64, 1>
+#define QMCG_TILED_BIG(TERMS) flush_tc_tiled_kernel<TERMS, 64, 64, 2>
 #define QMCG_TILED_SMALL(TERMS) flush_tc_tiled_kernel<TERMS, 96, 32, 3>
 
 cudaError_t setup_flush_tc()
@@ -796,7 +836,7 @@ cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cuda
   {
     if (f.k > TT_KMAX)
       return cudaErrorInvalidValue;
-    const TtPlan p = tt_plan(f.k, 128);
+    const TtPlan p = tt_plan(f.k, 64);
     if (terms == 1)
       QMCG_TILED_BIG(1)<<<grid, TC_NT, p.total, st>>>(f, err);
     else
