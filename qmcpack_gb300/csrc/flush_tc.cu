@@ -462,31 +462,41 @@ __global__ void __launch_bounds__(TC_NT, 2) flush_tc_kernel(FlushArgs<float> f, 
 
 // ---------------------------------------------------------------------------
 // N-tiled variant for large determinants and delay ranks up to 64: X = (T1 - E) Binv
-// is formed once, the last product runs over column tiles of TN inverse columns
-// with each V^T tile staged from global V, so neither N nor k is bounded by TMEM or
-// by a full V in shared memory.  TMEM: T1 and then X in columns [0, KM), the
-// product tile in [KM, KM + TN).
-// Two instances: delay ranks up to 64 with 64-column tiles (128 TMEM columns and 97 KB
-// of shared memory: two CTAs per SM), and delay ranks up to 32 with 96-column tiles
-// (128 TMEM columns and 70 KB: three CTAs per SM).  The loads of the next K chunk and of
-// the next V^T tile are issued before the current chunk's MMAs and tile's epilogue, so
-// their latency overlaps the work in flight.
+// is formed once, the last product runs over column tiles of TT_TN inverse columns with
+// each V^T tile staged from global V, so neither N nor k is bounded by TMEM or by a full
+// V in shared memory.
+//   T1  K chunks of 32: the raw Ainv and U chunks arrive by cp.async RAW chunks ahead
+//       (each thread copies and later splits the same 16-byte slots, so its own
+//       wait_group makes them visible to it), are split in shared memory, and their
+//       products alternate between two TMEM buffers; with split precision the previous
+//       chunk's product is summed in FP32 while the next chunk's products run
+//   X   one product over K = k1, Binv^T staged from a cp.async copy of Binv
+//   P   column tiles: while the products of tile t run, its inverse rows and the next
+//       tile's V^T values are read into registers; the product then passes through
+//       shared memory (over the V^T tile) in 32-column rounds so that every global
+//       access of a warp covers whole 128-byte row segments
+// TMEM: buffers of 64 columns at 0 and 64 (128 allocated).  Two instances: delay ranks up
+// to 64 with two raw chunks in flight (97 KB of shared memory: two CTAs per SM), and delay
+// ranks up to 32 with one (61 KB: three CTAs per SM).
 // ---------------------------------------------------------------------------
-constexpr int TT_KC = 32;  // K chunk of the first product
-// epilogue chunk (columns) of a product tile of TN columns
-__host__ __device__ constexpr int TT_EW(int TN) { return TN % 64 == 0 && TN > 64 ? 64 : 32; }
+constexpr int TT_KC   = 32; // K chunk of the first product
+constexpr int TT_TN   = 64; // columns of a product tile
 constexpr int TT_KMAX = 64;
+constexpr int TT_TMC  = 128;
+constexpr int TT_EP   = 36; // row pitch (floats) of the epilogue staging: 32 columns + 4
 
 struct TtPlan
 {
   int k1;                            // delay rank padded to 16
-  uint32_t a_hi, a_lo, u_hi, u_lo;   // first product: 128 x KC and k1 x KC
+  uint32_t a_hi, a_lo, u_hi, u_lo;   // split chunk tiles: 128 x KC and k1 x KC
+  uint32_t raw[2], raw_bytes;        // raw chunk stages: Ainv rows (128 x KC) then U rows (k1 x KC)
   uint32_t a2_hi, a2_lo, w_hi, w_lo; // later products: 128 x k1 (T1 - E, then X) and TN x k1 (V^T tile)
   uint32_t bt_hi, bt_lo;             // Binv^T: k1 x k1, over the V^T tile (read before the first tile)
+  int binv_smem;                     // Binv copied into raw stage 0 (clear of Binv^T and big enough)
   uint32_t dl, bar, total;
 };
 
-__host__ __device__ inline TtPlan tt_plan(int k, int TN)
+__host__ __device__ inline TtPlan tt_plan(int k, int raw_stages)
 {
   TtPlan p;
   p.k1    = ((k + 15) / 16) * 16;
@@ -496,34 +506,47 @@ __host__ __device__ inline TtPlan tt_plan(int k, int TN)
   p.a_lo  = o; o = al(o + TC_M * TT_KC * 4);
   p.u_hi  = o; o = al(o + p.k1 * TT_KC * 4);
   p.u_lo  = o; o = al(o + p.k1 * TT_KC * 4);
+  p.raw_bytes = (uint32_t)(TC_M + p.k1) * TT_KC * 4;
+  p.raw[0] = o;
+  o        = al(o + p.raw_bytes);
+  p.raw[1] = o;
+  if (raw_stages > 1)
+    o = al(o + p.raw_bytes);
   uint32_t o2 = 0;
   p.a2_hi = o2; o2 = al(o2 + TC_M * p.k1 * 4);
   p.a2_lo = o2; o2 = al(o2 + TC_M * p.k1 * 4);
-  p.w_hi  = o2; o2 = al(o2 + TN * p.k1 * 4);
-  p.w_lo  = o2; o2 = al(o2 + TN * p.k1 * 4);
-  // the X product (Binv^T) completes before the first V^T tile is staged
+  p.w_hi  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
+  p.w_lo  = o2; o2 = al(o2 + TT_TN * p.k1 * 4);
   p.bt_hi = p.w_hi;
   p.bt_lo = al(p.bt_hi + p.k1 * p.k1 * 4);
   const uint32_t btend = al(p.bt_lo + p.k1 * p.k1 * 4);
   o2 = o2 > btend ? o2 : btend;
-  // the epilogue's staging of the product tile overlays the V^T tile
-  const uint32_t eend = al(p.w_hi + TC_M * (TT_EW(TN) + 4) * 4);
+  // the epilogue's staging of a product tile (128 rows x 36 floats) over the V^T tile
+  const uint32_t eend = al(p.w_hi + TC_M * TT_EP * 4);
   o2 = o2 > eend ? o2 : eend;
-  o = o > o2 ? o : o2;
+  o  = o > o2 ? o : o2;
+  const uint32_t bbytes = (uint32_t)k * k * 4;
+  p.binv_smem = (k % 2 == 0) && bbytes <= p.raw_bytes && (p.raw[0] + bbytes <= p.bt_hi || p.raw[0] >= btend);
   p.dl    = o; o = al(o + k * 4);
   p.bar   = o; o += 16;
   p.total = al(o);
   return p;
 }
 
-template<int TERMS, int TN, int KM, int MINB>
+// 16-byte cp.async from global to shared, zero-filled when `valid` is false
+__device__ __forceinline__ void cp16(uint32_t saddr, const void* g, bool valid)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0)
+               : "memory");
+}
+
+template<int TERMS, int KM, int RAW, int MINB>
 __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<float> f, int* err)
 {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
-  constexpr int TMC = (KM + TN <= 128) ? 128 : 256; // TMEM columns allocated
-  const TtPlan P = tt_plan(f.k, TN);
+  const TtPlan P = tt_plan(f.k, RAW);
   const int n = f.n, k = f.k, dc = f.dc, lda = f.lda, k1 = P.k1;
   const int iw = blockIdx.x, r0 = blockIdx.y * TC_M;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -540,15 +563,15 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     mbar_init(bar);
   }
   if (warp == 0)
-    tmem_alloc(smem_u32(&s_tmem), TMC);
+    tmem_alloc(smem_u32(&s_tmem), TT_TMC);
   for (int e = tid; e < dc; e += TC_NT)
     dls[e] = dlist[e];
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = s_tmem;
-  const uint32_t d1 = tmem, d2 = tmem + KM;
-  uint32_t phase = 0;
+  const uint32_t lrow = (uint32_t)(warp * 32) << 16; // this warp's TMEM lanes
+  uint32_t phase      = 0;
   auto split_store = [&](float4 x, uint32_t hi_base, uint32_t lo_base, uint32_t off) {
     const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
     *reinterpret_cast<float4*>(sm + hi_base + off) = h;
@@ -568,94 +591,151 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
   auto slot_col = [](int e) { return ((e >> 3) % (TT_KC / 4)) * 4; };
   bool ok = true;
 
-  // ---------------- T1 = Ainv[rows] U^T over K = n in chunks of KC; with split
-  // precision the chunks are summed in FP32 here (round to nearest)
-  float t1[KM];
-#pragma unroll
-  for (int q = 0; q < KM; q++)
-    t1[q] = 0.f;
-  constexpr int AV = TC_M * (TT_KC / 4) / TC_NT;  // 8 float4 per thread
-  constexpr int UV = KM * (TT_KC / 4) / TC_NT;    // float4 of the U chunk per thread (k1 <= KM)
-  const int ub = k1 * (TT_KC / 4);
-  float4 ra[AV], ru[UV];
-  auto load_chunk = [&](int k0) {
+  // ---------------- T1 = Ainv[rows] U^T over K = n in chunks of KC
+  constexpr int AV = TC_M * (TT_KC / 4) / TC_NT; // Ainv slots per thread (8)
+  constexpr int UV = KM * (TT_KC / 4) / TC_NT;   // U slots per thread (k1 <= KM)
+  const int ub     = k1 * (TT_KC / 4);
+  const int nch    = (n + TT_KC - 1) / TT_KC;
+  // raw stage layout: Ainv chunk rows of KC floats, then the U chunk rows
+  auto issue_chunk = [&](int ch, int stage) {
+    const int k0    = ch * TT_KC;
+    const uint32_t base = smem_u32(sm + (stage ? P.raw[1] : P.raw[0]));
 #pragma unroll
     for (int q = 0; q < AV; q++)
     {
-      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e);
-      const int gr = r0 + r, gc = k0 + c4;
-      ra[q] = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int q = 0; q < UV; q++)
-    {
-      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e), gc = k0 + c4;
-      ru[q] = (e < ub && r < dc && gc < n) ? *reinterpret_cast<const float4*>(U + (size_t)r * lda + gc)
-                                           : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-  };
-  load_chunk(0);
-  for (int k0 = 0; k0 < n && ok; k0 += TT_KC)
-  {
-#pragma unroll
-    for (int q = 0; q < AV; q++)
-    {
-      const int e = tid + q * TC_NT;
-      split_store(ra[q], P.a_hi, P.a_lo, cm_off(slot_row(e), slot_col(e), TT_KC));
+      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e), gr = r0 + r, gc = k0 + c4;
+      const bool v = gr < n && gc < n;
+      cp16(base + (uint32_t)(r * TT_KC + c4) * 4, v ? A + (size_t)gr * lda + gc : A, v);
     }
 #pragma unroll
     for (int q = 0; q < UV; q++)
     {
       const int e = tid + q * TC_NT;
       if (e < ub)
-        split_store(ru[q], P.u_hi, P.u_lo, cm_off(slot_row(e), slot_col(e), TT_KC));
+      {
+        const int r = slot_row(e), c4 = slot_col(e), gc = k0 + c4;
+        const bool v = r < dc && gc < n;
+        cp16(base + (uint32_t)((TC_M + r) * TT_KC + c4) * 4, v ? U + (size_t)r * lda + gc : U, v);
+      }
     }
+  };
+  auto split_chunk = [&](int stage) {
+    const unsigned char* raw = sm + (stage ? P.raw[1] : P.raw[0]);
+#pragma unroll
+    for (int q = 0; q < AV; q++)
+    {
+      const int e = tid + q * TC_NT, r = slot_row(e), c4 = slot_col(e);
+      split_store(*reinterpret_cast<const float4*>(raw + (r * TT_KC + c4) * 4), P.a_hi, P.a_lo,
+                  cm_off(r, c4, TT_KC));
+    }
+#pragma unroll
+    for (int q = 0; q < UV; q++)
+    {
+      const int e = tid + q * TC_NT;
+      if (e < ub)
+      {
+        const int r = slot_row(e), c4 = slot_col(e);
+        split_store(*reinterpret_cast<const float4*>(raw + ((TC_M + r) * TT_KC + c4) * 4), P.u_hi, P.u_lo,
+                    cm_off(r, c4, TT_KC));
+      }
+    }
+  };
+  float t1[KM];
+#pragma unroll
+  for (int q = 0; q < KM; q++)
+    t1[q] = 0.f;
+  auto accumulate = [&](uint32_t buf) {
+#pragma unroll
+    for (int c0 = 0; c0 < KM; c0 += 32)
+      if (c0 < k1)
+      {
+        float t[32];
+        tmem_ld32(buf + lrow + c0, t);
+#pragma unroll
+        for (int q = 0; q < 32; q++)
+          t1[c0 + q] += t[q];
+      }
+  };
+#pragma unroll
+  for (int st = 0; st < RAW; st++)
+  {
+    if (st < nch)
+      issue_chunk(st, st);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
+  for (int c = 0; c < nch && ok; c++)
+  {
+    // this thread's copies of chunk c have landed: at most RAW - 1 younger groups pending
+    if (RAW > 1)
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    else
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // every thread waits for chunk c - 1's products itself: the split tiles are then free
+    bool mine = true;
+    if (c > 0)
+    {
+      mine = mbar_wait(bar, phase);
+      phase ^= 1;
+      tc_fence_after();
+    }
+    split_chunk(c % RAW);
+    if (c + RAW < nch)
+      issue_chunk(c + RAW, c % RAW);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     fence_async_smem();
     tc_fence_before();
-    __syncthreads();
+    if (__syncthreads_or(!mine))
+    {
+      ok = false;
+      break;
+    }
+    if (c == nch - 1 && P.binv_smem)
+    {
+      // Binv into raw stage 0, free now: it lands while the last products run
+      const uint32_t base = smem_u32(sm + P.raw[0]);
+      for (int e = tid; e < k * k / 4; e += TC_NT)
+        cp16(base + (uint32_t)e * 16, Bi + 4 * e, true);
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     if (tid == 0)
     {
       tc_fence_after();
       const uint32_t id = idesc_tf32(TC_M, k1);
       const uint32_t ah = smem_u32(sm + P.a_hi), al = smem_u32(sm + P.a_lo);
       const uint32_t bh = smem_u32(sm + P.u_hi), bl = smem_u32(sm + P.u_lo);
+      const uint32_t d  = TERMS > 1 ? tmem + 64 * (c & 1) : tmem;
       for (int ks = 0; ks < TT_KC / 8; ks++)
       {
         const uint32_t adv = ks * 256;
-        const int first    = TERMS > 1 ? (ks == 0) : (k0 == 0 && ks == 0);
-        mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, first ? 0 : 1);
+        const int first    = TERMS > 1 ? (ks == 0) : (c == 0 && ks == 0);
+        mma_tf32(d, smem_desc(ah + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, first ? 0 : 1);
         if (TERMS > 1)
         {
-          mma_tf32(d1, smem_desc(ah + adv, TT_KC), smem_desc(bl + adv, TT_KC), id, 1);
-          mma_tf32(d1, smem_desc(al + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, 1);
+          mma_tf32(d, smem_desc(ah + adv, TT_KC), smem_desc(bl + adv, TT_KC), id, 1);
+          mma_tf32(d, smem_desc(al + adv, TT_KC), smem_desc(bh + adv, TT_KC), id, 1);
         }
       }
       mma_commit(bar);
     }
-    // the next chunk's loads are in flight while this chunk's products run
-    if (k0 + TT_KC < n)
-      load_chunk(k0 + TT_KC);
-    ok = wait_mma();
-    if (TERMS > 1 && ok)
-    {
-#pragma unroll
-      for (int c0 = 0; c0 < KM; c0 += 32)
-        if (c0 < k1)
-        {
-          float t[32];
-          tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
-#pragma unroll
-          for (int q = 0; q < 32; q++)
-            t1[c0 + q] += t[q];
-        }
-    }
+    // with split precision: the previous chunk's product, summed while this one runs
+    if (TERMS > 1 && c > 0)
+      accumulate(tmem + 64 * ((c - 1) & 1));
+    tc_fence_before();
   }
+  if (ok)
+    ok = wait_mma();
+  if (TERMS > 1 && ok)
+    accumulate(tmem + 64 * ((nch - 1) & 1));
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads(); // Binv has landed for every thread's copies
 
-  // ---------------- (T1 - E) into the A operand of X = (T1 - E) Binv
+  // ---------------- Binv^T, then (T1 - E) into the A operand of X = (T1 - E) Binv
   const int r = warp * 32 + lane;
   if (ok)
   {
+    stage_binv_t<TERMS>(sm, P.bt_hi, P.bt_lo, P.binv_smem ? reinterpret_cast<const float*>(sm + P.raw[0]) : Bi, k,
+                        dc, k1, tid);
+    __syncthreads(); // the raw Binv (over the operand tiles) has been read
 #pragma unroll
     for (int c0 = 0; c0 < KM; c0 += 32)
     {
@@ -669,7 +749,7 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
           t[q] = t1[c0 + q];
       }
       else
-        tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+        tmem_ld32(tmem + lrow + c0, t);
 #pragma unroll
       for (int q = 0; q < 32; q += 4)
         if (c0 + q < k1)
@@ -689,14 +769,13 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
           split_store(make_float4(v[0], v[1], v[2], v[3]), P.a2_hi, P.a2_lo, cm_off(r, c0 + q, k1));
         }
     }
-    stage_binv_t<TERMS>(sm, P.bt_hi, P.bt_lo, Bi, k, dc, k1, tid);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     if (tid == 0)
     {
       tc_fence_after();
-      mma_k1<TERMS>(d1, sm, P.a2_hi, P.a2_lo, P.bt_hi, P.bt_lo, k1, idesc_tf32(TC_M, k1));
+      mma_k1<TERMS>(tmem, sm, P.a2_hi, P.a2_lo, P.bt_hi, P.bt_lo, k1, idesc_tf32(TC_M, k1));
       mma_commit(bar);
     }
     ok = wait_mma();
@@ -707,7 +786,7 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     for (int c0 = 0; c0 < k1; c0 += 32)
     {
       float t[32];
-      tmem_ld32(d1 + ((uint32_t)(warp * 32) << 16) + c0, t);
+      tmem_ld32(tmem + lrow + c0, t);
 #pragma unroll
       for (int q = 0; q < 32; q += 4)
         if (c0 + q < k1)
@@ -715,28 +794,47 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     }
   }
   // ---------------- column tiles: P_tile = X V[:, tile], Ainv -= P.  V^T tile: element
-  // (i, l) = V[l][t0 + i], consecutive threads on consecutive columns; the next tile's
-  // values are read while this tile's epilogue runs
-  constexpr int VV = TN * (KM / 4) / TC_NT; // slots of a V^T tile per thread (k1 <= KM)
+  // (i, l) = V[l][t0 + i], consecutive threads on consecutive columns
+  constexpr int VV = TT_TN * (KM / 4) / TC_NT; // slots of a V^T tile per thread (k1 <= KM)
   float vq[VV][4];
   auto load_vt = [&](int t0) {
 #pragma unroll
     for (int h = 0; h < VV; h++)
     {
-      const int e = tid + h * TC_NT, i = e % TN, l4 = (e / TN) * 4, col = t0 + i;
+      const int e = tid + h * TC_NT, i = e % TT_TN, l4 = (e / TT_TN) * 4, col = t0 + i;
 #pragma unroll
       for (int q = 0; q < 4; q++)
         vq[h][q] = (l4 + q < dc && l4 + q < k1 && col < n) ? V[(size_t)(l4 + q) * lda + col] : 0.f;
     }
   };
+  // inverse rows of a tile: round j (32 columns), slot i: row e / 8, float4 e % 8 of the
+  // round's 32 columns (e = tid + 128 i), so a warp reads four whole 128-byte row segments
+  constexpr int ER = TT_TN / 32;
+  float4 ap[ER][8];
+  auto load_rows = [&](int t0) {
+#pragma unroll
+    for (int j = 0; j < ER; j++)
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+      {
+        const int e = tid + i * TC_NT, gr = r0 + (e >> 3), gc = t0 + 32 * j + (e & 7) * 4;
+        ap[j][i] = (gr < n && gc < n) ? *reinterpret_cast<const float4*>(A + (size_t)gr * lda + gc)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+  };
+  const uint32_t d2 = tmem + 64;
+  const int nt      = (n + TT_TN - 1) / TT_TN;
   if (ok)
     load_vt(0);
-  for (int t0 = 0; t0 < n && ok; t0 += TN)
+  for (int t = 0; t < nt && ok; t++)
   {
+    const int t0 = t * TT_TN;
+    // V^T tile: the previous tile's epilogue staging (over it) is done, and for the first
+    // tile the X product (Binv^T over it) has completed
 #pragma unroll
     for (int h = 0; h < VV; h++)
     {
-      const int e = tid + h * TC_NT, i = e % TN, l4 = (e / TN) * 4;
+      const int e = tid + h * TC_NT, i = e % TT_TN, l4 = (e / TT_TN) * 4;
       if (l4 < k1)
         split_store(make_float4(vq[h][0], vq[h][1], vq[h][2], vq[h][3]), P.w_hi, P.w_lo, cm_off(i, l4, k1));
     }
@@ -746,25 +844,49 @@ __global__ void __launch_bounds__(TC_NT, MINB) flush_tc_tiled_kernel(FlushArgs<f
     if (tid == 0)
     {
       tc_fence_after();
-      mma_k1<TERMS>(d2, sm, P.a2_hi, P.a2_lo, P.w_hi, P.w_lo, k1, idesc_tf32(TC_M, TN));
+      mma_k1<TERMS>(d2, sm, P.a2_hi, P.a2_lo, P.w_hi, P.w_lo, k1, idesc_tf32(TC_M, TT_TN));
       mma_commit(bar);
     }
-    if (t0 + TN < n)
-      load_vt(t0 + TN);
+    // while the products run: this tile's inverse rows and the next tile's V^T values
+    load_rows(t0);
+    if (t + 1 < nt)
+      load_vt(t0 + TT_TN);
     ok = wait_mma();
     if (!ok)
       break;
-    // epilogue through shared memory over the V^T tile (its MMA has completed)
-    epilogue_rows<TT_EW(TN)>(A, lda, n, r0, t0, TN, d2, reinterpret_cast<float*>(sm + P.w_hi), tid);
-    tc_fence_before();
-    __syncthreads();
+    float* E = reinterpret_cast<float*>(sm + P.w_hi);
+#pragma unroll
+    for (int j = 0; j < ER; j++)
+    {
+      float p[32];
+      tmem_ld32(d2 + 32 * j + lrow, p);
+#pragma unroll
+      for (int q = 0; q < 32; q += 4)
+        *reinterpret_cast<float4*>(E + r * TT_EP + q) = make_float4(p[q], p[q + 1], p[q + 2], p[q + 3]);
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+      {
+        const int e = tid + i * TC_NT, rr = e >> 3, c4 = (e & 7) * 4, gr = r0 + rr, gc = t0 + 32 * j + c4;
+        if (gr < n && gc < n)
+        {
+          const float4 pv = *reinterpret_cast<const float4*>(E + rr * TT_EP + c4);
+          const float4 a  = ap[j][i];
+          *reinterpret_cast<float4*>(A + (size_t)gr * lda + gc) =
+              make_float4(a.x - pv.x, a.y - pv.y, a.z - pv.z, a.w - pv.w);
+        }
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
   }
   if (!ok && tid == 0)
     atomicExch(err, 1);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   tc_fence_before();
   __syncthreads();
   if (warp == 0)
-    tmem_dealloc(tmem, TMC);
+    tmem_dealloc(tmem, TT_TMC);
 }
 
 // the compact kernel: whole product in TMEM, k <= 32, and the second product is one
@@ -778,11 +900,11 @@ static bool flush_tc_compact_ok(int n, int k)
 bool flush_tc_supported(int n, int k, int lda)
 {
   // 16-byte aligned rows; delay rank up to 64 (the tiled kernels cover any N)
-  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k, 64).total <= 200 * 1024;
+  return k >= 1 && k <= TT_KMAX && (lda % 4) == 0 && (n % 4) == 0 && tt_plan(k, 2).total <= 200 * 1024;
 }
 
-#define QMCG_TILED_BIG(TERMS) flush_tc_tiled_kernel<TERMS, 64, 64, 2>
-#define QMCG_TILED_SMALL(TERMS) flush_tc_tiled_kernel<TERMS, 96, 32, 3>
+#define QMCG_TILED_BIG(TERMS) flush_tc_tiled_kernel<TERMS, 64, 2, 2>
+#define QMCG_TILED_SMALL(TERMS) flush_tc_tiled_kernel<TERMS, 32, 1, 3>
 
 cudaError_t setup_flush_tc()
 {
@@ -800,7 +922,7 @@ cudaError_t setup_flush_tc()
   return e;
 }
 
-// which kernel flushes a shape: 0 one-pass, 1 tiled (k <= 32, 96-column tiles), 2 tiled (k <= 64)
+// which kernel flushes a shape: 0 one-pass, 1 tiled (k <= 32, one raw chunk in flight), 2 tiled (k <= 64)
 int flush_tc_variant(int n, int k)
 {
   if (flush_tc_compact_ok(n, k))
@@ -826,7 +948,7 @@ cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cuda
   }
   else if (v == 1)
   {
-    const TtPlan p = tt_plan(f.k, 96);
+    const TtPlan p = tt_plan(f.k, 1);
     if (terms == 1)
       QMCG_TILED_SMALL(1)<<<grid, TC_NT, p.total, st>>>(f, err);
     else
@@ -836,7 +958,7 @@ cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cuda
   {
     if (f.k > TT_KMAX)
       return cudaErrorInvalidValue;
-    const TtPlan p = tt_plan(f.k, 64);
+    const TtPlan p = tt_plan(f.k, 2);
     if (terms == 1)
       QMCG_TILED_BIG(1)<<<grid, TC_NT, p.total, st>>>(f, err);
     else
