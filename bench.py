@@ -547,7 +547,8 @@ def run_reference(args, rank: int, world: int):
     c.evaluate_log(nthreads=cores)
     rec_s = time.perf_counter() - t0
     rng = orc.Rng(11)
-    c.vmc_sweeps(rng, args.warmup, spec.tau, True)
+    # the same untimed sweeps before the timed ones as the GPU arm (equilibration + warm-up)
+    c.vmc_sweeps(rng, args.equil + args.warmup, spec.tau, True)
     t0 = time.perf_counter()
     na, nr, _ = c.vmc_sweeps(rng, args.steps, spec.tau, True)
     sweep_s = time.perf_counter() - t0
@@ -555,7 +556,7 @@ def run_reference(args, rank: int, world: int):
     total_s = sweep_s + n_rec * rec_s
     moves = args.steps * nw * ne
     value = moves / total_s
-    sample = (f"{args.steps} timed sweeps (after {args.warmup} warm-up) x {nw} walkers x {ne} electrons of "
+    sample = (f"{args.steps} timed sweeps (after {args.equil} + {args.warmup} untimed) x {nw} walkers x {ne} electrons of "
               f"{args.workload}, {'FP32' if spec.precision == 4 else 'FP64'} move loop, mt19937 stream, "
               f"{sweep_s:.1f} s; FP64 recompute of all walkers {rec_s * 1e3:.0f} ms, added {n_rec:g} times")
     base = {"value": value, "unit": "walker-moves/s", "cores": cores, "kind": "port", "sample": sample}
@@ -611,6 +612,15 @@ def run_ours(args, rank: int, world: int):
     if args.equil > 0:
         crowd.vmc_sweeps(args.equil, spec.tau, seed, rng_mode=1, recompute_every=recompute_every, flush=args.flush)
     crowd.vmc_sweeps(args.warmup, spec.tau, seed, rng_mode=1, recompute_every=0, flush=args.flush)
+    # every measurement below starts from this configuration: the chain is still relaxing
+    # (acceptance, and with it the cost of a sweep, keeps falling), so measurements taken one
+    # after the other would see different amounts of work
+    R_start = crowd.positions()
+
+    def restart():
+        crowd.load_walkers(R_start)
+        crowd.mw_evaluateLog()
+
     stream = torch.cuda.ExternalStream(crowd.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(dev)
@@ -638,6 +648,7 @@ def run_ours(args, rank: int, world: int):
 
     # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
     # (the caller's buffers are pinned and reused every step, as a driver's walker buffers are)
+    restart()
     Rh = torch.from_numpy(crowd.positions()).pin_memory()
     Rnp = Rh.numpy()
     log_out = tuple(torch.from_numpy(a).pin_memory().numpy()
@@ -661,6 +672,7 @@ def run_ours(args, rank: int, world: int):
     # dominant kernel: per-launch CUDA-event time of the walker-resident kernel (one
     # launch = one segment of up to k electrons of every walker); the batched flush
     # is timed alongside
+    restart()
     seg_ms, flush_ms, seg_per_sweep, flush_per_sweep = crowd.profile_sweep(3)
     algo = bytes_per_walker_move(system, k, with_flush=False) * nw * system.n_elec // seg_per_sweep
     flush_bytes = flush_bytes_per_launch(system, k, nw)
