@@ -327,8 +327,9 @@ __device__ __forceinline__ void block_sum(T (&v)[NV], T* scratch)
 
 // sum NV <= 16 values over the block; the totals are valid in warp 0 (thread 0 included).
 // Inside a warp a reduce-scatter halves the values a lane keeps at every step (16
-// shuffles for 16 values instead of 5 per value) until lane l holds the warp's total of
-// value l / 2; warp 0 then adds the warps' totals and broadcasts them to its lanes.
+// shuffles for 16 values instead of 5 per value; NV padded to the next power of two P,
+// then plain butterfly sums) until lane l holds the warp's total of value l / (32 / P);
+// warp 0 then adds the warps' totals and broadcasts them to its lanes.
 // scratch: 16 * stride elements, stride >= the number of warps.  No trailing barrier: the
 // caller synchronises before scratch is written again.
 template<typename T, int NV>
@@ -336,25 +337,32 @@ __device__ __forceinline__ void block_sum_to0(T (&v)[NV], T* scratch, int stride
 {
   static_assert(NV <= 16, "up to 16 values");
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
-  T x[16];
+  // NV padded to P = 2^S: S transposing stages at distances 16, 8, ... keep half the values
+  // each, plain butterfly sums cover the smaller distances; value q ends in lanes q * (32 / P)
+  constexpr int S = NV <= 1 ? 0 : (NV <= 2 ? 1 : (NV <= 4 ? 2 : (NV <= 8 ? 3 : 4)));
+  constexpr int P = 1 << S, G = 32 / P;
+  T x[P];
 #pragma unroll
-  for (int q = 0; q < 16; q++)
+  for (int q = 0; q < P; q++)
     x[q] = q < NV ? v[q] : T(0);
 #pragma unroll
-  for (int h = 8; h >= 1; h >>= 1) // exchange distance 2h, keep h values
+  for (int h = P / 2; h >= 1; h >>= 1)
   {
-    const bool up = (lane & (2 * h)) != 0;
+    const int d   = G * h; // exchange distance, keep h values
+    const bool up = (lane & d) != 0;
 #pragma unroll
     for (int q = 0; q < h; q++)
     {
       const T send = up ? x[q] : x[q + h];
-      const T recv = __shfl_xor_sync(0xffffffffu, send, 2 * h);
+      const T recv = __shfl_xor_sync(0xffffffffu, send, d);
       x[q]         = (up ? x[q + h] : x[q]) + recv;
     }
   }
-  x[0] += __shfl_xor_sync(0xffffffffu, x[0], 1);
-  if ((lane & 1) == 0 && (lane >> 1) < NV)
-    scratch[(lane >> 1) * stride + wid] = x[0];
+#pragma unroll
+  for (int d = G / 2; d >= 1; d >>= 1)
+    x[0] += __shfl_xor_sync(0xffffffffu, x[0], d);
+  if ((lane & (G - 1)) == 0 && lane / G < NV)
+    scratch[(lane / G) * stride + wid] = x[0];
   __syncthreads();
   if (wid == 0)
   {

@@ -150,49 +150,51 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
 }
 
 // out[c] = scale * (rows[c] . x) for c < nrows (rows in shared or global memory, stride
-// ld, x in shared memory): every warp owns up to 8 rows and issues the loads of four
-// 32-column strips of all of them (32 loads in flight) before the first product
+// ld, x in shared memory): every warp owns up to 8 rows, a lane sums its columns of all of
+// them, and one transposed reduction (9 shuffles for the 8 sums) finishes them.  The loop
+// is kept short: the walker-resident kernel's speed depends on how much of its loop body
+// the SM's instruction cache holds.
 template<typename T, int NT>
 __device__ __forceinline__ void rows_dot(const T* rows, int ld, int nrows, const T* x, int n, T* out, T scale)
 {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int NW = NT / 32;
-  constexpr int JB = 4; // 32-column strips per batch of loads
   for (int c0 = wid; c0 < nrows; c0 += 8 * NW)
   {
     T a[8];
 #pragma unroll
     for (int q = 0; q < 8; q++)
       a[q] = T(0);
-    for (int jb = lane; jb < n; jb += 32 * JB)
+#pragma unroll 1
+    for (int j = lane; j < n; j += 32)
     {
-      T v[JB][8], xv[JB];
+      const T xv = x[j];
 #pragma unroll
-      for (int u = 0; u < JB; u++)
+      for (int q = 0; q < 8; q++)
       {
-        const int j = jb + 32 * u;
-        xv[u]       = j < n ? x[j] : T(0);
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-        {
-          const int c = c0 + q * NW;
-          v[u][q]     = (c < nrows && j < n) ? rows[(size_t)c * ld + j] : T(0);
-        }
+        const int c = c0 + q * NW;
+        a[q] += (c < nrows ? rows[(size_t)c * ld + j] : T(0)) * xv;
       }
-#pragma unroll
-      for (int u = 0; u < JB; u++)
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-          a[q] += v[u][q] * xv[u];
     }
+    // transposed reduction: distances 16, 8, 4 halve the values, 2 and 1 finish the sums;
+    // lane l ends with the sum of row value (l >> 2) & 7
 #pragma unroll
-    for (int q = 0; q < 8; q++)
+    for (int h = 4; h >= 1; h >>= 1)
     {
-      const T v = warp_sum(a[q]);
-      const int c = c0 + q * NW;
-      if (lane == 0 && c < nrows)
-        out[c] = scale * v;
+      const bool up = (lane & (4 * h)) != 0;
+#pragma unroll
+      for (int q = 0; q < h; q++)
+      {
+        const T send = up ? a[q] : a[q + h];
+        const T recv = __shfl_xor_sync(0xffffffffu, send, 4 * h);
+        a[q]         = (up ? a[q + h] : a[q]) + recv;
+      }
     }
+    a[0] += __shfl_xor_sync(0xffffffffu, a[0], 2);
+    a[0] += __shfl_xor_sync(0xffffffffu, a[0], 1);
+    const int q = (lane >> 2) & 7, c = c0 + q * NW;
+    if ((lane & 3) == 0 && c < nrows)
+      out[c] = scale * a[0];
   }
 }
 
@@ -222,25 +224,34 @@ __device__ __forceinline__ void spline_pair_vgl(const DevState<T>& s, const T* o
 #pragma unroll
       for (int k = 0; k < 4; k++)
         Vec<T>::load(base + i * s.xs + j * s.ys + k * s.zs, v[j][k]);
+    // z sums of every (j, orbital), then y sums, then this plane's x weights
+    T t0[2] = {T(0), T(0)}, t1[2] = {T(0), T(0)}, t2[2] = {T(0), T(0)}, u1[2] = {T(0), T(0)}, u2[2] = {T(0), T(0)};
 #pragma unroll
     for (int j = 0; j < 4; j++)
     {
-      const T pre00 = a[i] * b[j], pre10 = da[i] * b[j], pre01 = a[i] * db[j], pre20 = d2a[i] * b[j],
-              pre02 = a[i] * d2b[j];
 #pragma unroll
       for (int w = 0; w < 2; w++)
       {
         const T s0 = c[0] * v[j][0][w] + c[1] * v[j][1][w] + c[2] * v[j][2][w] + c[3] * v[j][3][w];
         const T s1 = dc[0] * v[j][0][w] + dc[1] * v[j][1][w] + dc[2] * v[j][2][w] + dc[3] * v[j][3][w];
         const T s2 = d2c[0] * v[j][0][w] + d2c[1] * v[j][1][w] + d2c[2] * v[j][2][w] + d2c[3] * v[j][3][w];
-        acc[0][w] += pre00 * s0;
-        acc[1][w] += pre10 * s0;
-        acc[2][w] += pre01 * s0;
-        acc[3][w] += pre00 * s1;
-        acc[4][w] += pre20 * s0;
-        acc[5][w] += pre02 * s0;
-        acc[6][w] += pre00 * s2;
+        t0[w] += b[j] * s0;
+        t1[w] += db[j] * s0;
+        t2[w] += d2b[j] * s0;
+        u1[w] += b[j] * s1;
+        u2[w] += b[j] * s2;
       }
+    }
+#pragma unroll
+    for (int w = 0; w < 2; w++)
+    {
+      acc[0][w] += a[i] * t0[w];
+      acc[1][w] += da[i] * t0[w];
+      acc[2][w] += a[i] * t1[w];
+      acc[3][w] += a[i] * u1[w];
+      acc[4][w] += d2a[i] * t0[w];
+      acc[5][w] += a[i] * t2[w];
+      acc[6][w] += a[i] * u2[w];
     }
   }
   const T fx = s.grid_scale[0], fy = s.grid_scale[1], fz = s.grid_scale[2];
@@ -933,7 +944,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         if (s.has_j2)
         {
           const T xo = Rs[iat], yo = Rs[s.ne_pad + iat], zo = Rs[2 * s.ne_pad + iat];
-#pragma unroll 2
+          // not unrolled: a smaller loop body keeps more of the kernel in the instruction cache
+#pragma unroll 1
           for (int j = threadIdx.x; j < s.ne; j += NT)
           {
             if (j == iat)
