@@ -242,16 +242,21 @@ __device__ __forceinline__ void spline_pair_vgl(const DevState<T>& s, const T* o
         u2[w] += b[j] * s2;
       }
     }
+    // this plane's x weights by selection: indexing the weight arrays with the loop counter
+    // would place them in local memory
+    const T ai   = i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+    const T dai  = i == 0 ? da[0] : (i == 1 ? da[1] : (i == 2 ? da[2] : da[3]));
+    const T d2ai = i == 0 ? d2a[0] : (i == 1 ? d2a[1] : (i == 2 ? d2a[2] : d2a[3]));
 #pragma unroll
     for (int w = 0; w < 2; w++)
     {
-      acc[0][w] += a[i] * t0[w];
-      acc[1][w] += da[i] * t0[w];
-      acc[2][w] += a[i] * t1[w];
-      acc[3][w] += a[i] * u1[w];
-      acc[4][w] += d2a[i] * t0[w];
-      acc[5][w] += a[i] * t2[w];
-      acc[6][w] += a[i] * u2[w];
+      acc[0][w] += ai * t0[w];
+      acc[1][w] += dai * t0[w];
+      acc[2][w] += ai * t1[w];
+      acc[3][w] += ai * u1[w];
+      acc[4][w] += d2ai * t0[w];
+      acc[5][w] += ai * t2[w];
+      acc[6][w] += ai * u2[w];
     }
   }
   const T fx = s.grid_scale[0], fy = s.grid_scale[1], fz = s.grid_scale[2];
