@@ -205,3 +205,25 @@ def test_resident_sweep_matches_staged(prec, delay):
     assert rel_err(L1, L0) < tol
     assert rel_err(A1, A0) < (1e-9 if prec == 8 else 1e-3)
     assert rel_err(B1, B0) < (1e-9 if prec == 8 else 1e-3)
+
+
+def test_positions_and_log_into_caller_buffers():
+    """positions(out=...) and get_log(out=...) fill the caller's arrays (the e2e path's pinned
+    buffers) with exactly what the allocating calls return; a wrong shape is refused."""
+    Crowd, DeviceSystem = _gpu()
+    s = small(3)
+    g = Crowd(DeviceSystem(s), 5, 3)
+    g.load_walkers(make_walkers(s, 5, seed=3))
+    g.mw_evaluateLog()
+    g.vmc_sweeps(2, 0.3, 5, rng_mode=1)
+    buf = np.full((5, s.n_elec, 3), np.nan)
+    assert g.positions(out=buf) is buf
+    np.testing.assert_array_equal(buf, g.positions())
+    out = (np.zeros(5), np.zeros(5, np.int32), np.zeros((5, 4)))
+    lp, sg, parts = g.get_log(out=out)
+    assert lp is out[0]
+    ref = g.get_log()
+    for a, b in zip((lp, sg, parts), ref):
+        np.testing.assert_array_equal(a, b)
+    with pytest.raises(AssertionError):
+        g.positions(out=np.zeros((5, s.n_elec, 2)))
