@@ -313,14 +313,18 @@ __device__ __forceinline__ void sweep_shared_init(SweepShared<T, LEARNED>& sh)
   __syncthreads();
 }
 
-// The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.
-template<typename T, int NT, bool LEARNED>
+// The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.  STAGED
+// compiles the delayed-update form with the segment's inverse rows in shared memory and
+// nothing else (the rank-1 and unstaged branches drop out of the loop body, which the
+// instruction cache then holds better); the generic form decides both at run time.
+template<typename T, int NT, bool LEARNED, bool STAGED>
 __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i1, int w, unsigned char* smem_raw,
                                              SweepShared<T, LEARNED>& sh, unsigned long long& n_acc,
                                              unsigned long long& n_rej)
 {
   const int lda = s.lda, n = s.norb, K = s.k;
-  const bool seg_smem  = K > 1 && s.seg_smem != 0;
+  const bool delayed   = STAGED || K > 1;
+  const bool seg_smem  = STAGED || (K > 1 && s.seg_smem != 0);
   const SweepLayout Ly = sweep_layout<T>(lda, s.ne_pad, K, seg_smem, LEARNED, sweep_ncoef(s));
   T* sm     = reinterpret_cast<T*>(smem_raw);
   T* pre    = sm + Ly.pre;    // 2 x npre x lda prefetch buffers
@@ -453,7 +457,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       // the gradient and self-ratio sums of the same elements
       const T* inv = arow;
       T g[4]       = {0, 0, 0, 0};
-      if (K > 1 && dc > 0)
+      if (delayed && dc > 0)
       {
         // pv_c = U_c . Ainv[row] of the earlier slots of this segment, formed when slot c
         // was decided (zero for a rejected move), read straight from the table
@@ -497,7 +501,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
       else
       {
-        if (iat + 1 < i1 && K > 1)
+        if (iat + 1 < i1 && delayed)
           prefetch_rows(s, slot, row + 1, pnext, !seg_smem, threadIdx.x, NT);
         for (int j = threadIdx.x; j < n; j += NT)
         {
@@ -845,7 +849,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
       // ------------------------------------------------ accept / reject
       const bool accd = sh.acc != 0;
-      if (K > 1)
+      if (delayed)
       {
         T* U       = s.U + slot * K * lda;
         T* V       = s.V + slot * K * lda;
@@ -927,7 +931,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         }
         __syncthreads();
       }
-      if (K == 1 && iat + 1 < i1)
+      if (!delayed && iat + 1 < i1)
       {
         // rank-1 updates change the whole inverse: the next electron's rows are read after it
         __syncthreads();
@@ -1000,7 +1004,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         }
       }
       __syncthreads();
-      if (K > 1)
+      if (delayed)
         dc++;
     }
     async_wait_all();
@@ -1016,7 +1020,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       }
     }
     // hand the segment's Binv to the batched flush, positions and J2 state back to HBM
-    if (K > 1)
+    if (delayed)
     {
       T* Binv = s.Binv + slot * K * K;
       for (int e = threadIdx.x; e < dc * K; e += NT)
@@ -1030,7 +1034,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   }
 }
 
-template<typename T, int NT, int MINB, bool LEARNED>
+template<typename T, int NT, int MINB, bool LEARNED, bool STAGED>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1038,7 +1042,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
   sweep_shared_init(sh);
   unsigned long long n_acc = 0, n_rej = 0;
   for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
-    sweep_walker<T, NT, LEARNED>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
+    sweep_walker<T, NT, LEARNED, STAGED>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
   if (threadIdx.x == 0)
   {
     atomicAdd(s.counters + 0, n_acc);
@@ -1093,7 +1097,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_multi_kernel(const DevState<T>
       __syncthreads();
       cur = c;
     }
-    sweep_walker<T, NT, false>(ds, st.i0[a], st.i1[a], item - st.begin[a], smem_raw, sh, n_acc, n_rej);
+    sweep_walker<T, NT, false, false>(ds, st.i0[a], st.i1[a], item - st.begin[a], smem_raw, sh, n_acc, n_rej);
     __syncthreads();
   }
   if (cur >= 0 && threadIdx.x == 0)
@@ -1164,18 +1168,40 @@ static cudaError_t with_threads(int nt, F&& f)
   return cudaErrorInvalidValue;
 }
 
+// the two forms of the kernel: delayed updates with the segment rows staged, or generic
+template<typename F>
+static cudaError_t with_staged(bool staged, F&& f)
+{
+  return staged ? f(std::true_type{}) : f(std::false_type{});
+}
+
+template<typename T>
+static bool sweep_staged(const DevState<T>& s)
+{
+  return s.k > 1 && s.seg_smem != 0;
+}
+
 template<typename T>
 cudaError_t setup_sweep_kernel()
 {
-  cudaError_t e = cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  for (int nt : {128, 256, 512})
-    if (e == cudaSuccess && sweep_threads_ok(nt, sizeof(T)))
-      e = with_threads<T>(nt, [](auto c) {
-        constexpr int NT = decltype(c)::value;
-        return cudaFuncSetAttribute(sweep_kernel<T, NT, SweepMinb<T, NT>::v, false>,
+  cudaError_t e = cudaSuccess;
+  for (bool staged : {false, true})
+  {
+    if (e == cudaSuccess)
+      e = with_staged(staged, [](auto g) {
+        return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true, decltype(g)::value>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       });
+    for (int nt : {128, 256, 512})
+      if (e == cudaSuccess && sweep_threads_ok(nt, sizeof(T)))
+        e = with_staged(staged, [&](auto g) {
+          return with_threads<T>(nt, [](auto c) {
+            constexpr int NT = decltype(c)::value;
+            return cudaFuncSetAttribute(sweep_kernel<T, NT, SweepMinb<T, NT>::v, false, decltype(g)::value>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+          });
+        });
+  }
   return e;
 }
 
@@ -1200,13 +1226,18 @@ cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1,
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
     if (!s.mlp_simt || !s.mlp_params)
       return cudaErrorInvalidValue;
-    sweep_kernel<T, NT, MINB, true><<<grid, NT, sweep_smem_bytes(s, true), st>>>(s, i0, i1);
-    return cudaGetLastError();
+    return with_staged(sweep_staged(s), [&](auto g) {
+      sweep_kernel<T, NT, MINB, true, decltype(g)::value><<<grid, NT, sweep_smem_bytes(s, true), st>>>(s, i0, i1);
+      return cudaGetLastError();
+    });
   }
-  return with_threads<T>(nt, [&](auto c) {
-    constexpr int NT = decltype(c)::value;
-    sweep_kernel<T, NT, SweepMinb<T, NT>::v, false><<<grid, NT, sweep_smem_bytes(s, false), st>>>(s, i0, i1);
-    return cudaGetLastError();
+  return with_staged(sweep_staged(s), [&](auto g) {
+    return with_threads<T>(nt, [&](auto c) {
+      constexpr int NT = decltype(c)::value;
+      sweep_kernel<T, NT, SweepMinb<T, NT>::v, false, decltype(g)::value>
+          <<<grid, NT, sweep_smem_bytes(s, false), st>>>(s, i0, i1);
+      return cudaGetLastError();
+    });
   });
 }
 
@@ -1223,14 +1254,19 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
   if (learned)
   {
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, MINB, true>, NT,
-                                                      sweep_smem_bytes(s, true));
+    e = with_staged(sweep_staged(s), [&](auto g) {
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, sweep_kernel<T, NT, MINB, true, decltype(g)::value>, NT, sweep_smem_bytes(s, true));
+    });
   }
   else
-    e = with_threads<T>(nt, [&](auto c) {
-      constexpr int NT = decltype(c)::value;
-      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, NT, SweepMinb<T, NT>::v, false>,
-                                                           NT, sweep_smem_bytes(s, false));
+    e = with_staged(sweep_staged(s), [&](auto g) {
+      return with_threads<T>(nt, [&](auto c) {
+        constexpr int NT = decltype(c)::value;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, sweep_kernel<T, NT, SweepMinb<T, NT>::v, false, decltype(g)::value>, NT,
+            sweep_smem_bytes(s, false));
+      });
     });
   if (e != cudaSuccess)
     return e;
