@@ -80,10 +80,26 @@ def launches_per_sweep(system, k: int) -> int:
     return 1 + 5
 
 
-def flush_kernel_name(n: int, k: int, flush: int) -> str:
+def block_update_bytes_per_sweep(system, k: int, nw: int, acceptance: float) -> int:
+    """Algorithmic bytes of the block-lazy updates of one sweep: per spin group, every row
+    block but the first read and written before its segment and every block read and
+    written by the completing pass; per (block, set) application the accepted U and V rows
+    (acceptance x k of them), Binv restricted to them and the delay list."""
+    s = 4 if system.spec.precision == 4 else 8
+    lda, nspin = system.npad, system.spec.n_up
+    nseg = (nspin + k - 1) // k
+    rows = 2 * (nspin - min(k, nspin)) * lda + 2 * nspin * lda
+    m = acceptance * k
+    sets = nseg * nseg * (2 * m * lda + m * m + k)
+    return int(2 * nw * s * (rows + sets))
+
+
+def flush_kernel_name(n: int, k: int, flush: int, block_lazy: bool = False) -> str:
     """The flush kernel the library takes for n orbitals and delay rank k (flush_tc_variant:
     one pass while the whole product fits one MMA and 200 KB of shared memory, else column
-    tiles)."""
+    tiles; block-lazy updates where the crowd's segment rows are staged)."""
+    if flush == 4 and block_lazy:
+        return "block_update_kernel (block-lazy, SIMT FP32)"
     if flush == 0:
         return "flush_fused_kernel (SIMT)"
     terms = "TF32" if flush == 1 else "3xTF32"
@@ -675,7 +691,11 @@ def run_ours(args, rank: int, world: int):
     restart()
     seg_ms, flush_ms, seg_per_sweep, flush_per_sweep = crowd.profile_sweep(3)
     algo = bytes_per_walker_move(system, k, with_flush=False) * nw * system.n_elec // seg_per_sweep
-    flush_bytes = flush_bytes_per_launch(system, k, nw)
+    block_lazy = crowd.sweep_info(args.flush)["block_lazy"]
+    if block_lazy:
+        flush_bytes = block_update_bytes_per_sweep(system, k, nw, acc / max(acc + rej, 1)) // flush_per_sweep
+    else:
+        flush_bytes = flush_bytes_per_launch(system, k, nw)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -696,7 +716,9 @@ def run_ours(args, rank: int, world: int):
     extras = {}
     if world == 1 and not args.no_extras:
         extras["virtual_moves"] = virtual_moves(crowd, system, peak)
-        extras["dmc"] = dmc_rate(dsys, system, crowd.positions(), args.flush)
+        # DMC's small time step accepts ~3/4 of the moves: the block-lazy updates then carry
+        # most slots of every set and the tensor-core flush after every segment is faster
+        extras["dmc"] = dmc_rate(dsys, system, crowd.positions(), 3 if args.flush == 4 else args.flush)
     if world == 1 and not args.no_effective and args.workload == "c1_384e":
         Req = crowd.positions()[:64]
         rerr = {"uniform_start": ratio_error(system, dsys, 64, k),
@@ -710,7 +732,8 @@ def run_ours(args, rank: int, world: int):
         "config": {"workload": f"{args.workload}: {DESCRIPTIONS.get(args.workload, '')}",
                    "step": "one VMC sweep (every electron of every walker moved once), CUDA graph replay",
                    "walkers_per_gpu": nw, "electrons": system.n_elec, "delay_rank": k,
-                   "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32"}[args.flush],
+                   "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32",
+                             4: "block-lazy updates, SIMT FP32" if block_lazy else "tcgen05 3xTF32"}[args.flush],
                    "l2": "inputs larger than L2 (spline table 102 MB + inverses/gradients ~0.8 GB per sweep)",
                    "recompute": ({"every_sweeps": recompute_every, "measured_ms": rec_ms, "added": n_rec,
                                   "how": "the FP64 recompute of all walkers, timed once with CUDA events, added "
@@ -724,7 +747,7 @@ def run_ours(args, rank: int, world: int):
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                      else "fallback 6.8 TB/s", "traffic": traffic, "ms_per_launch": seg_ms,
                      "algorithmic_bytes_per_launch": algo, "launches_per_sweep": seg_per_sweep,
-                     "flush": {"kernel": flush_kernel_name(system.spec.n_up, k, args.flush),
+                     "flush": {"kernel": flush_kernel_name(system.spec.n_up, k, args.flush, block_lazy),
                                "ms_per_launch": flush_ms,
                                "launches_per_sweep": flush_per_sweep, "algorithmic_bytes_per_launch": flush_bytes,
                                "achieved_gbs": flush_bytes / (flush_ms / 1e3) / 1e9 if flush_ms else None}},
@@ -754,8 +777,9 @@ def main():
     ap.add_argument("--workload", default="c1_384e", choices=sorted(SPECS) + ["c3_mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--equil", type=int, default=20, help="untimed equilibration sweeps before the warm-up")
-    ap.add_argument("--flush", type=int, default=3, choices=[0, 1, 3],
-                    help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32")
+    ap.add_argument("--flush", type=int, default=4, choices=[0, 1, 3, 4],
+                    help="delayed-update flush: 0 SIMT, 1 tensor cores TF32, 3 tensor cores 3xTF32, 4 block-lazy "
+                         "updates where the segment rows are staged (else as 3)")
     ap.add_argument("--no-effective", action="store_true", help="skip the effective-samples comparison")
     ap.add_argument("--no-extras", action="store_true", help="skip the virtual-move and DMC measurements")
     ap.add_argument("--walkers", type=int, default=0, help="walkers of the crowd (0: the workload's own count; "

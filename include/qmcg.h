@@ -91,7 +91,10 @@ typedef struct
                           sweep), else the staged per-electron kernels; 1: always the staged kernels */
   int flush;           /* delayed-update flush of the walker-resident path: 0 = SIMT (FP32 or FP64),
                           1 = tensor cores TF32, 3 = tensor cores 3xTF32 split precision (FP32 move loop,
-                          delay rank <= 64; otherwise the SIMT flush is used) */
+                          delay rank <= 64; otherwise the SIMT flush is used), 4 = block-lazy updates: a
+                          segment's row block receives the pending updates of its spin group right before
+                          the segment, and one pass completes the inverse after the spin group (crowds
+                          whose segment rows are staged, see qmcg_sweep_info; otherwise as 3) */
 } qmcg_sweep_params;
 
 typedef struct
@@ -438,6 +441,13 @@ int qmcg_profile_ratio(qmcg_crowd crowd, int num_electrons, double* ms_per_launc
  * per batched flush launch, out[2] and out[3] = launches of each per sweep.
  * Needs a graph built by qmcg_vmc_sweeps with rng_mode 1 and path 0. */
 int qmcg_profile_sweep(qmcg_crowd crowd, int num_sweeps, double* out4);
+
+/* Configuration helper (no reference counterpart): how the walker-resident sweep of
+ * this crowd runs with delayed-update flush kind `flush` (qmcg_sweep_params.flush).
+ * out[0] = threads per walker of the resident kernel, out[1] = 1 if a segment's inverse
+ * rows are staged in shared memory, out[2] = delayed-update sets kept per spin and
+ * walker, out[3] = 1 if the flush kind runs as block-lazy updates on this crowd. */
+int qmcg_sweep_info(qmcg_crowd crowd, int flush, int* out4);
 
 /* Measurement helper (no reference counterpart): device time in ms of one periodic
  * FP64 recompute of every walker (the full recompute qmcg_vmc_sweeps runs every

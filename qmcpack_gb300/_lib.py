@@ -19,7 +19,7 @@ EXPORTS = [
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
     "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
     "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_ex", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
-    "qmcg_profile_sweep", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
+    "qmcg_profile_sweep", "qmcg_sweep_info", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
     "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
     "qmcg_proposal_backward", "qmcg_proposal_features", "qmcg_vmc_sweeps_learned",
     "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info", "qmcg_crowd_set_threads",
@@ -103,6 +103,7 @@ def load(path: str = LIB_PATH):
         "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
         "qmcg_profile_sweep": [vp, C.c_int, _dp],
+        "qmcg_sweep_info": [vp, C.c_int, _ip],
         "qmcg_mw_evaluate_local_energy": [vp, _dp, _dp, _dp],
         "qmcg_vmc_sweeps_measure": [vp, C.POINTER(SweepParams), C.c_int, _dp, _dp, C.POINTER(SweepStats)],
         "qmcg_proposal_init": [vp, C.c_uint64, C.c_double],

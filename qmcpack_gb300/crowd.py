@@ -354,6 +354,13 @@ class Crowd:
         check(self.L.qmcg_profile_sweep(self.handle, nsweeps, _p(out)))
         return float(out[0]), float(out[1]), int(out[2]), int(out[3])
 
+    def sweep_info(self, flush: int = 0):
+        """How the walker-resident sweep runs with this flush kind: threads per walker,
+        segment rows staged, delayed-update sets per spin and walker, block-lazy updates."""
+        out = np.zeros(4, np.int32)
+        check(self.L.qmcg_sweep_info(self.handle, flush, _p(out, _ip)))
+        return {"threads": int(out[0]), "rows_staged": bool(out[1]), "sets": int(out[2]), "block_lazy": bool(out[3])}
+
     def profile_recompute(self) -> float:
         """Device ms of one periodic FP64 recompute of every walker."""
         ms = C.c_double()

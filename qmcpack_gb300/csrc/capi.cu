@@ -456,6 +456,7 @@ struct qmcg_crowd_s
   virtual int sweeps_async(int n)                        = 0;
   virtual int profile_ratio(int niat, double* ms)        = 0;
   virtual int profile_sweep(int n, double* out)          = 0;
+  virtual int sweep_info(int flush, int* out)            = 0;
   virtual int sync(qmcg_sweep_stats* st)                 = 0;
   virtual int local_energy(double* el, double* ke, double* vp) = 0;
   virtual int set_threads(int nt)                        = 0;
@@ -700,10 +701,15 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&d.dgrad, 2 * (size_t)nw * N * 3 * lda));
     CUDA_TRY(mem.alloc(&d.dlap, 2 * (size_t)nw * N * lda));
     CUDA_TRY(mem.alloc(&d.psiv, 2 * (size_t)nw * N * lda));
-    CUDA_TRY(mem.alloc(&d.U, 2 * (size_t)nw * k * lda));
-    CUDA_TRY(mem.alloc(&d.V, 2 * (size_t)nw * k * lda));
-    CUDA_TRY(mem.alloc(&d.Binv, 2 * (size_t)nw * k * k));
-    CUDA_TRY(mem.alloc(&d.delay_list, 2 * (size_t)nw * k));
+    // a set of delayed-update factors per segment where the segment rows are staged (the
+    // block-lazy updates read the sets of a whole spin group), one set otherwise
+    d.seg_smem = sweep_seg_smem<T>(d) ? 1 : 0;
+    d.nsets    = d.seg_smem ? (std::max(sys->nup, sys->ne - sys->nup) + k - 1) / k : 1;
+    const size_t ns = d.nsets;
+    CUDA_TRY(mem.alloc(&d.U, 2 * (size_t)nw * ns * k * lda));
+    CUDA_TRY(mem.alloc(&d.V, 2 * (size_t)nw * ns * k * lda));
+    CUDA_TRY(mem.alloc(&d.Binv, 2 * (size_t)nw * ns * k * k));
+    CUDA_TRY(mem.alloc(&d.delay_list, 2 * (size_t)nw * ns * k));
     CUDA_TRY(mem.alloc(&d.J2, (size_t)nw * 5 * ne_pad));
     CUDA_TRY(mem.alloc(&d.J1, (size_t)nw * 5 * ne_pad));
     CUDA_TRY(mem.alloc(&d.log_abs, 2 * (size_t)nw));
@@ -727,6 +733,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&tc_err, 1));
     if (std::is_same<T, float>::value)
       CUDA_TRY(setup_flush_tc());
+    CUDA_TRY(setup_block_update<T>());
     CUDA_TRY(mem.alloc(&d.ucursor, 2));
     CUDA_TRY(mem.alloc(&d.sweep_counter, 1));
     CUDA_TRY(mem.alloc(&Mt, 2 * (size_t)nw * N * N));
@@ -741,7 +748,6 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
     sweep_nt   = sweep_default_threads<T>(d);
-    d.seg_smem = sweep_seg_smem<T>(d) ? 1 : 0;
     CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size, false, sweep_nt));
     CUDA_TRY(setup_local_energy<T>());
     CUDA_TRY(mem.alloc(&e_out, 3 * (size_t)nw));
@@ -1058,15 +1064,51 @@ struct Crowd final : qmcg_crowd_s
 
   bool resident(const qmcg_sweep_params* p) const { return p->rng_mode == 1 && p->path == 0; }
 
-  // the flush of one spin after a resident segment: tensor cores when asked for and possible
-  cudaError_t launch_flush_choice(int spin, int dc, cudaStream_t st = nullptr)
+  // the flush of one spin after a resident segment (delayed-update set `set`): tensor cores
+  // when asked for and possible (the block-lazy kind flushes with 3xTF32 where it does not apply)
+  cudaError_t launch_flush_choice(int spin, int dc, int set = 0, cudaStream_t st = nullptr)
   {
     if (!st)
       st = stream;
     if constexpr (std::is_same<T, float>::value)
-      if ((flush_kind == 1 || flush_kind == 3) && flush_tc_supported(sys->norb, k, sys->lda))
-        return launch_flush_tc(crowd_flush_args<float>(s, spin, dc, W), flush_kind, tc_err, st);
-    return launch_flush_fused<T>(crowd_flush_args<T>(s, spin, dc, W), st);
+      if ((flush_kind == 1 || flush_kind == 3 || flush_kind == 4) && flush_tc_supported(sys->norb, k, sys->lda))
+        return launch_flush_tc(crowd_flush_args<float>(s, spin, dc, W, set), flush_kind == 1 ? 1 : 3, tc_err, st);
+    return launch_flush_fused<T>(crowd_flush_args<T>(s, spin, dc, W, set), st);
+  }
+
+  // block-lazy delayed updates on this sweep (flush kind 4, segment rows staged)
+  bool lazy_updates() const { return flush_kind == 4 && k > 1 && block_update_supported<T>(s); }
+
+  // the launches of one spin group of the walker-resident sweep with delayed updates: each
+  // segment followed by its flush, or (block-lazy) each segment preceded by the update of
+  // its row block and the spin group followed by the completing pass; `seg(i0, i1)` and
+  // `upd(launch)` enqueue a segment and an update launch
+  template<typename Seg, typename Upd>
+  int enqueue_spin_group(int g, Seg&& seg, Upd&& upd)
+  {
+    const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
+    const bool lazy = lazy_updates();
+    const int nseg  = (last - first + k - 1) / k;
+    for (int b = 0; b < nseg; b++)
+    {
+      const int i0 = first + b * k, i1 = std::min(i0 + k, last);
+      if (lazy && b > 0)
+      {
+        const int rc = upd([=] { return launch_block_update<T>(s, g, b, 1, b, false, stream); });
+        if (rc)
+          return rc;
+      }
+      int rc = seg(i0, i1);
+      if (rc)
+        return rc;
+      if (!lazy)
+        rc = upd([=] { return launch_flush_choice(g, i1 - i0, s.nsets > 1 ? b : 0); });
+      if (rc)
+        return rc;
+    }
+    if (lazy)
+      return upd([=] { return launch_block_update<T>(s, g, 0, nseg, nseg, true, stream); });
+    return QMCG_OK;
   }
 
   // the segments [i0, i1) of one sweep on the walker-resident path, in launch order
@@ -1095,13 +1137,18 @@ struct Crowd final : qmcg_crowd_s
     {
       for (int g = 0; g < 2; g++)
       {
-        const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
-        for (int i0 = first; i0 < last; i0 += k)
-        {
-          const int i1 = std::min(i0 + k, last);
-          CUDA_TRY(launch_sweep_segment<T>(s, grid, i0, i1, stream, learned, sweep_nt));
-          CUDA_TRY(launch_flush_choice(g, i1 - i0));
-        }
+        const int rc = enqueue_spin_group(
+            g,
+            [&](int i0, int i1) -> int {
+              CUDA_TRY(launch_sweep_segment<T>(s, grid, i0, i1, stream, learned, sweep_nt));
+              return QMCG_OK;
+            },
+            [&](auto launch) -> int {
+              CUDA_TRY(launch());
+              return QMCG_OK;
+            });
+        if (rc)
+          return rc;
       }
     }
     else
@@ -2014,6 +2061,17 @@ struct Crowd final : qmcg_crowd_s
   // out[2] = sweep-kernel launches per sweep, out[3] = flush launches per sweep.
   // CUDA events on the crowd's stream around every launch; the repair and counter
   // kernels run between sweeps untimed.
+  int sweep_info(int flush, int* out) override
+  {
+    if (!out)
+      return fail(QMCG_ERR_ARG, "null output");
+    out[0] = sweep_nt;
+    out[1] = s.seg_smem;
+    out[2] = s.nsets;
+    out[3] = flush == 4 && k > 1 && block_update_supported<T>(s) ? 1 : 0;
+    return QMCG_OK;
+  }
+
   int profile_sweep(int n, double* out) override
   {
     if (n <= 0 || !out)
@@ -2043,23 +2101,20 @@ struct Crowd final : qmcg_crowd_s
       {
         for (int g = 0; g < 2; g++)
         {
-          const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
-          for (int i0 = first; i0 < last; i0 += k)
-          {
-            const int i1 = std::min(i0 + k, last);
-            int rc = timed(0, [&] { return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream, false,
-                                                                  sweep_nt); });
-            if (rc)
-              return rc;
-            rc = timed(1, [&] { return launch_flush_choice(g, i1 - i0); });
-            if (rc)
-              return rc;
-            if (it == 0)
-            {
-              nsk++;
-              nfl++;
-            }
-          }
+          const int rc = enqueue_spin_group(
+              g,
+              [&](int i0, int i1) {
+                nsk += it == 0;
+                return timed(0, [&] {
+                  return launch_sweep_segment<T>(s, sweep_grid_size, i0, i1, stream, false, sweep_nt);
+                });
+              },
+              [&](auto launch) {
+                nfl += it == 0;
+                return timed(1, launch);
+              });
+          if (rc)
+            return rc;
         }
       }
       else
@@ -2325,7 +2380,11 @@ struct Group final : qmcg_group_s
       {
         Crowd<T>* x = cs[st.crowd[a]];
         if (x->k > 1)
-          CUDA_TRY(x->launch_flush_choice(st.i0[a] >= x->sys->nup ? 1 : 0, st.i1[a] - st.i0[a], stream));
+          {
+            const int sp = st.i0[a] >= x->sys->nup ? 1 : 0, first = sp ? x->sys->nup : 0;
+            const int set = x->s.nsets > 1 ? (st.i0[a] - first) / x->k : 0;
+            CUDA_TRY(x->launch_flush_choice(sp, st.i1[a] - st.i0[a], set, stream));
+          }
       }
     }
     for (auto* x : cs)
@@ -2598,6 +2657,7 @@ extern "C" int qmcg_mw_evaluate_gl(qmcg_crowd c, double* lp, double* grads, doub
 }
 extern "C" int qmcg_profile_ratio(qmcg_crowd c, int niat, double* ms) { CROWD_CALL(c, profile_ratio(niat, ms)); }
 extern "C" int qmcg_profile_sweep(qmcg_crowd c, int n, double* ms) { CROWD_CALL(c, profile_sweep(n, ms)); }
+extern "C" int qmcg_sweep_info(qmcg_crowd c, int flush, int* out) { CROWD_CALL(c, sweep_info(flush, out)); }
 
 // ---------------------------------------------------------------------------
 // determinant-engine flush on caller device buffers

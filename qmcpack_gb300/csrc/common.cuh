@@ -127,6 +127,10 @@ struct DevState
   // when that does not enlarge the kernel's shared-memory footprint)
   int seg_smem;
   int j1_nspecies; // ion species of the one-body functors (rows of j1c)
+  // delayed-update sets per spin slot: U, V, Binv and delay_list hold nsets sets of k slots
+  // per (spin, walker) ([2][nw][nsets][k][...]); a segment of the walker-resident sweep writes
+  // set (i0 - first) / k when nsets > 1, and every other user works on set 0
+  int nsets;
 };
 
 // fields of one move record of the walker-resident sweep (qmcg_vmc_sweeps_trace)

@@ -74,9 +74,9 @@ bool flush_tc_supported(int n, int k, int lda);
 cudaError_t setup_flush_tc();
 cudaError_t launch_flush_tc(const FlushArgs<float>& f, int terms, int* err, cudaStream_t st);
 
-// flush arguments of one spin of a crowd
+// flush arguments of one spin of a crowd, delayed-update set `set`
 template<typename T>
-inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* W)
+inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* W, int set = 0)
 {
   FlushArgs<T> f;
   f.nw         = s.nw;
@@ -85,17 +85,29 @@ inline FlushArgs<T> crowd_flush_args(const DevState<T>& s, int spin, int dc, T* 
   f.k          = s.k;
   f.dc         = dc;
   f.sA         = (long long)s.norb * s.lda;
-  f.sU         = (long long)s.k * s.lda;
-  f.sB         = (long long)s.k * s.k;
-  f.sD         = s.k;
+  f.sU         = (long long)s.nsets * s.k * s.lda;
+  f.sB         = (long long)s.nsets * s.k * s.k;
+  f.sD         = s.nsets * s.k;
   f.ainv       = s.Ainv + (size_t)spin * s.nw * f.sA;
-  f.u          = s.U + (size_t)spin * s.nw * f.sU;
-  f.v          = s.V + (size_t)spin * s.nw * f.sU;
-  f.binv       = s.Binv + (size_t)spin * s.nw * f.sB;
-  f.delay_list = s.delay_list + (size_t)spin * s.nw * f.sD;
+  f.u          = s.U + (size_t)spin * s.nw * f.sU + (size_t)set * s.k * s.lda;
+  f.v          = s.V + (size_t)spin * s.nw * f.sU + (size_t)set * s.k * s.lda;
+  f.binv       = s.Binv + (size_t)spin * s.nw * f.sB + (size_t)set * s.k * s.k;
+  f.delay_list = s.delay_list + (size_t)spin * s.nw * f.sD + (size_t)set * s.k;
   f.w          = W;
   return f;
 }
+
+// block-lazy delayed updates of the walker-resident sweep (block_update.cu): the row block
+// `block` (and, with complete, every block from it on: grid y = nblocks) of one spin
+// receives the sets it has not seen: [0, set_hi) before the segment that reads it, or
+// [block, set_hi) at the end of the spin group
+template<typename T>
+bool block_update_supported(const DevState<T>& s);
+template<typename T>
+cudaError_t setup_block_update();
+template<typename T>
+cudaError_t launch_block_update(const DevState<T>& s, int spin, int block, int nblocks, int set_hi, bool complete,
+                                cudaStream_t st);
 
 // local energy (energy.cu)
 struct EwaldHost

@@ -49,9 +49,10 @@ __global__ void __launch_bounds__(NT) propose_kernel(DevState<T> s, int iat, int
     T* invRow = s.invRow + (size_t)iw * s.lda;
     if (dc > 0)
     {
-      const T* U = s.U + wslot * s.k * s.lda;
-      const T* V = s.V + wslot * s.k * s.lda;
-      T* Binv    = s.Binv + wslot * s.k * s.k;
+      const size_t set0 = wslot * s.nsets; // set 0 of this slot
+      const T* U = s.U + set0 * s.k * s.lda;
+      const T* V = s.V + set0 * s.k * s.lda;
+      T* Binv    = s.Binv + set0 * s.k * s.k;
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
       // p[c] = U[c] . Ainv[row]
       for (int c = wid; c < dc; c += NT / 32)
@@ -439,10 +440,11 @@ __global__ void __launch_bounds__(NT) accept_kernel(DevState<T> s, int iat, int 
   }
   if (s.k > 1)
   {
-    T* U       = s.U + wslot * s.k * s.lda;
-    T* V       = s.V + wslot * s.k * s.lda;
-    T* Binv    = s.Binv + wslot * s.k * s.k;
-    int* dlist = s.delay_list + wslot * s.k;
+    const size_t set0 = wslot * s.nsets; // set 0 of this slot
+    T* U       = s.U + set0 * s.k * s.lda;
+    T* V       = s.V + set0 * s.k * s.lda;
+    T* Binv    = s.Binv + set0 * s.k * s.k;
+    int* dlist = s.delay_list + set0 * s.k;
     for (int j = threadIdx.x; j < n; j += blockDim.x)
       V[(size_t)dc * s.lda + j] = A[j];
     if (acc)
@@ -759,9 +761,9 @@ cudaError_t launch_flush_simt(const DevState<T>& s, int spin, int dc, T* W, cuda
   f.k          = s.k;
   f.dc         = dc;
   f.sA         = (long long)s.norb * s.lda;
-  f.sU         = (long long)s.k * s.lda;
-  f.sB         = (long long)s.k * s.k;
-  f.sD         = s.k;
+  f.sU         = (long long)s.nsets * s.k * s.lda;
+  f.sB         = (long long)s.nsets * s.k * s.k;
+  f.sD         = s.nsets * s.k;
   f.ainv       = s.Ainv + (size_t)spin * s.nw * f.sA;
   f.u          = s.U + (size_t)spin * s.nw * f.sU;
   f.v          = s.V + (size_t)spin * s.nw * f.sU;

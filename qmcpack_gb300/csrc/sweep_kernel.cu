@@ -369,6 +369,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   {
     const size_t slot = (size_t)spin * s.nw + w;
     const T* ainv_seg = s.Ainv + (slot * n + (i0 - first)) * lda; // rows of this segment's electrons
+    // this segment's delayed-update set: its own one when the crowd keeps a set per segment
+    const size_t dset = slot * s.nsets + (s.nsets > 1 ? (i0 - first) / K : 0);
     if (seg_smem && threadIdx.x == 0)
     {
       // the previous walker's reads of seg (generic proxy) precede this copy (async proxy)
@@ -851,9 +853,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       const bool accd = sh.acc != 0;
       if (delayed)
       {
-        T* U       = s.U + slot * K * lda;
-        T* V       = s.V + slot * K * lda;
-        int* dlist = s.delay_list + slot * K;
+        T* U       = s.U + dset * K * lda;
+        T* V       = s.V + dset * K * lda;
+        int* dlist = s.delay_list + dset * K;
         for (int j = threadIdx.x; j < n; j += NT)
           V[(size_t)dc * lda + j] = arow[j];
         const int m = i1 - i0; // slots of this segment
@@ -1022,7 +1024,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
     // hand the segment's Binv to the batched flush, positions and J2 state back to HBM
     if (delayed)
     {
-      T* Binv = s.Binv + slot * K * K;
+      T* Binv = s.Binv + dset * K * K;
       for (int e = threadIdx.x; e < dc * K; e += NT)
         Binv[e] = Bs[e];
     }

@@ -11,6 +11,20 @@ def test_flush_kernel_names_follow_the_library_choice():
     assert bench.flush_kernel_name(768, 64, 3).startswith("flush_tc_tiled_kernel ")
     assert bench.flush_kernel_name(384, 32, 3).startswith("flush_tc_tiled_kernel ")
     assert bench.flush_kernel_name(192, 32, 0) == "flush_fused_kernel (SIMT)"
+    # block-lazy updates where the segment rows are staged, the 3xTF32 flush elsewhere
+    assert bench.flush_kernel_name(192, 32, 4, True).startswith("block_update_kernel ")
+    assert bench.flush_kernel_name(768, 64, 4, False) == "flush_tc_tiled_kernel (tcgen05 3xTF32)"
+
+
+def test_block_update_bytes():
+    from qmcpack_gb300.system import make_system
+    s = make_system("c1_384e")
+    # no accepted slot: only the row blocks (5 before their segments, 6 in the completing
+    # pass, each read and written) and the delay lists
+    b0 = bench.block_update_bytes_per_sweep(s, 32, 512, 0.0)
+    rows = 2 * 512 * 4 * (2 * (192 - 32) * 192 + 2 * 192 * 192)
+    assert b0 == rows + 2 * 512 * 4 * 36 * 32
+    assert bench.block_update_bytes_per_sweep(s, 32, 512, 0.25) > b0
 
 
 def test_traffic_lines_of_the_committed_profiles():

@@ -103,13 +103,14 @@ def oracle_crowd(system, nw, k, R):
     return o
 
 
-def fp64_parity(name, system, nw, k, nsweeps, seed, walker_seed):
+def fp64_parity(name, system, nw, k, nsweeps, seed, walker_seed, flush=0):
     Crowd, DeviceSystem = _gpu()
     R = make_walkers(system, nw, seed=walker_seed)
     g = Crowd(DeviceSystem(system), nw, k)
+    assert g.sweep_info(flush)["block_lazy"] == (flush == 4)
     g.load_walkers(R)
     g.mw_evaluateLog()
-    ag, _, tg = g.vmc_sweeps_trace(nsweeps, TAU, seed)
+    ag, _, tg = g.vmc_sweeps_trace(nsweeps, TAU, seed, flush=flush)
     # ---- step by step on the GPU's trajectory
     o = oracle_crowd(system, nw, k, R)
     to, margin = o.replay_philox(tg, seed, TAU)
@@ -159,10 +160,13 @@ def test_c0_exact_parity():
     fp64_parity("c0_32e_fp64", s, s.spec.walkers, s.spec.delay, s.spec.steps, seed=20241, walker_seed=31)
 
 
-def test_c1_system_fp64_parity():
-    """The 384-electron system (FP32 coefficient values upcast to FP64) with delay rank 32."""
+@pytest.mark.parametrize("flush", [0, 4])
+def test_c1_system_fp64_parity(flush):
+    """The 384-electron system (FP32 coefficient values upcast to FP64) with delay rank 32,
+    flushing after every segment (0) or with block-lazy updates (4)."""
     s = fp64_twin(make_system("c1_384e"))
-    fp64_parity("c1_384e_fp64", s, 4, s.spec.delay, 2, seed=777, walker_seed=41)
+    name = "c1_384e_fp64" + ("_block_lazy" if flush == 4 else "")
+    fp64_parity(name, s, 4, s.spec.delay, 2, seed=777, walker_seed=41, flush=flush)
 
 
 def fp32_errors(system, nw, k, equil, nsweeps, seed, flush, walker_seed):
@@ -208,7 +212,7 @@ def fp32_errors(system, nw, k, equil, nsweeps, seed, flush, walker_seed):
     self_dev = np.abs(tg[..., 11] - 1.0)
     table = {
         "moves": int(r32.size), "walkers": nw, "sweeps": nsweeps, "equilibration_sweeps": equil,
-        "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32"}[flush],
+        "flush": {0: "SIMT FP32", 1: "tcgen05 TF32", 3: "tcgen05 3xTF32", 4: "block-lazy SIMT FP32"}[flush],
         "ratio_rel": stats(rat), "ratio_rel_away_from_nodes": stats(rat[away]),
         "grad_new_rel": stats(gn), "grad_now_rel": stats(gw),
         "inverse_rel_to_max": stats(inv), "laplacian_rel": stats(Le), "gradient_G_rel": stats(Ge),
@@ -221,12 +225,14 @@ def fp32_errors(system, nw, k, equil, nsweeps, seed, flush, walker_seed):
     return table
 
 
-def test_c1_fp32_against_fp64_oracle():
-    """The 384-electron production shape in FP32 (tensor-core 3xTF32 flush) against the
-    FP64 oracle: per-move ratio and gradient errors, then inverse, G, L and log|psi|."""
+@pytest.mark.parametrize("flush", [3, 4])
+def test_c1_fp32_against_fp64_oracle(flush):
+    """The 384-electron production shape in FP32 (tensor-core 3xTF32 flush after every
+    segment, or block-lazy updates) against the FP64 oracle: per-move ratio and gradient
+    errors, then inverse, G, L and log|psi|."""
     s = make_system("c1_384e")
-    t = fp32_errors(s, 8, s.spec.delay, equil=20, nsweeps=2, seed=4242, flush=3, walker_seed=51)
-    report("c1_384e", t)
+    t = fp32_errors(s, 8, s.spec.delay, equil=20, nsweeps=2, seed=4242, flush=flush, walker_seed=51)
+    report("c1_384e" + ("_block_lazy" if flush == 4 else ""), t)
     assert t["ratio_rel"]["median"] < 1e-4 and t["ratio_rel_away_from_nodes"]["p99"] < 1e-2
     assert t["grad_new_rel"]["median"] < 1e-4 and t["grad_now_rel"]["median"] < 1e-4
     assert t["inverse_rel_to_max"]["max"] < 2e-2
