@@ -23,6 +23,8 @@
 // barrier); T1 = rows U^T - E is formed by the lanes over the columns and finished by a
 // transposed warp reduction, X = T1 Binv and rows -= X V stay inside the warp.  The
 // delay lists of all pending sets are compacted at the start, one warp per set.
+#include <type_traits>
+
 #include "common.cuh"
 #include "launch.h"
 
@@ -40,16 +42,22 @@ constexpr int BU_JN   = 8;  // columns per lane: lda <= 256
 
 struct BuLayout
 {
+  int ldu;                       // row stride of Us and Vs: 32 x columns per lane, zero beyond lda
   int us, vs, t1, xs, bs, total; // offsets in elements of T
   int ac_bytes;                  // the compacted delay lists (ints), after total
 };
 
+// rows of Us and Vs: the delay rank rounded up to the 8-column chunks of T1 (rows beyond a
+// set's accepted count are zero)
+__host__ __device__ inline int bu_urows(int k) { return (k + 7) / 8 * 8; }
+
 __host__ __device__ inline BuLayout bu_layout(int lda, int k, int nsets)
 {
   BuLayout L;
+  L.ldu = (lda + 31) / 32 * 32;
   int o = 0;
-  L.us       = o, o += k * lda;
-  L.vs       = o, o += k * lda;
+  L.us       = o, o += bu_urows(k) * L.ldu;
+  L.vs       = o, o += bu_urows(k) * L.ldu;
   L.t1       = o, o += BU_MAXK * (k + 1);
   L.xs       = o, o += BU_MAXK * (k + 1);
   L.bs       = o, o += k * (k + 1);
@@ -82,10 +90,11 @@ __device__ __forceinline__ void row_async(T* dst, const T* src, int lda, int lan
 // T1 columns [c0, c0 + CW) of this warp's four rows: every lane forms its columns'
 // partial dot products of the 4 x CW values, a transposed warp reduction finishes them
 // (lane l ends with value l / (32 / (4 CW)), row-major over the 4 x CW), and the values
-// minus E land in t1w
-template<typename T, int CW>
-__device__ __forceinline__ void t1_chunk(const T (&a)[BU_RPW][BU_JN], const T* Us, int lda, int jn, int m,
-                                         int c0, const int* acrq, int r0w, T* t1w, int ldk, int lane)
+// minus E land in t1w.  Us rows beyond the set's accepted count and columns beyond lda
+// are zero, so the loads need no guard.
+template<typename T, int JN, int CW>
+__device__ __forceinline__ void t1_chunk(const T (&a)[BU_RPW][JN], const T* Us, int ldu, int m, int c0,
+                                         const int* acrq, int r0w, T* t1w, int ldk, int lane)
 {
   constexpr int NV = BU_RPW * CW; // 32 or 16 values
   T acc[NV];
@@ -93,19 +102,18 @@ __device__ __forceinline__ void t1_chunk(const T (&a)[BU_RPW][BU_JN], const T* U
   for (int v = 0; v < NV; v++)
     acc[v] = T(0);
 #pragma unroll
-  for (int i = 0; i < BU_JN; i++)
-    if (i < jn)
+  for (int i = 0; i < JN; i++)
+  {
+    const T* up = Us + c0 * ldu + lane + 32 * i;
+#pragma unroll
+    for (int cc = 0; cc < CW; cc++)
     {
-      const int j = lane + 32 * i;
+      const T u = up[cc * ldu];
 #pragma unroll
-      for (int cc = 0; cc < CW; cc++)
-      {
-        const T u = (c0 + cc < m && j < lda) ? Us[(c0 + cc) * lda + j] : T(0);
-#pragma unroll
-        for (int rr = 0; rr < BU_RPW; rr++)
-          acc[rr * CW + cc] += a[rr][i] * u;
-      }
+      for (int rr = 0; rr < BU_RPW; rr++)
+        acc[rr * CW + cc] += a[rr][i] * u;
     }
+  }
   // halve the values at distances 16, 8, ...: after the stage at distance h lane l keeps
   // the values whose index bit (h / (32 / NV)) matches its lane bit
 #pragma unroll
@@ -129,7 +137,8 @@ __device__ __forceinline__ void t1_chunk(const T (&a)[BU_RPW][BU_JN], const T* U
     t1w[rr * ldk + c] = acrq_is(acrq, c, r0w + rr) ? acc[0] - T(1) : acc[0];
 }
 
-template<typename T>
+// JN = columns per lane (lda <= 32 JN)
+template<typename T, int JN>
 __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_kernel(DevState<T> s, int spin,
                                                                                      int block0, int set_hi,
                                                                                      int complete)
@@ -143,6 +152,7 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
   if (rb <= 0 || nq <= 0)
     return;
   const BuLayout L = bu_layout(lda, K, s.nsets);
+  const int ldu    = L.ldu;
   T* sm   = reinterpret_cast<T*>(smem_raw);
   T* Us   = sm + L.us;
   T* Vs   = sm + L.vs;
@@ -173,18 +183,24 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
     if (lane == 0)
       ms[q] = __popc(bal);
   }
+  // columns [lda, ldu) of Us and Vs stay zero for the whole CTA
+  if (ldu > lda)
+    for (int e = threadIdx.x; e < 2 * bu_urows(K) * (ldu - lda); e += BU_NT)
+    {
+      const int r = e / (ldu - lda), j = lda + e % (ldu - lda);
+      (r < bu_urows(K) ? Us : Vs)[(r % bu_urows(K)) * ldu + j] = T(0);
+    }
   // this warp's rows in registers, lane l holding columns l + 32 i (columns beyond n are zero)
-  const int jn = (lda + 31) / 32;
-  T a[BU_RPW][BU_JN];
+  T a[BU_RPW][JN];
 #pragma unroll
   for (int rr = 0; rr < BU_RPW; rr++)
   {
     const int r = BU_RPW * wid + rr;
 #pragma unroll
-    for (int i = 0; i < BU_JN; i++)
+    for (int i = 0; i < JN; i++)
     {
       const int j = lane + 32 * i;
-      a[rr][i]    = (i < jn && r < rb && j < n) ? A[(size_t)r * lda + j] : T(0);
+      a[rr][i]    = (r < rb && j < n) ? A[(size_t)r * lda + j] : T(0);
     }
   }
   __syncthreads();
@@ -205,10 +221,13 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
     const int* acq  = ac + q * K;
     for (int c = wid; c < m; c += BU_NW)
     {
-      row_async(Us + c * lda, U + (size_t)acq[c] * lda, lda, lane);
-      row_async(Vs + c * lda, V + (size_t)acq[c] * lda, lda, lane);
+      row_async(Us + c * ldu, U + (size_t)acq[c] * lda, lda, lane);
+      row_async(Vs + c * ldu, V + (size_t)acq[c] * lda, lda, lane);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
+    // U rows [m, 8-column boundary) read as zero by the last chunk of T1
+    for (int e = threadIdx.x; e < (bu_urows(m) - m) * lda; e += BU_NT)
+      Us[(m + e / lda) * ldu + e % lda] = T(0);
     for (int e = threadIdx.x; e < m * m; e += BU_NT)
     {
       const int c = e / m, c2 = e % m;
@@ -221,12 +240,12 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
     for (int c0 = 0; c0 < m;)
       if (m - c0 > 4)
       {
-        t1_chunk<T, 8>(a, Us, lda, jn, m, c0, acr + q * K, r0 + BU_RPW * wid, t1w, ldk, lane);
+        t1_chunk<T, JN, 8>(a, Us, ldu, m, c0, acr + q * K, r0 + BU_RPW * wid, t1w, ldk, lane);
         c0 += 8;
       }
       else
       {
-        t1_chunk<T, 4>(a, Us, lda, jn, m, c0, acr + q * K, r0 + BU_RPW * wid, t1w, ldk, lane);
+        t1_chunk<T, JN, 4>(a, Us, ldu, m, c0, acr + q * K, r0 + BU_RPW * wid, t1w, ldk, lane);
         c0 += 4;
       }
     __syncwarp();
@@ -240,23 +259,22 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
       xw[rr * ldk + c2] = x;
     }
     __syncwarp();
-    // rows -= X V (the padding columns of V may hold anything: those of the rows are never stored)
+    // rows -= X V (columns beyond n of the rows are never stored)
     for (int c = 0; c < m; c++)
     {
       T x[BU_RPW];
 #pragma unroll
       for (int rr = 0; rr < BU_RPW; rr++)
         x[rr] = xw[rr * ldk + c];
+      const T* vp = Vs + c * ldu + lane;
 #pragma unroll
-      for (int i = 0; i < BU_JN; i++)
-        if (i < jn)
-        {
-          const int j = lane + 32 * i;
-          const T v   = j < lda ? Vs[c * lda + j] : T(0);
+      for (int i = 0; i < JN; i++)
+      {
+        const T v = vp[32 * i];
 #pragma unroll
-          for (int rr = 0; rr < BU_RPW; rr++)
-            a[rr][i] -= x[rr] * v;
-        }
+        for (int rr = 0; rr < BU_RPW; rr++)
+          a[rr][i] -= x[rr] * v;
+      }
     }
     // the next set's rows overwrite Us, Vs and bs
     __syncthreads();
@@ -268,12 +286,30 @@ __global__ void __launch_bounds__(BU_NT, sizeof(T) == 4 ? 2 : 1) block_update_ke
   {
     const int r = BU_RPW * wid + rr;
 #pragma unroll
-    for (int i = 0; i < BU_JN; i++)
+    for (int i = 0; i < JN; i++)
     {
       const int j = lane + 32 * i;
-      if (i < jn && r < rb && j < n)
+      if (r < rb && j < n)
         A[(size_t)r * lda + j] = a[rr][i];
     }
+  }
+}
+
+// the kernel instantiation for lda (columns per lane 1..8)
+template<typename T, typename F>
+static cudaError_t with_columns(int lda, F&& f)
+{
+  switch ((lda + 31) / 32)
+  {
+  case 1: return f(std::integral_constant<int, 1>{});
+  case 2: return f(std::integral_constant<int, 2>{});
+  case 3: return f(std::integral_constant<int, 3>{});
+  case 4: return f(std::integral_constant<int, 4>{});
+  case 5: return f(std::integral_constant<int, 5>{});
+  case 6: return f(std::integral_constant<int, 6>{});
+  case 7: return f(std::integral_constant<int, 7>{});
+  case 8: return f(std::integral_constant<int, 8>{});
+  default: return cudaErrorInvalidValue;
   }
 }
 
@@ -287,7 +323,13 @@ bool block_update_supported(const DevState<T>& s)
 template<typename T>
 cudaError_t setup_block_update()
 {
-  return cudaFuncSetAttribute(block_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaError_t e = cudaSuccess;
+  for (int jn = 1; jn <= BU_JN && e == cudaSuccess; jn++)
+    e = with_columns<T>(32 * jn, [](auto c) {
+      return cudaFuncSetAttribute(block_update_kernel<T, decltype(c)::value>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+  return e;
 }
 
 template<typename T>
@@ -297,9 +339,11 @@ cudaError_t launch_block_update(const DevState<T>& s, int spin, int block, int n
   if (!block_update_supported(s) || nblocks < 1)
     return cudaErrorInvalidValue;
   const dim3 grid(s.nw, nblocks);
-  block_update_kernel<T>
-      <<<grid, BU_NT, bu_smem<T>(s.lda, s.k, s.nsets), st>>>(s, spin, block, set_hi, complete ? 1 : 0);
-  return cudaGetLastError();
+  return with_columns<T>(s.lda, [&](auto c) {
+    block_update_kernel<T, decltype(c)::value>
+        <<<grid, BU_NT, bu_smem<T>(s.lda, s.k, s.nsets), st>>>(s, spin, block, set_hi, complete ? 1 : 0);
+    return cudaGetLastError();
+  });
 }
 
 template bool block_update_supported<float>(const DevState<float>&);
