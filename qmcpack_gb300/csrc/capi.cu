@@ -2380,11 +2380,23 @@ struct Group final : qmcg_group_s
       {
         Crowd<T>* x = cs[st.crowd[a]];
         if (x->k > 1)
+        {
+          const int sp = st.i0[a] >= x->sys->nup ? 1 : 0, first = sp ? x->sys->nup : 0;
+          const int blk = (st.i0[a] - first) / x->k;
+          if (x->lazy_updates())
           {
-            const int sp = st.i0[a] >= x->sys->nup ? 1 : 0, first = sp ? x->sys->nup : 0;
-            const int set = x->s.nsets > 1 ? (st.i0[a] - first) / x->k : 0;
-            CUDA_TRY(x->launch_flush_choice(sp, st.i1[a] - st.i0[a], set, stream));
+            // block-lazy: the crowd's next row block of this spin group receives the sets so
+            // far before its segment (a later stage), or the spin group is completed
+            const int nspin = sp ? x->sys->ne - x->sys->nup : x->sys->nup;
+            const int nseg  = (nspin + x->k - 1) / x->k;
+            if (blk + 1 < nseg)
+              CUDA_TRY(launch_block_update<T>(x->s, sp, blk + 1, 1, blk + 1, false, stream));
+            else
+              CUDA_TRY(launch_block_update<T>(x->s, sp, 0, nseg, nseg, true, stream));
           }
+          else
+            CUDA_TRY(x->launch_flush_choice(sp, st.i1[a] - st.i0[a], x->s.nsets > 1 ? blk : 0, stream));
+        }
       }
     }
     for (auto* x : cs)

@@ -1,5 +1,7 @@
 """Uneven crowds swept together (one persistent launch per stage): every crowd's
-result is bit-identical to sweeping it alone with its group seed."""
+result is bit-identical to sweeping it alone with its group seed, with the flush after
+every segment (kind 0) and with the block-lazy updates (kind 4: the crowds whose segment
+rows are staged sequence them per stage of the group)."""
 import numpy as np
 import pytest
 
@@ -15,8 +17,8 @@ def _systems(prec):
     return [a, b, c]
 
 
-@pytest.mark.parametrize("prec", [8, 4])
-def test_group_matches_separate_crowds(prec):
+@pytest.mark.parametrize("prec,flush", [(8, 0), (4, 0), (8, 4), (4, 4)])
+def test_group_matches_separate_crowds(prec, flush):
     from qmcpack_gb300.crowd import Crowd, DeviceSystem, Group, group_seed
     systems = _systems(prec)
     dss = [DeviceSystem(s) for s in systems]
@@ -34,10 +36,12 @@ def test_group_matches_separate_crowds(prec):
     together = crowds()
     grp = Group(together)
     print("group", grp.info())
-    stats = grp.sweeps(2, 0.3, 1234, flush=0)
+    if flush == 4:
+        assert any(g.sweep_info(4)["block_lazy"] for g in together)
+    stats = grp.sweeps(2, 0.3, 1234, flush=flush)
     alone = crowds()
     for i, g in enumerate(alone):
-        a, r, _ = g.vmc_sweeps(2, 0.3, group_seed(1234, i), rng_mode=1, flush=0)
+        a, r, _ = g.vmc_sweeps(2, 0.3, group_seed(1234, i), rng_mode=1, flush=flush)
         assert (a, r) == stats[i][:2]
         np.testing.assert_array_equal(g.positions(), together[i].positions())
         np.testing.assert_array_equal(g.get_log()[0], together[i].get_log()[0])
