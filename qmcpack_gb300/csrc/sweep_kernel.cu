@@ -313,18 +313,22 @@ __device__ __forceinline__ void sweep_shared_init(SweepShared<T, LEARNED>& sh)
   __syncthreads();
 }
 
-// The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.  STAGED
+// The segment [i0, i1) of walker w by one CTA: the body of the resident sweep.  FORM 1
 // compiles the delayed-update form with the segment's inverse rows in shared memory and
 // nothing else (the rank-1 and unstaged branches drop out of the loop body, which the
-// instruction cache then holds better); the generic form decides both at run time.
-template<typename T, int NT, bool LEARNED, bool STAGED>
+// instruction cache then holds better), FORM 2 the same for plain VMC sweeps (no DMC
+// sign rule or sums, no move records); FORM 0, the generic form, decides all at run time.
+template<typename T, int NT, bool LEARNED, int FORM>
 __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i1, int w, unsigned char* smem_raw,
                                              SweepShared<T, LEARNED>& sh, unsigned long long& n_acc,
                                              unsigned long long& n_rej)
 {
+  constexpr bool STAGED = FORM >= 1, PLAIN = FORM == 2;
   const int lda = s.lda, n = s.norb, K = s.k;
   const bool delayed   = STAGED || K > 1;
   const bool seg_smem  = STAGED || (K > 1 && s.seg_smem != 0);
+  const bool dmc       = !PLAIN && s.dmc != 0;
+  double* const trace  = PLAIN ? nullptr : s.trace;
   const SweepLayout Ly = sweep_layout<T>(lda, s.ne_pad, K, seg_smem, LEARNED, sweep_ncoef(s));
   T* sm     = reinterpret_cast<T*>(smem_raw);
   T* pre    = sm + Ly.pre;    // 2 x npre x lda prefetch buffers
@@ -604,15 +608,15 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
             else
               u -= floor(u);
             sh.ru[d] = u;
-            if (s.trace)
-              s.trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_GRAD_NOW + d] = static_cast<double>(gs);
+            if (trace)
+              trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_GRAD_NOW + d] = static_cast<double>(gs);
           }
           if (lane == 0)
           {
             if (!(fabs(g[3] - T(1)) <= HealthTol<T>::v))
               atomicOr(s.status + w, spin ? ST_ILLCOND_DN : ST_ILLCOND_UP);
-            if (s.trace)
-              s.trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_SELF] = static_cast<double>(g[3]);
+            if (trace)
+              trace[((size_t)iat * s.nw + w) * TRACE_FIELDS + TR_SELF] = static_cast<double>(g[3]);
             sh.loggf = s.use_drift ? -(T(0.5) / tau) * dsq : T(0);
           }
         }
@@ -766,11 +770,11 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         int a = 0;
         // DMC: a move that changes the sign of psi is rejected (fixed node,
         // DMCBatched.cpp:203-210 with SFNBranch::phaseChanged for real ratios)
-        if (p >= Eps<T>::v && (!s.dmc || detr > T(0)))
+        if (p >= Eps<T>::v && (!dmc || detr > T(0)))
         {
           a = sh.runif[jj] < p * exp(log_gb - sh.loggf) ? 1 : 0;
         }
-        if (s.dmc)
+        if (dmc)
         {
           const double r2 = static_cast<double>(tau) *
               static_cast<double>(sh.rgauss[jj][0] * sh.rgauss[jj][0] + sh.rgauss[jj][1] * sh.rgauss[jj][1] +
@@ -791,9 +795,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         else
           n_rej++;
         sh.acc = a;
-        if (s.trace)
+        if (trace)
         {
-          double* tr = s.trace + ((size_t)iat * s.nw + w) * TRACE_FIELDS;
+          double* tr = trace + ((size_t)iat * s.nw + w) * TRACE_FIELDS;
           for (int d = 0; d < 3; d++)
           {
             tr[TR_POS + d]      = sh.pos[d];
@@ -1015,7 +1019,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       s.log_abs[slot] += log(det_mant) + det_exp * 0.69314718055994530942;
       if (det_neg)
         s.sign[slot] = -s.sign[slot];
-      if (s.dmc)
+      if (dmc)
       {
         s.rr[2 * w] += rr_prop;
         s.rr[2 * w + 1] += rr_acc;
@@ -1036,7 +1040,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   }
 }
 
-template<typename T, int NT, int MINB, bool LEARNED, bool STAGED>
+template<typename T, int NT, int MINB, bool LEARNED, int FORM>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, int i1)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1044,7 +1048,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(DevState<T> s, int i0, 
   sweep_shared_init(sh);
   unsigned long long n_acc = 0, n_rej = 0;
   for (int w = blockIdx.x; w < s.nw; w += gridDim.x)
-    sweep_walker<T, NT, LEARNED, STAGED>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
+    sweep_walker<T, NT, LEARNED, FORM>(s, i0, i1, w, smem_raw, sh, n_acc, n_rej);
   if (threadIdx.x == 0)
   {
     atomicAdd(s.counters + 0, n_acc);
@@ -1099,7 +1103,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_multi_kernel(const DevState<T>
       __syncthreads();
       cur = c;
     }
-    sweep_walker<T, NT, false, false>(ds, st.i0[a], st.i1[a], item - st.begin[a], smem_raw, sh, n_acc, n_rej);
+    sweep_walker<T, NT, false, 0>(ds, st.i0[a], st.i1[a], item - st.begin[a], smem_raw, sh, n_acc, n_rej);
     __syncthreads();
   }
   if (cur >= 0 && threadIdx.x == 0)
@@ -1170,33 +1174,41 @@ static cudaError_t with_threads(int nt, F&& f)
   return cudaErrorInvalidValue;
 }
 
-// the two forms of the kernel: delayed updates with the segment rows staged, or generic
-template<typename F>
-static cudaError_t with_staged(bool staged, F&& f)
+// the forms of the kernel: 0 generic, 1 delayed updates with the segment rows staged,
+// 2 the same for plain VMC sweeps (no DMC, no move records; FP32 only)
+template<typename T, typename F>
+static cudaError_t with_form(int form, F&& f)
 {
-  return staged ? f(std::true_type{}) : f(std::false_type{});
+  if constexpr (sizeof(T) == 4)
+    if (form == 2)
+      return f(std::integral_constant<int, 2>{});
+  if (form >= 1)
+    return f(std::integral_constant<int, 1>{});
+  return f(std::integral_constant<int, 0>{});
 }
 
 template<typename T>
-static bool sweep_staged(const DevState<T>& s)
+static int sweep_form(const DevState<T>& s)
 {
-  return s.k > 1 && s.seg_smem != 0;
+  if (s.k <= 1 || s.seg_smem == 0)
+    return 0;
+  return sizeof(T) == 4 && !s.dmc && !s.trace ? 2 : 1;
 }
 
 template<typename T>
 cudaError_t setup_sweep_kernel()
 {
   cudaError_t e = cudaSuccess;
-  for (bool staged : {false, true})
+  for (int form : {0, 1, 2})
   {
     if (e == cudaSuccess)
-      e = with_staged(staged, [](auto g) {
+      e = with_form<T>(form, [](auto g) {
         return cudaFuncSetAttribute(sweep_kernel<T, SweepCfg<T>::NT, SweepCfg<T>::MINB, true, decltype(g)::value>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
       });
     for (int nt : {128, 256, 512})
       if (e == cudaSuccess && sweep_threads_ok(nt, sizeof(T)))
-        e = with_staged(staged, [&](auto g) {
+        e = with_form<T>(form, [&](auto g) {
           return with_threads<T>(nt, [](auto c) {
             constexpr int NT = decltype(c)::value;
             return cudaFuncSetAttribute(sweep_kernel<T, NT, SweepMinb<T, NT>::v, false, decltype(g)::value>,
@@ -1228,12 +1240,12 @@ cudaError_t launch_sweep_segment(const DevState<T>& s, int grid, int i0, int i1,
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
     if (!s.mlp_simt || !s.mlp_params)
       return cudaErrorInvalidValue;
-    return with_staged(sweep_staged(s), [&](auto g) {
+    return with_form<T>(sweep_form(s), [&](auto g) {
       sweep_kernel<T, NT, MINB, true, decltype(g)::value><<<grid, NT, sweep_smem_bytes(s, true), st>>>(s, i0, i1);
       return cudaGetLastError();
     });
   }
-  return with_staged(sweep_staged(s), [&](auto g) {
+  return with_form<T>(sweep_form(s), [&](auto g) {
     return with_threads<T>(nt, [&](auto c) {
       constexpr int NT = decltype(c)::value;
       sweep_kernel<T, NT, SweepMinb<T, NT>::v, false, decltype(g)::value>
@@ -1256,13 +1268,13 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
   if (learned)
   {
     constexpr int NT = SweepCfg<T>::NT, MINB = SweepCfg<T>::MINB;
-    e = with_staged(sweep_staged(s), [&](auto g) {
+    e = with_form<T>(sweep_form(s), [&](auto g) {
       return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per_sm, sweep_kernel<T, NT, MINB, true, decltype(g)::value>, NT, sweep_smem_bytes(s, true));
     });
   }
   else
-    e = with_staged(sweep_staged(s), [&](auto g) {
+    e = with_form<T>(sweep_form(s), [&](auto g) {
       return with_threads<T>(nt, [&](auto c) {
         constexpr int NT = decltype(c)::value;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(

@@ -249,3 +249,27 @@ def test_c2_fp32_against_fp64_oracle():
     assert t["grad_new_rel"]["median"] < 1e-3
     assert t["inverse_rel_to_max"]["max"] < 5e-2
     assert t["gradient_G_rel"]["median"] < 1e-2 and t["laplacian_rel"]["median"] < 1e-2
+
+
+@pytest.mark.parametrize("flush", [3, 4])
+def test_plain_sweeps_match_traced_sweeps(flush):
+    """The benchmarked FP32 sweep (the kernel form compiled without move records or DMC
+    rules) gives bit-identical results to the traced sweep the oracle replays above."""
+    Crowd, DeviceSystem = _gpu()
+    s = make_system("c1_384e")
+    ds = DeviceSystem(s)
+    R = make_walkers(s, 8, seed=71)
+    out = []
+    for traced in (False, True):
+        g = Crowd(ds, 8, s.spec.delay)
+        g.load_walkers(R)
+        g.mw_evaluateLog()
+        if traced:
+            a, r, _ = g.vmc_sweeps_trace(2, TAU, 505, flush=flush)
+        else:
+            a, r, _ = g.vmc_sweeps(2, TAU, 505, rng_mode=1, flush=flush)
+        out.append((a, r, g.positions(), g.get_log()[0], g.inverse(0), g.inverse(1), *g.jastrow_state()))
+    (a0, r0, *x0), (a1, r1, *x1) = out
+    assert (a0, r0) == (a1, r1)
+    for u, v in zip(x0, x1):
+        np.testing.assert_array_equal(u, v)
