@@ -437,6 +437,10 @@ struct qmcg_crowd_s
   virtual ~qmcg_crowd_s() = default;
   qmcg_system sys        = nullptr;
   cudaStream_t stream    = nullptr;
+  // the completing pass of the up spin's block-lazy updates runs here, at a lower priority,
+  // beside the down spin's segments (it touches only the up spin's inverse and sets)
+  cudaStream_t side      = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int nw = 0, k = 1;
   int dc[2]              = {0, 0};
   int invrow_iat         = -1;
@@ -640,6 +644,12 @@ struct Crowd final : qmcg_crowd_s
     if (dm.graph)
       cudaGraphExecDestroy(dm.graph);
     vp.release();
+    if (ev_fork)
+      cudaEventDestroy(ev_fork);
+    if (ev_join)
+      cudaEventDestroy(ev_join);
+    if (side)
+      cudaStreamDestroy(side);
     if (stream)
       cudaStreamDestroy(stream);
   }
@@ -653,7 +663,12 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(setup_recompute_kernels<T>());
     CUDA_TRY(setup_sweep_kernel<T>());
     CUDA_TRY(setup_flush_fused<T>());
-    CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    int prio_low = 0, prio_high = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    CUDA_TRY(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, prio_high));
+    CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio_low));
+    CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     DevState<T>& d = s;
     d.nw        = nw;
     d.ne        = sys->ne;
@@ -1084,7 +1099,7 @@ struct Crowd final : qmcg_crowd_s
   // its row block and the spin group followed by the completing pass; `seg(i0, i1)` and
   // `upd(launch)` enqueue a segment and an update launch
   template<typename Seg, typename Upd>
-  int enqueue_spin_group(int g, Seg&& seg, Upd&& upd)
+  int enqueue_spin_group(int g, Seg&& seg, Upd&& upd, bool defer_complete = false)
   {
     const int first = g ? sys->nup : 0, last = g ? sys->ne : sys->nup;
     const bool lazy = lazy_updates();
@@ -1106,9 +1121,24 @@ struct Crowd final : qmcg_crowd_s
       if (rc)
         return rc;
     }
-    if (lazy)
+    if (lazy && !defer_complete)
       return upd([=] { return launch_block_update<T>(s, g, 0, nseg, nseg, true, stream); });
     return QMCG_OK;
+  }
+
+  // the completing pass of spin g on the side stream, after everything enqueued so far
+  cudaError_t fork_complete(int g)
+  {
+    const int nspin = g ? sys->ne - sys->nup : sys->nup;
+    const int nseg  = (nspin + k - 1) / k;
+    cudaError_t e   = cudaEventRecord(ev_fork, stream);
+    if (e == cudaSuccess)
+      e = cudaStreamWaitEvent(side, ev_fork, 0);
+    if (e == cudaSuccess)
+      e = launch_block_update<T>(s, g, 0, nseg, nseg, true, side);
+    if (e == cudaSuccess)
+      e = cudaEventRecord(ev_join, side);
+    return e;
   }
 
   // the segments [i0, i1) of one sweep on the walker-resident path, in launch order
@@ -1135,6 +1165,8 @@ struct Crowd final : qmcg_crowd_s
     const int grid = learned ? sweep_grid_learned : sweep_grid_size;
     if (k > 1)
     {
+      // block-lazy: the up spin's completing pass overlaps the down spin's segments
+      const bool fork = lazy_updates();
       for (int g = 0; g < 2; g++)
       {
         const int rc = enqueue_spin_group(
@@ -1146,10 +1178,15 @@ struct Crowd final : qmcg_crowd_s
             [&](auto launch) -> int {
               CUDA_TRY(launch());
               return QMCG_OK;
-            });
+            },
+            fork && g == 0);
         if (rc)
           return rc;
+        if (fork && g == 0)
+          CUDA_TRY(fork_complete(0));
       }
+      if (fork)
+        CUDA_TRY(cudaStreamWaitEvent(stream, ev_join, 0));
     }
     else
     {
@@ -1186,7 +1223,7 @@ struct Crowd final : qmcg_crowd_s
       return rc;
     if (e != cudaSuccess)
       return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&graph, g, 0);
+    e = cudaGraphInstantiate(&graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess)
       return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
@@ -1337,7 +1374,7 @@ struct Crowd final : qmcg_crowd_s
           return rc;
         if (e != cudaSuccess)
           return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-        const cudaError_t ei = cudaGraphInstantiate(&dm.graph, g, 0);
+        const cudaError_t ei = cudaGraphInstantiate(&dm.graph, g, cudaGraphInstantiateFlagUseNodePriority);
         cudaGraphDestroy(g);
         if (ei != cudaSuccess)
           return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ei));
@@ -1861,7 +1898,7 @@ struct Crowd final : qmcg_crowd_s
         return rc;
       if (e != cudaSuccess)
         return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-      e = cudaGraphInstantiate(&ln.graph, g, 0);
+      e = cudaGraphInstantiate(&ln.graph, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (e != cudaSuccess)
         return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
@@ -2358,7 +2395,7 @@ struct Group final : qmcg_group_s
       return rc;
     if (e != cudaSuccess)
       return fail(QMCG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&graph, g, 0);
+    e = cudaGraphInstantiate(&graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess)
       return fail(QMCG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
