@@ -53,6 +53,9 @@ struct SweepLayout
 {
   int npre; // rows per prefetch buffer: dgrad xyz, values (+ the inverse row when the segment rows are not staged)
   int pre, invrow, phi, Rs, J2s, Bs, pv, tv, yv, red, tri, seg, ml, coef, total;
+  // delayed updates with unstaged rows: the orbital values at the proposed position are
+  // written over the current electron's prefetch buffer (five rows, spent by then)
+  int phi_in_pre;
 };
 
 template<typename T>
@@ -63,10 +66,11 @@ __host__ __device__ inline SweepLayout sweep_layout(int lda, int ne_pad, int K, 
   auto up         = [](int x) { return (x + a - 1) / a * a; };
   SweepLayout L;
   int o    = 0;
-  L.npre   = seg_smem ? 4 : 5;
-  L.pre    = o, o += up(2 * L.npre * lda);
-  L.invrow = o, o += up(lda);
-  L.phi    = o, o += up(5 * lda);
+  L.npre       = seg_smem ? 4 : 5;
+  L.phi_in_pre = !seg_smem && K > 1 && !learned;
+  L.pre        = o, o += up(2 * L.npre * lda);
+  L.invrow     = o, o += up(lda);
+  L.phi        = o, o += L.phi_in_pre ? 0 : up(5 * lda);
   L.Rs     = o, o += up(3 * ne_pad);
   L.J2s    = o, o += up(5 * ne_pad);
   L.Bs     = o, o += up(K * K);
@@ -333,7 +337,7 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
   T* sm     = reinterpret_cast<T*>(smem_raw);
   T* pre    = sm + Ly.pre;    // 2 x npre x lda prefetch buffers
   T* invrow = sm + Ly.invrow; // lda
-  T* phi    = sm + Ly.phi;    // 5 x lda
+  T* const phi_own = sm + Ly.phi; // 5 x lda (unless phi_in_pre)
   T* Rs     = sm + Ly.Rs;     // 3 x ne_pad
   T* J2s    = sm + Ly.J2s;    // 5 x ne_pad
   T* Bs     = sm + Ly.Bs;     // K x K
@@ -433,6 +437,10 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
       const T* dg   = seg_smem ? pb : pb + lda;
       const T* pv0  = dg + 3 * lda;
       T* pnext      = pre + ((iat + 1 - i0) & 1) * Ly.npre * lda;
+      T* const phi  = Ly.phi_in_pre ? pb : phi_own;
+      // with phi over the prefetch buffer the inverse row (V of this slot) is stored before
+      // the evaluation overwrites it
+      T* const vrow = s.V + (dset * K + dc) * lda;
       // the random numbers of the next 32 electrons, one electron per thread (counter-based:
       // the same values the single-electron calls would draw)
       const int jj = (iat - i0) & 31;
@@ -498,6 +506,8 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
             a[0] += V[(size_t)c * lda + j] * tv[c];
           const T x = arow[j] + ((a[0] + a[1]) + (a[2] + a[3]));
           invrow[j] = x;
+          if (Ly.phi_in_pre)
+            vrow[j] = arow[j];
           g[0] += x * dg[j];
           g[1] += x * dg[lda + j];
           g[2] += x * dg[2 * lda + j];
@@ -516,7 +526,14 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
           g[1] += x * dg[lda + j];
           g[2] += x * dg[2 * lda + j];
           g[3] += x * pv0[j];
+          if (Ly.phi_in_pre)
+          {
+            invrow[j] = x;
+            vrow[j]   = x;
+          }
         }
+        if (Ly.phi_in_pre)
+          inv = invrow;
         // rank-1 updates: the next rows are fetched after this electron's update
       }
       // ------------------------------------------------ gradient, health check, proposal
@@ -860,8 +877,9 @@ __device__ __forceinline__ void sweep_walker(const DevState<T>& s, int i0, int i
         T* U       = s.U + dset * K * lda;
         T* V       = s.V + dset * K * lda;
         int* dlist = s.delay_list + dset * K;
-        for (int j = threadIdx.x; j < n; j += NT)
-          V[(size_t)dc * lda + j] = arow[j];
+        if (!Ly.phi_in_pre)
+          for (int j = threadIdx.x; j < n; j += NT)
+            V[(size_t)dc * lda + j] = arow[j];
         const int m = i1 - i0; // slots of this segment
         if (accd)
         {
@@ -1294,7 +1312,7 @@ cudaError_t sweep_grid(const DevState<T>& s, int* grid, bool learned, int nt)
 template<typename T>
 int sweep_default_threads(const DevState<T>& s)
 {
-  const size_t sm = sweep_smem_reference<T>(s.lda, s.ne_pad, s.k);
+  const size_t sm = sweep_smem_bytes<T>(s, false);
   if (sm > 114 * 1024)
     return sizeof(T) == 4 ? 512 : 256;
   if (sm > 76 * 1024)
