@@ -186,9 +186,11 @@ def test_training_lowers_the_objective():
     assert np.isfinite(obj1) and obj1 < obj0
 
 
-def test_resident_zero_output_layer_is_drift_diffusion():
+@pytest.mark.parametrize("flush", [0, 4])
+def test_resident_zero_output_layer_is_drift_diffusion(flush):
     """Walker-resident inference with a zero output layer reproduces the resident
-    drift-diffusion sweep (FP64)."""
+    drift-diffusion sweep (FP64), with the flush after every segment and with the
+    block-lazy updates."""
     Crowd, DeviceSystem = _gpu()
     s = _small(nw=8)
     ds = DeviceSystem(s)
@@ -200,9 +202,9 @@ def test_resident_zero_output_layer_is_drift_diffusion():
         g.mw_evaluateLog()
         if learned:
             g.proposal_init(seed=4)
-            a, r, _, _ = g.vmc_sweeps_learned(2, 0.3, 23)
+            a, r, _, _ = g.vmc_sweeps_learned(2, 0.3, 23, flush=flush)
         else:
-            a, r, _ = g.vmc_sweeps(2, 0.3, 23, rng_mode=1)
+            a, r, _ = g.vmc_sweeps(2, 0.3, 23, rng_mode=1, flush=flush)
         out.append((a, r, g.positions()))
     assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
     np.testing.assert_allclose(out[0][2], out[1][2], rtol=0, atol=1e-10)
