@@ -16,8 +16,10 @@
 // (eps = 1e-7 for the FP32 move loop, 1e-12 for FP64).  Sums are FP64; the terms are
 // evaluated in the move-loop precision T.  The structure factor uses per-electron
 // phase tables exp(i n 2 pi x_d / L_d), n = 0..n_max, built in shared memory for a
-// chunk of electrons; each thread owns a set of G vectors (sorted by (n1, n2, n3) so a
-// warp's table reads are mostly broadcasts) and accumulates rho_e(G) in registers.
+// chunk of electrons, and from them the products exp(i 2 pi (n1 x/Lx + n2 y/Ly)) for
+// every (n1 >= 0, n2) of the half space, so a (G, electron) term is two table reads and
+// one complex multiply-add; each thread owns a set of G vectors (sorted by (n1, n2, n3)
+// so a warp's table reads are mostly broadcasts) and accumulates rho_e(G) in registers.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -29,17 +31,52 @@ namespace qmcg
 {
 
 constexpr int LE_NT  = 256; // threads per walker
-constexpr int LE_CH  = 32;  // electrons per phase-table chunk
+constexpr int LE_CH  = 32;  // electrons per phase-table chunk at most
 constexpr int LE_GPT = 12;  // G vectors per thread per pass
+constexpr size_t LE_SMEM_MAX = 200 * 1024;
+
+// a complex value from two consecutive elements of shared memory (8- or 16-byte aligned)
+template<typename T>
+struct Cplx
+{
+  T x, y;
+};
+__device__ __forceinline__ Cplx<float> ld_cplx(const float* p)
+{
+  const float2 v = *reinterpret_cast<const float2*>(p);
+  return {v.x, v.y};
+}
+__device__ __forceinline__ Cplx<double> ld_cplx(const double* p)
+{
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  return {v.x, v.y};
+}
 
 __device__ __forceinline__ float t_erfc(float x) { return erfcf(x); }
 __device__ __forceinline__ double t_erfc(double x) { return erfc(x); }
 __device__ __forceinline__ void t_sincospi(float x, float* s, float* c) { sincospif(x, s, c); }
 __device__ __forceinline__ void t_sincospi(double x, double* s, double* c) { sincospi(x, s, c); }
 
+// shared memory of the local-energy kernel for `ch` electrons per table chunk: positions
+// (padded to 4 elements), the 1-D phase tables and the (n1, n2) products of the chunk
+static size_t le_smem_ch(int ne, int nmax, int tsize, int ch)
+{
+  const size_t nm1 = (size_t)nmax + 1, nb = 2 * (size_t)nmax + 1;
+  return (size_t)tsize * ((3 * (size_t)ne + 3) / 4 * 4 + (size_t)ch * (3 * nm1 * 2 + nm1 * nb * 2));
+}
+
+// electrons per table chunk: as many as fit (LE_CH at most)
+static int le_chunk(int ne, int nmax, int tsize)
+{
+  int ch = LE_CH;
+  while (ch > 1 && le_smem_ch(ne, nmax, tsize, ch) > LE_SMEM_MAX)
+    ch--;
+  return ch;
+}
+
 size_t local_energy_smem(int ne, int nmax, int tsize)
 {
-  return (size_t)tsize * (3 * (size_t)ne + (size_t)LE_CH * 3 * (nmax + 1) * 2);
+  return le_smem_ch(ne, nmax, tsize, le_chunk(ne, nmax, tsize));
 }
 
 // a thread's sum of many terms: compensated (Kahan) in FP32, which keeps the sum to
@@ -66,14 +103,15 @@ struct CompSum<float>
 };
 
 template<typename T>
-__global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, EwaldDev<T> ew, double* out)
+__global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, EwaldDev<T> ew, double* out, int ch)
 {
   extern __shared__ __align__(16) unsigned char le_smem[];
   __shared__ double red[3 * 32];
   const int iw = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ne = s.ne, N = s.norb, lda = s.lda, nm1 = ew.nmax + 1;
-  T* pos = reinterpret_cast<T*>(le_smem); // [3][ne], wrapped into the cell
-  T* tab = pos + 3 * ne;                   // [LE_CH][3][nm1] complex
+  const int ne = s.ne, N = s.norb, lda = s.lda, nm1 = ew.nmax + 1, nb = 2 * ew.nmax + 1;
+  T* pos = reinterpret_cast<T*>(le_smem);   // [3][ne], wrapped into the cell
+  T* tab = pos + (3 * ne + 3) / 4 * 4;      // [ch][3][nm1] complex
+  T* t12 = tab + (size_t)ch * 3 * nm1 * 2;  // [ch][nm1][nb] complex: e1(n1) e2(n2), n2 = -nmax..nmax
   const T Lc[3]   = {T(s.L[0]), T(s.L[1]), T(s.L[2])};
   const T Li[3]   = {T(s.G[0]), T(s.G[1]), T(s.G[2])};
 
@@ -89,7 +127,8 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
 
   double ke = 0, vk = 0;
   CompSum<T> vr; // the ~300 pair terms of a thread
-  // ---------------- kinetic energy: a warp per electron
+  // ---------------- kinetic energy: a warp per electron, lanes over orbital pairs (lda is
+  // even), the four sums of a row in flight together
   for (int i = warp; i < ne; i += LE_NT / 32)
   {
     const int sp     = i < s.nup ? 0 : 1;
@@ -97,38 +136,51 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
     const T* a       = s.Ainv + rb * lda;
     const T* g       = s.dgrad + rb * 3 * lda;
     const T* l       = s.dlap + rb * lda;
-    T gx = 0, gy = 0, gz = 0, lp = 0;
-    for (int o = lane; o < N; o += 32)
-    {
-      const T av = a[o];
-      gx += av * g[o];
-      gy += av * g[lda + o];
-      gz += av * g[2 * lda + o];
-      lp += av * l[o];
-    }
-    // lane sums in the move precision (FP64 arithmetic is slow on this GPU), the
-    // per-electron combination in FP64
-    double G[3] = {static_cast<double>(warp_sum(gx)), static_cast<double>(warp_sum(gy)),
-                   static_cast<double>(warp_sum(gz))};
-    double L    = static_cast<double>(warp_sum(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+    // the Jastrow terms of this electron (gradient xyz, Laplacian), read by lane 0 ahead
+    // of the sums
+    T j2v[4] = {T(0), T(0), T(0), T(0)}, j1v[4] = {T(0), T(0), T(0), T(0)};
     if (lane == 0)
     {
       if (s.has_j2)
       {
         const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + i;
 #pragma unroll
-        for (int d = 0; d < 3; d++)
-          G[d] += static_cast<double>(j2[(1 + d) * s.ne_pad]);
-        L += static_cast<double>(j2[4 * s.ne_pad]);
+        for (int d = 0; d < 4; d++)
+          j2v[d] = j2[(1 + d) * s.ne_pad];
       }
       if (s.has_j1)
       {
         const T* j1 = s.J1 + (size_t)iw * 5 * s.ne_pad + i;
 #pragma unroll
-        for (int d = 0; d < 3; d++)
-          G[d] += static_cast<double>(j1[(1 + d) * s.ne_pad]);
-        L -= static_cast<double>(j1[4 * s.ne_pad]);
+        for (int d = 0; d < 4; d++)
+          j1v[d] = j1[(1 + d) * s.ne_pad];
       }
+    }
+    T gx = 0, gy = 0, gz = 0, lp = 0;
+#pragma unroll 4
+    for (int o = 2 * lane; o < N; o += 64)
+    {
+      const bool h1 = o + 1 < N;
+      const T a0 = a[o], a1 = h1 ? a[o + 1] : T(0);
+      gx += a0 * g[o] + (h1 ? a1 * g[o + 1] : T(0));
+      gy += a0 * g[lda + o] + (h1 ? a1 * g[lda + o + 1] : T(0));
+      gz += a0 * g[2 * lda + o] + (h1 ? a1 * g[2 * lda + o + 1] : T(0));
+      lp += a0 * l[o] + (h1 ? a1 * l[o + 1] : T(0));
+    }
+    // lane sums in the move precision, the per-electron combination in FP64 on lane 0
+    // (FP64 arithmetic is slow on this GPU)
+    gx = warp_sum(gx);
+    gy = warp_sum(gy);
+    gz = warp_sum(gz);
+    lp = warp_sum(lp);
+    if (lane == 0)
+    {
+      double G[3] = {static_cast<double>(gx), static_cast<double>(gy), static_cast<double>(gz)};
+      double L    = static_cast<double>(lp) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        G[d] += static_cast<double>(j2v[d]) + static_cast<double>(j1v[d]);
+      L += static_cast<double>(j2v[3]) - static_cast<double>(j1v[3]);
       ke += -0.5 * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + L);
     }
   }
@@ -187,21 +239,21 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
   // ---------------- reciprocal space
   for (int g0 = 0; g0 < ew.ng; g0 += LE_NT * LE_GPT)
   {
-    T re[LE_GPT], im[LE_GPT];
-    int n1[LE_GPT], n2[LE_GPT], n3[LE_GPT];
+    T re[LE_GPT], im[LE_GPT], sg3[LE_GPT];
+    int i12[LE_GPT], a3[LE_GPT];
 #pragma unroll
     for (int q = 0; q < LE_GPT; q++)
     {
       const int g = g0 + tid + q * LE_NT;
       const char4 c = g < ew.ng ? ew.gn[g] : make_char4(0, 0, 0, 0);
-      n1[q] = c.x;
-      n2[q] = c.y;
-      n3[q] = c.z;
+      i12[q] = c.x * nb + c.y + ew.nmax;
+      a3[q]  = c.z < 0 ? -c.z : c.z;
+      sg3[q] = c.z < 0 ? T(-1) : T(1);
       re[q] = im[q] = T(0);
     }
-    for (int c0 = 0; c0 < ne; c0 += LE_CH)
+    for (int c0 = 0; c0 < ne; c0 += ch)
     {
-      const int cn = min(LE_CH, ne - c0);
+      const int cn = min(ch, ne - c0);
       __syncthreads();
       for (int e = tid; e < cn * 3 * nm1; e += LE_NT)
       {
@@ -213,20 +265,31 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
         tab[2 * e + 1] = sv;
       }
       __syncthreads();
+      // e1(n1) e2(n2) of every electron of the chunk; e2(-n) = conj(e2(n))
+      for (int e = tid; e < cn * nm1 * nb; e += LE_NT)
+      {
+        const int ci = e / (nm1 * nb), rem = e - ci * nm1 * nb, a = rem / nb, b = rem - a * nb - ew.nmax;
+        const T* t   = tab + (size_t)ci * 3 * nm1 * 2;
+        const T c1 = t[2 * a], s1 = t[2 * a + 1];
+        const int ab = b < 0 ? -b : b;
+        const T c2 = t[2 * (nm1 + ab)], s2 = b < 0 ? -t[2 * (nm1 + ab) + 1] : t[2 * (nm1 + ab) + 1];
+        t12[2 * e]     = c1 * c2 - s1 * s2;
+        t12[2 * e + 1] = s1 * c2 + c1 * s2;
+      }
+      __syncthreads();
       for (int ci = 0; ci < cn; ci++)
       {
-        const T* t = tab + (size_t)ci * 3 * nm1 * 2;
+        const T* t3 = tab + (size_t)ci * 3 * nm1 * 2 + 2 * (2 * nm1);
+        const T* u  = t12 + (size_t)ci * nm1 * nb * 2;
 #pragma unroll
         for (int q = 0; q < LE_GPT; q++)
-        {
-          const int a2 = n2[q] < 0 ? -n2[q] : n2[q], a3 = n3[q] < 0 ? -n3[q] : n3[q];
-          const T c1 = t[2 * n1[q]], s1 = t[2 * n1[q] + 1];
-          const T c2 = t[2 * (nm1 + a2)], s2 = n2[q] < 0 ? -t[2 * (nm1 + a2) + 1] : t[2 * (nm1 + a2) + 1];
-          const T c3 = t[2 * (2 * nm1 + a3)], s3 = n3[q] < 0 ? -t[2 * (2 * nm1 + a3) + 1] : t[2 * (2 * nm1 + a3) + 1];
-          const T c12 = c1 * c2 - s1 * s2, s12 = s1 * c2 + c1 * s2;
-          re[q] += c12 * c3 - s12 * s3;
-          im[q] += s12 * c3 + c12 * s3;
-        }
+          if (g0 + q * LE_NT < ew.ng) // uniform: the G slots past the last vector are skipped
+          {
+            const Cplx<T> p = ld_cplx(u + 2 * i12[q]), z = ld_cplx(t3 + 2 * a3[q]);
+            const T s3      = sg3[q] * z.y;
+            re[q] += p.x * z.x - p.y * s3;
+            im[q] += p.y * z.x + p.x * s3;
+          }
       }
     }
 #pragma unroll
@@ -263,10 +326,11 @@ cudaError_t setup_local_energy()
 template<typename T>
 cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st)
 {
-  const size_t sm = local_energy_smem(s.ne, ew.nmax, sizeof(T));
-  if (sm > 200 * 1024)
+  const int ch    = le_chunk(s.ne, ew.nmax, sizeof(T));
+  const size_t sm = le_smem_ch(s.ne, ew.nmax, sizeof(T), ch);
+  if (sm > LE_SMEM_MAX)
     return cudaErrorInvalidValue;
-  local_energy_kernel<T><<<s.nw, LE_NT, sm, st>>>(s, ew, out);
+  local_energy_kernel<T><<<s.nw, LE_NT, sm, st>>>(s, ew, out, ch);
   return cudaGetLastError();
 }
 
