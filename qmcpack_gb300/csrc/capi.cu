@@ -2297,16 +2297,21 @@ struct Group final : qmcg_group_s
   int g_drift = -1, g_flush = -1;
   std::vector<int> since_recompute;
 
+  cudaEvent_t ev_stage = nullptr; // end of a stage's launch: the crowds' updates fork from it
+
   ~Group() override
   {
     if (graph)
       cudaGraphExecDestroy(graph);
+    if (ev_stage)
+      cudaEventDestroy(ev_stage);
   }
 
   int init(const std::vector<Crowd<T>*>& crowds)
   {
     cs     = crowds;
     stream = cs[0]->stream;
+    CUDA_TRY(cudaEventCreateWithFlags(&ev_stage, cudaEventDisableTiming));
     since_recompute.assign(cs.size(), 0);
     for (auto* c : cs)
       smem = std::max(smem, sweep_smem_bytes<T>(c->s));
@@ -2413,11 +2418,15 @@ struct Group final : qmcg_group_s
     {
       const MultiStage& st = stages[j];
       CUDA_TRY(launch_sweep_multi<T>(table, st, smem, grid, work + j, stream, nt));
+      // the crowds' updates after the stage run side by side, each on its crowd's side
+      // stream, and the next stage waits for all of them
+      CUDA_TRY(cudaEventRecord(ev_stage, stream));
       for (int a = 0; a < st.nactive; a++)
       {
         Crowd<T>* x = cs[st.crowd[a]];
         if (x->k > 1)
         {
+          CUDA_TRY(cudaStreamWaitEvent(x->side, ev_stage, 0));
           const int sp = st.i0[a] >= x->sys->nup ? 1 : 0, first = sp ? x->sys->nup : 0;
           const int blk = (st.i0[a] - first) / x->k;
           if (x->lazy_updates())
@@ -2427,20 +2436,27 @@ struct Group final : qmcg_group_s
             const int nspin = sp ? x->sys->ne - x->sys->nup : x->sys->nup;
             const int nseg  = (nspin + x->k - 1) / x->k;
             if (blk + 1 < nseg)
-              CUDA_TRY(launch_block_update<T>(x->s, sp, blk + 1, 1, blk + 1, false, stream));
+              CUDA_TRY(launch_block_update<T>(x->s, sp, blk + 1, 1, blk + 1, false, x->side));
             else
-              CUDA_TRY(launch_block_update<T>(x->s, sp, 0, nseg, nseg, true, stream));
+              CUDA_TRY(launch_block_update<T>(x->s, sp, 0, nseg, nseg, true, x->side));
           }
           else
-            CUDA_TRY(x->launch_flush_choice(sp, st.i1[a] - st.i0[a], x->s.nsets > 1 ? blk : 0, stream));
+            CUDA_TRY(x->launch_flush_choice(sp, st.i1[a] - st.i0[a], x->s.nsets > 1 ? blk : 0, x->side));
+          CUDA_TRY(cudaEventRecord(x->ev_join, x->side));
+          CUDA_TRY(cudaStreamWaitEvent(stream, x->ev_join, 0));
         }
       }
     }
+    // the crowds' masked repairs, side by side
+    CUDA_TRY(cudaEventRecord(ev_stage, stream));
     for (auto* x : cs)
     {
-      CUDA_TRY(launch_recompute<T>(x->s, x->Mt, 1, stream));
-      bump_counter_kernel<<<1, 1, 0, stream>>>(x->s.sweep_counter);
+      CUDA_TRY(cudaStreamWaitEvent(x->side, ev_stage, 0));
+      CUDA_TRY(launch_recompute<T>(x->s, x->Mt, 1, x->side));
+      bump_counter_kernel<<<1, 1, 0, x->side>>>(x->s.sweep_counter);
       CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaEventRecord(x->ev_join, x->side));
+      CUDA_TRY(cudaStreamWaitEvent(stream, x->ev_join, 0));
     }
     return QMCG_OK;
   }
