@@ -662,22 +662,19 @@ def run_ours(args, rank: int, world: int):
     moves, ms = aggregate_timing(args.steps * nw * system.n_elec, ms)
     value = moves / (ms / 1e3)
 
-    # end to end through the C ABI with host buffers: H2D positions, sweep, D2H positions + log|psi|
-    # (the caller's buffers are pinned and reused every step, as a driver's walker buffers are)
+    # end to end through the C ABI with host buffers: one qmcg_vmc_sweeps_host call per step copies
+    # the positions in, sweeps, and copies the positions and log|psi| out (the caller's buffers are
+    # pinned and reused every step, as a driver's walker buffers are)
     restart()
-    Rh = torch.from_numpy(crowd.positions()).pin_memory()
-    Rnp = Rh.numpy()
-    log_out = tuple(torch.from_numpy(a).pin_memory().numpy()
-                    for a in (np.zeros(nw), np.zeros(nw, np.int32), np.zeros((nw, 4))))
+    Rnp = torch.from_numpy(crowd.positions()).pin_memory().numpy()
+    lp = torch.from_numpy(np.zeros(nw)).pin_memory().numpy()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        crowd.load_walkers(Rnp)
-        crowd.vmc_sweeps(1, spec.tau, seed, rng_mode=1, recompute_every=0, flush=args.flush)
-        crowd.positions(out=Rnp)
-        lp, _, _ = crowd.get_log(out=log_out)
+        crowd.vmc_sweeps_host(1, spec.tau, seed, R_in=Rnp, R_out=Rnp, log_out=lp, recompute_every=0,
+                              flush=args.flush)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0 + n_rec * rec_ms / 1e3
     _, e2e_s = aggregate_timing(0.0, e2e_s)

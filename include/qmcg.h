@@ -201,6 +201,16 @@ int qmcg_vmc_sweeps(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_s
  * graph must have been built by a previous qmcg_vmc_sweeps with rng_mode 1). */
 int qmcg_vmc_sweeps_async(qmcg_crowd crowd, int num_sweeps);
 
+/* The body of VMCBatched::advanceWalkers for walkers whose positions live in host
+ * memory (the driver's ParticleSet R): positions_in [nw][n_elec][3] copied in (NULL:
+ * keep the device's positions), num_sweeps as qmcg_vmc_sweeps (no accept log), then
+ * the positions and log|psi| [nw] copied back to positions_out and log_psi (either may
+ * be NULL), with a single synchronisation at the end.  positions_in may equal
+ * positions_out.  Pinned (page-locked) buffers make the copies DMA transfers. */
+int qmcg_vmc_sweeps_host(qmcg_crowd crowd, const qmcg_sweep_params* params, int num_sweeps,
+                         const double* positions_in, double* positions_out, double* log_psi,
+                         qmcg_sweep_stats* stats);
+
 /* Local energy E_L = T + V of every walker after all delayed updates
  * (QMCHamiltonian::mw_evaluate over BareKineticEnergy::mw_evaluate,
  * src/QMCHamiltonians/BareKineticEnergy.cpp:102-160, and the Coulomb terms

@@ -17,7 +17,7 @@ EXPORTS = [
     "qmcg_get_positions", "qmcg_mw_evaluate_log", "qmcg_mw_recompute_walkers", "qmcg_mw_prepare_group", "qmcg_mw_eval_grad",
     "qmcg_mw_make_move", "qmcg_mw_calc_ratio_grad", "qmcg_mw_accept_reject_move",
     "qmcg_mw_complete_updates", "qmcg_get_log", "qmcg_get_inverse", "qmcg_get_jastrow_state",
-    "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_crowd_sync",
+    "qmcg_get_phi_vgl", "qmcg_vmc_sweeps", "qmcg_vmc_sweeps_async", "qmcg_vmc_sweeps_host", "qmcg_crowd_sync",
     "qmcg_mw_update_inv_mat", "qmcg_mw_update_inv_mat_ex", "qmcg_mw_update_inv_mat_noalloc", "qmcg_profile_ratio",
     "qmcg_profile_sweep", "qmcg_sweep_info", "qmcg_mw_evaluate_local_energy", "qmcg_vmc_sweeps_measure",
     "qmcg_proposal_init", "qmcg_proposal_get_params", "qmcg_proposal_set_params", "qmcg_proposal_forward",
@@ -100,6 +100,7 @@ def load(path: str = LIB_PATH):
         "qmcg_get_phi_vgl": [vp, _dp],
         "qmcg_vmc_sweeps": [vp, C.POINTER(SweepParams), C.c_int, C.POINTER(SweepStats), _ip],
         "qmcg_vmc_sweeps_async": [vp, C.c_int],
+        "qmcg_vmc_sweeps_host": [vp, C.POINTER(SweepParams), C.c_int, _dp, _dp, _dp, C.POINTER(SweepStats)],
         "qmcg_crowd_sync": [vp, C.POINTER(SweepStats)],
         "qmcg_profile_ratio": [vp, C.c_int, _dp],
         "qmcg_profile_sweep": [vp, C.c_int, _dp],

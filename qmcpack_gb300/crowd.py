@@ -337,6 +337,23 @@ class Crowd:
     def vmc_sweeps_async(self, nsweeps: int):
         check(self.L.qmcg_vmc_sweeps_async(self.handle, nsweeps))
 
+    def vmc_sweeps_host(self, nsweeps: int, tau: float, seed: int, R_in: Optional[np.ndarray] = None,
+                        R_out: Optional[np.ndarray] = None, log_out: Optional[np.ndarray] = None,
+                        use_drift: bool = True, recompute_every: int = 0, flush: int = 0):
+        """Positions in from R_in, nsweeps device-RNG sweeps, positions and log|psi| out to R_out and
+        log_out (C-contiguous float64 arrays, e.g. pinned; any may be None) with one synchronisation."""
+        for a, shape in ((R_in, (self.nw, self.ne, 3)), (R_out, (self.nw, self.ne, 3)), (log_out, (self.nw,))):
+            assert a is None or (a.shape == shape and a.dtype == np.float64 and a.flags.c_contiguous)
+        p = SweepParams(tau=tau, use_drift=int(use_drift), rng_mode=1, seed=seed,
+                        recompute_every=recompute_every, path=0, flush=flush)
+        st = SweepStats()
+        check(self.L.qmcg_vmc_sweeps_host(self.handle, C.byref(p), nsweeps,
+                                          _p(R_in) if R_in is not None else None,
+                                          _p(R_out) if R_out is not None else None,
+                                          _p(log_out) if log_out is not None else None, C.byref(st)))
+        self.last_repaired = st.repaired
+        return st.accepted, st.rejected
+
     def sync(self):
         st = SweepStats()
         check(self.L.qmcg_crowd_sync(self.handle, C.byref(st)))

@@ -457,6 +457,8 @@ struct qmcg_crowd_s
   virtual int get_jastrow(double* j2, double* j1)        = 0;
   virtual int get_phi(double* phi)                       = 0;
   virtual int sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log) = 0;
+  virtual int sweeps_host(const qmcg_sweep_params* p, int n, const double* r_in, double* r_out, double* lp,
+                          qmcg_sweep_stats* st) = 0;
   virtual int sweeps_async(int n)                        = 0;
   virtual int profile_ratio(int niat, double* ms)        = 0;
   virtual int profile_sweep(int n, double* out)          = 0;
@@ -553,6 +555,18 @@ struct Crowd final : qmcg_crowd_s
   T* W       = nullptr; // flush scratch, [nw][k][lda]
   double* gauss_d = nullptr;
   double* unif_d  = nullptr;
+  // pinned staging of the per-sweep results read back: counters, flush error flag, status words,
+  // and the log|psi| parts (log|det| and sign per spin, Jastrow sums)
+  struct IoStage
+  {
+    unsigned long long* cnt = nullptr; // [3]
+    int* tce    = nullptr;             // [1]
+    int* status = nullptr;             // [nw]
+    double* la  = nullptr;             // [2 nw]
+    double* js  = nullptr;             // [2 nw]
+    int* sg     = nullptr;             // [2 nw]
+    void* block = nullptr;
+  } io;
   double* gauss_h = nullptr; // pinned
   double* unif_h  = nullptr; // pinned
   HostStream hs;
@@ -635,6 +649,8 @@ struct Crowd final : qmcg_crowd_s
       cudaGraphExecDestroy(graph);
     if (gauss_h)
       cudaFreeHost(gauss_h);
+    if (io.block)
+      cudaFreeHost(io.block);
     if (unif_h)
       cudaFreeHost(unif_h);
     if (e_hist)
@@ -761,6 +777,18 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(mem.alloc(&gauss_d, ng));
     CUDA_TRY(mem.alloc(&unif_d, nu));
     CUDA_TRY(cudaMallocHost(&gauss_h, ng * sizeof(double)));
+    {
+      const size_t nwz = (size_t)nw;
+      const size_t bytes = 4 * sizeof(unsigned long long) + 4 * nwz * sizeof(double) + (1 + 3 * nwz) * sizeof(int);
+      CUDA_TRY(cudaMallocHost(&io.block, bytes));
+      char* b   = static_cast<char*>(io.block);
+      io.cnt    = reinterpret_cast<unsigned long long*>(b);
+      io.la     = reinterpret_cast<double*>(b + 4 * sizeof(unsigned long long));
+      io.js     = io.la + 2 * nwz;
+      io.tce    = reinterpret_cast<int*>(io.js + 2 * nwz);
+      io.status = io.tce + 1;
+      io.sg     = io.status + nwz;
+    }
     CUDA_TRY(cudaMallocHost(&unif_h, nu * sizeof(double)));
     sweep_nt   = sweep_default_threads<T>(d);
     CUDA_TRY(sweep_grid<T>(d, &sweep_grid_size, false, sweep_nt));
@@ -963,19 +991,33 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 
-  int get_log(double* lp, int* sg, double* parts) override
+  // the log|psi| parts of every walker to the pinned staging buffer (asynchronous)
+  int enqueue_log()
   {
-    std::vector<double> la, js;
-    std::vector<int> sgn;
     jastrow_log_sums_kernel<T><<<(nw + 7) / 8, 256, 0, stream>>>(s.J2, s.J1, nw, sys->ne, s.ne_pad, jsum);
     CUDA_TRY(cudaGetLastError());
-    int rc = d2h(la, s.log_abs, 2 * (size_t)nw);
-    if (!rc)
-      rc = d2h(sgn, s.sign, 2 * (size_t)nw);
-    if (!rc)
-      rc = d2h(js, jsum, 2 * (size_t)nw);
+    CUDA_TRY(cudaMemcpyAsync(io.la, s.log_abs, 2 * (size_t)nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(io.sg, s.sign, 2 * (size_t)nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(io.js, jsum, 2 * (size_t)nw * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    return QMCG_OK;
+  }
+
+  int get_log(double* lp, int* sg, double* parts) override
+  {
+    int rc = enqueue_log();
     if (rc)
       return rc;
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    log_from_stage(lp, sg, parts);
+    return QMCG_OK;
+  }
+
+  // log|psi| = log|det up| + log|det down| + J1 + J2 and the sign, from the staged parts
+  void log_from_stage(double* lp, int* sg, double* parts) const
+  {
+    const double* la = io.la;
+    const double* js = io.js;
+    const int* sgn   = io.sg;
     for (int iw = 0; iw < nw; iw++)
     {
       const double u2 = js[iw], u1 = js[nw + iw];
@@ -992,7 +1034,6 @@ struct Crowd final : qmcg_crowd_s
         parts[iw * 4 + 3] = lj2;
       }
     }
-    return QMCG_OK;
   }
 
   int get_inverse(int spin, double* a) override
@@ -1971,7 +2012,7 @@ struct Crowd final : qmcg_crowd_s
   }
 
   int run_sweeps(const qmcg_sweep_params* p, int n, qmcg_sweep_stats* st, int* acc_log, bool measure,
-                 double* trace = nullptr)
+                 double* trace = nullptr, bool defer_sync = false)
   {
     if (!p || n < 0 || !(p->tau > 0) || (p->rng_mode != 0 && p->rng_mode != 1))
       return fail(QMCG_ERR_ARG, "bad sweep parameters");
@@ -2039,7 +2080,40 @@ struct Crowd final : qmcg_crowd_s
         sweeps_since_recompute = 0;
       }
     }
-    return measure ? QMCG_OK : sync(st);
+    return measure || defer_sync ? QMCG_OK : sync(st);
+  }
+
+  // positions from the caller's host buffer, n sweeps, positions and log|psi| back to host
+  // buffers, with one synchronisation at the end (every copy is stream-ordered; pinned
+  // buffers make them DMA transfers)
+  int sweeps_host(const qmcg_sweep_params* p, int n, const double* r_in, double* r_out, double* lp,
+                  qmcg_sweep_stats* st) override
+  {
+    const int ne = sys->ne, ne_pad = s.ne_pad;
+    const size_t bytes = (size_t)nw * ne * 3 * sizeof(double);
+    if (r_in)
+    {
+      CUDA_TRY(cudaMemcpyAsync(aos, r_in, bytes, cudaMemcpyHostToDevice, stream));
+      positions_from_caller_kernel<T><<<304, 256, 0, stream>>>(aos, s.R, s.Rt, nw, ne, ne_pad);
+      CUDA_TRY(cudaGetLastError());
+    }
+    int rc = run_sweeps(p, n, nullptr, nullptr, false, nullptr, true);
+    if (rc)
+      return rc;
+    if (r_out)
+    {
+      positions_to_caller_kernel<<<304, 256, 0, stream>>>(s.R, aos, nw, ne, ne_pad);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(r_out, aos, bytes, cudaMemcpyDeviceToHost, stream));
+    }
+    if (lp && (rc = enqueue_log()))
+      return rc;
+    if ((rc = enqueue_stats()))
+      return rc;
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (lp)
+      log_from_stage(lp, nullptr, nullptr);
+    return finish_stats(st);
   }
 
   int sweep_logged(int* acc_log)
@@ -2232,18 +2306,34 @@ struct Crowd final : qmcg_crowd_s
     return QMCG_OK;
   }
 
+  // the sweep counters, the flush error flag and the status words to the pinned staging
+  // buffer (asynchronous)
+  int enqueue_stats()
+  {
+    CUDA_TRY(cudaMemcpyAsync(io.tce, tc_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(io.cnt, s.counters, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(io.status, s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    return QMCG_OK;
+  }
+
   int sync(qmcg_sweep_stats* st) override
   {
-    unsigned long long c[3];
-    int tce = 0;
-    CUDA_TRY(cudaMemcpyAsync(&tce, tc_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    std::vector<int> stv(nw);
-    CUDA_TRY(cudaMemcpyAsync(c, s.counters, sizeof(c), cudaMemcpyDeviceToHost, stream));
-    CUDA_TRY(cudaMemcpyAsync(stv.data(), s.status, nw * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    int rc = enqueue_stats();
+    if (rc)
+      return rc;
     CUDA_TRY(cudaStreamSynchronize(stream));
+    return finish_stats(st);
+  }
+
+  // after the stream synchronised: the staged counters into st, the status words cleared,
+  // the flags turned into a status code
+  int finish_stats(qmcg_sweep_stats* st)
+  {
+    const unsigned long long* c = io.cnt;
+    const int tce = *io.tce;
     int any = 0;
-    for (int v : stv)
-      any |= v;
+    for (int iw = 0; iw < nw; iw++)
+      any |= io.status[iw];
     CUDA_TRY(cudaMemsetAsync(s.status, 0, nw * sizeof(int), stream));
     if (st)
     {
@@ -2645,6 +2735,11 @@ extern "C" int qmcg_vmc_sweeps(qmcg_crowd c, const qmcg_sweep_params* p, int n, 
   CROWD_CALL(c, sweeps(p, n, st, acc));
 }
 extern "C" int qmcg_vmc_sweeps_async(qmcg_crowd c, int n) { CROWD_CALL(c, sweeps_async(n)); }
+extern "C" int qmcg_vmc_sweeps_host(qmcg_crowd c, const qmcg_sweep_params* p, int n, const double* r_in,
+                                    double* r_out, double* log_psi, qmcg_sweep_stats* st)
+{
+  CROWD_CALL(c, sweeps_host(p, n, r_in, r_out, log_psi, st));
+}
 extern "C" int qmcg_proposal_init(qmcg_crowd c, uint64_t seed, double init_scale)
 {
   CROWD_CALL(c, proposal_init(seed, init_scale));
