@@ -128,7 +128,9 @@ def test_zero_output_layer_is_drift_diffusion():
 
 def test_learned_sampling_is_unbiased():
     """A random (untrained) proposal network still samples |psi|^2: the VMC energy
-    agrees with drift-diffusion's within 4 combined standard errors."""
+    agrees with drift-diffusion's within 2 combined standard errors (autocorrelation-
+    corrected).  A correct sampler misses a 2-sigma bound for about one seed in twenty;
+    the seeds here are fixed, and this one is at 1.2 sigma."""
     Crowd, DeviceSystem = _gpu()
     s = _small(prec=8, n=8, nw=256, delay=4, seed=15)
     ds = DeviceSystem(s)
@@ -149,7 +151,7 @@ def test_learned_sampling_is_unbiased():
         res[mode] = energy_statistics(el)
     a, b = res["plain"], res["learned"]
     print("plain", a, "learned", b)
-    assert abs(a["energy"] - b["energy"]) < 4 * np.hypot(a["error"], b["error"])
+    assert abs(a["energy"] - b["energy"]) < 2 * np.hypot(a["error"], b["error"])
 
 
 def test_training_lowers_the_objective():
@@ -211,7 +213,8 @@ def test_resident_zero_output_layer_is_drift_diffusion(flush):
 
 
 def test_resident_learned_sampling_is_unbiased():
-    """Walker-resident inference with a random network samples |psi|^2 (FP32 and FP64)."""
+    """Walker-resident inference with a random network samples |psi|^2 (FP32 and FP64):
+    energies within 2 combined standard errors (0.7 and 1.3 sigma with these seeds)."""
     Crowd, DeviceSystem = _gpu()
     for prec in (8, 4):
         s = _small(prec=prec, n=8, nw=256, delay=4, seed=35)
@@ -233,4 +236,4 @@ def test_resident_learned_sampling_is_unbiased():
             res[mode] = energy_statistics(el)
         a, b = res["plain"], res["learned"]
         print("precision", prec, "plain", a, "learned (resident)", b)
-        assert abs(a["energy"] - b["energy"]) < 4 * np.hypot(a["error"], b["error"])
+        assert abs(a["energy"] - b["energy"]) < 2 * np.hypot(a["error"], b["error"])
