@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from oracle import mlp_oracle as mo
-from qmcpack_gb300.stats import energy_statistics
+from qmcpack_gb300.stats import agree_within, ensemble_statistics, energy_statistics
 from qmcpack_gb300.system import make_system, make_walkers, scaled_spec
 
 pytestmark = pytest.mark.gpu
@@ -127,10 +127,11 @@ def test_zero_output_layer_is_drift_diffusion():
 
 
 def test_learned_sampling_is_unbiased():
-    """A random (untrained) proposal network still samples |psi|^2: the VMC energy
-    agrees with drift-diffusion's within 2 combined standard errors (autocorrelation-
-    corrected).  A correct sampler misses a 2-sigma bound for about one seed in twenty;
-    the seeds here are fixed, and this one is at 1.2 sigma."""
+    """A random (untrained) proposal network still samples |psi|^2: the VMC energy and
+    the variance of the local energy agree with drift-diffusion's within 2 combined
+    standard errors (autocorrelation-corrected).  A correct sampler misses a 2-sigma
+    bound for about one seed in twenty; the seeds here are fixed (the energies at 1.2
+    sigma)."""
     Crowd, DeviceSystem = _gpu()
     s = _small(prec=8, n=8, nw=256, delay=4, seed=15)
     ds = DeviceSystem(s)
@@ -148,10 +149,12 @@ def test_learned_sampling_is_unbiased():
             g.set_proposal_params(_params(np.random.default_rng(8), w4_scale=0.5))
             g.vmc_sweeps_learned(30, 0.3, 5, staged=True)
             _, _, el, _ = g.vmc_sweeps_learned(150, 0.3, 6, measure=True, staged=True)
-        res[mode] = energy_statistics(el)
-    a, b = res["plain"], res["learned"]
-    print("plain", a, "learned", b)
+        res[mode] = (energy_statistics(el), ensemble_statistics(el))
+    (a, ea), (b, eb) = res["plain"], res["learned"]
+    print("plain", a, "learned", b, "variance", ea["variance"], ea["variance_error"], eb["variance"],
+          eb["variance_error"])
     assert abs(a["energy"] - b["energy"]) < 2 * np.hypot(a["error"], b["error"])
+    assert agree_within(ea, eb, "variance", "variance_error")
 
 
 def test_training_lowers_the_objective():
@@ -214,7 +217,8 @@ def test_resident_zero_output_layer_is_drift_diffusion(flush):
 
 def test_resident_learned_sampling_is_unbiased():
     """Walker-resident inference with a random network samples |psi|^2 (FP32 and FP64):
-    energies within 2 combined standard errors (0.7 and 1.3 sigma with these seeds)."""
+    energies (0.7 and 1.3 sigma with these seeds) and variances within 2 combined standard
+    errors."""
     Crowd, DeviceSystem = _gpu()
     for prec in (8, 4):
         s = _small(prec=prec, n=8, nw=256, delay=4, seed=35)
@@ -233,7 +237,9 @@ def test_resident_learned_sampling_is_unbiased():
                 g.set_proposal_params(_params(np.random.default_rng(9), w4_scale=0.5))
                 g.vmc_sweeps_learned(30, 0.3, 5)
                 _, _, el, _ = g.vmc_sweeps_learned(200, 0.3, 6, measure=True)
-            res[mode] = energy_statistics(el)
-        a, b = res["plain"], res["learned"]
-        print("precision", prec, "plain", a, "learned (resident)", b)
+            res[mode] = (energy_statistics(el), ensemble_statistics(el))
+        (a, ea), (b, eb) = res["plain"], res["learned"]
+        print("precision", prec, "plain", a, "learned (resident)", b, "variance", ea["variance"],
+              ea["variance_error"], eb["variance"], eb["variance_error"])
         assert abs(a["energy"] - b["energy"]) < 2 * np.hypot(a["error"], b["error"])
+        assert agree_within(ea, eb, "variance", "variance_error")
