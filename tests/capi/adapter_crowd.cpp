@@ -11,6 +11,8 @@
 // output: float64 log_psi_after_recompute[nw], per move: grads_now[nw*3], ratios[nw],
 //         grads_new[nw*3]; then log_psi[nw], G[nw*ne*3], L[nw*ne], positions[nw*ne*3]
 //         after the electron-by-electron sweeps; accepted/rejected of one resident sweep.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -215,6 +217,22 @@ int main(int argc, char** argv)
     check(qmcg_vmc_sweeps(a.crowd, &p, 1, &st, nullptr));
     const double counts[2] = {static_cast<double>(st.accepted), static_cast<double>(st.rejected)};
     wr(out, counts, 2);
+    // the same with the walkers' positions in host buffers: in, one sweep, positions and
+    // log|psi| out in one call; they must equal what the separate getters return after it
+    std::vector<double> Pin((size_t)nw * ne * 3), Pout((size_t)nw * ne * 3), lph(nw), Pchk((size_t)nw * ne * 3),
+        lchk(nw);
+    check(qmcg_get_positions(a.crowd, Pin.data()));
+    qmcg_sweep_stats st2{};
+    check(qmcg_vmc_sweeps_host(a.crowd, &p, 1, Pin.data(), Pout.data(), lph.data(), &st2));
+    check(qmcg_get_positions(a.crowd, Pchk.data()));
+    check(qmcg_get_log(a.crowd, lchk.data(), nullptr, nullptr));
+    double dpos = 0, dlog = 0;
+    for (size_t e = 0; e < Pout.size(); e++)
+      dpos = std::max(dpos, std::fabs(Pout[e] - Pchk[e]));
+    for (int w = 0; w < nw; w++)
+      dlog = std::max(dlog, std::fabs(lph[w] - lchk[w]));
+    const double host_sweep[4] = {static_cast<double>(st2.accepted), static_cast<double>(st2.rejected), dpos, dlog};
+    wr(out, host_sweep, 4);
     std::fclose(out);
   }
   catch (const std::exception& e)

@@ -92,4 +92,6 @@ def test_adapter_against_oracle(tmp_path, delay):
     np.testing.assert_allclose(P, o.positions(), rtol=0, atol=1e-13)
     counts = take(2, (2,))
     assert counts.sum() == nw * ne and counts[0] > 0
+    acc2, rej2, dpos, dlog = take(4, (4,))
+    assert acc2 + rej2 == nw * ne and dpos == 0 and dlog == 0
     assert pos == out.size
