@@ -171,7 +171,9 @@ __global__ void __launch_bounds__(VP_NT) vp_ratio_kernel(DevState<T> s, int nvp,
       logj += s.J2[(size_t)w * 5 * s.ne_pad + e] - u2;
     if (s.has_j1)
       logj += s.J1[(size_t)w * 5 * s.ne_pad + e] - u1;
-    out[v] = static_cast<double>(det) * exp(static_cast<double>(logj));
+    // in the move-loop precision, as the move loop forms its ratios: one FP64 exp per move
+    // would cost the FP32 kernel a large share of its time on this GPU's FP64 pipe
+    out[v] = static_cast<double>(det * exp(logj));
   }
 }
 
