@@ -128,34 +128,19 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
   double ke = 0, vk = 0;
   CompSum<T> vr; // the ~300 pair terms of a thread
   // ---------------- kinetic energy: a warp per electron, lanes over orbital pairs (lda is
-  // even), the four sums of a row in flight together
-  for (int i = warp; i < ne; i += LE_NT / 32)
+  // even), the four sums of a row in flight together.  The per-electron combination runs in
+  // FP64 for 32 electrons at once: lane q keeps the sums of the warp's q-th electron of a
+  // batch (the FP64 pipe's time goes by warp instruction, whatever the active lanes)
+  T kg[4]  = {T(0), T(0), T(0), T(0)};
+  int kel  = -1; // the electron whose sums this lane keeps
+  int slot = 0;
+  for (int i = warp; i < ne; i += LE_NT / 32, slot = (slot + 1) & 31)
   {
     const int sp     = i < s.nup ? 0 : 1;
     const size_t rb  = ((size_t)sp * s.nw + iw) * N + (i - sp * s.nup);
     const T* a       = s.Ainv + rb * lda;
     const T* g       = s.dgrad + rb * 3 * lda;
     const T* l       = s.dlap + rb * lda;
-    // the Jastrow terms of this electron (gradient xyz, Laplacian), read by lane 0 ahead
-    // of the sums
-    T j2v[4] = {T(0), T(0), T(0), T(0)}, j1v[4] = {T(0), T(0), T(0), T(0)};
-    if (lane == 0)
-    {
-      if (s.has_j2)
-      {
-        const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + i;
-#pragma unroll
-        for (int d = 0; d < 4; d++)
-          j2v[d] = j2[(1 + d) * s.ne_pad];
-      }
-      if (s.has_j1)
-      {
-        const T* j1 = s.J1 + (size_t)iw * 5 * s.ne_pad + i;
-#pragma unroll
-        for (int d = 0; d < 4; d++)
-          j1v[d] = j1[(1 + d) * s.ne_pad];
-      }
-    }
     T gx = 0, gy = 0, gz = 0, lp = 0;
 #pragma unroll 4
     for (int o = 2 * lane; o < N; o += 64)
@@ -167,21 +152,48 @@ __global__ void __launch_bounds__(LE_NT) local_energy_kernel(DevState<T> s, Ewal
       gz += a0 * g[2 * lda + o] + (h1 ? a1 * g[2 * lda + o + 1] : T(0));
       lp += a0 * l[o] + (h1 ? a1 * l[o + 1] : T(0));
     }
-    // lane sums in the move precision, the per-electron combination in FP64 on lane 0
-    // (FP64 arithmetic is slow on this GPU)
+    // butterfly sums: every lane holds the same totals
     gx = warp_sum(gx);
     gy = warp_sum(gy);
     gz = warp_sum(gz);
     lp = warp_sum(lp);
-    if (lane == 0)
+    if (lane == slot)
     {
-      double G[3] = {static_cast<double>(gx), static_cast<double>(gy), static_cast<double>(gz)};
-      double L    = static_cast<double>(lp) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+      kg[0] = gx;
+      kg[1] = gy;
+      kg[2] = gz;
+      kg[3] = lp;
+      kel   = i;
+    }
+    if (slot == 31 || i + LE_NT / 32 >= ne)
+    {
+      if (kel >= 0)
+      {
+        // the Jastrow terms of the electron (gradient xyz, Laplacian)
+        T j2v[4] = {T(0), T(0), T(0), T(0)}, j1v[4] = {T(0), T(0), T(0), T(0)};
+        if (s.has_j2)
+        {
+          const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + kel;
 #pragma unroll
-      for (int d = 0; d < 3; d++)
-        G[d] += static_cast<double>(j2v[d]) + static_cast<double>(j1v[d]);
-      L += static_cast<double>(j2v[3]) - static_cast<double>(j1v[3]);
-      ke += -0.5 * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + L);
+          for (int d = 0; d < 4; d++)
+            j2v[d] = j2[(1 + d) * s.ne_pad];
+        }
+        if (s.has_j1)
+        {
+          const T* j1 = s.J1 + (size_t)iw * 5 * s.ne_pad + kel;
+#pragma unroll
+          for (int d = 0; d < 4; d++)
+            j1v[d] = j1[(1 + d) * s.ne_pad];
+        }
+        double G[3] = {static_cast<double>(kg[0]), static_cast<double>(kg[1]), static_cast<double>(kg[2])};
+        double L    = static_cast<double>(kg[3]) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+          G[d] += static_cast<double>(j2v[d]) + static_cast<double>(j1v[d]);
+        L += static_cast<double>(j2v[3]) - static_cast<double>(j1v[3]);
+        ke += -0.5 * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + L);
+      }
+      kel = -1;
     }
   }
 
