@@ -438,6 +438,24 @@ int qmcg_mw_update_inv_mat_noalloc(int precision, int num_walkers, int n, int ld
                                    void* ainv, const void* u, const void* v, const void* binv, const int* delay_list,
                                    void* stream);
 
+/* Orbital input (QMCPACK's ESHDF orbitals, EinsplineSetBuilderESHDF.fft.cpp and
+ * OneSplineOrbData::fft_spline, OneSplineOrbData.cpp:62-95, for real Gamma-point orbitals):
+ * the spline coefficient table of qmcg_system_desc.spline_coefs from the bands' plane-wave
+ * coefficients, which the caller has read from the ESHDF file.  Per band: the coefficients
+ * placed on the mesh (unpack4fftw), the backward 3-D transform psi(r) = sum_G c_G
+ * exp(+2 pi i G.r/mesh), unnormalized, the global phase rotation of fix_phase_rotate_c2r,
+ * and einspline's periodic cubic B-spline interpolation (set_multi_UBspline_3d_d), all on the
+ * GPU in FP64.
+ *   gvecs        [num_g][3] Miller indices (shared by the bands; distinct)
+ *   coefs_g      [num_orbitals][num_g][2] real, imaginary parts
+ *   mesh         grid points per axis (4..256), the spline grid of qmcg_system_desc.grid
+ *   spline_coefs host output [mesh0+3][mesh1+3][mesh2+3][num_orbitals_padded], float
+ *                (precision 4) or double (precision 8), zero beyond num_orbitals
+ *   phases       [num_orbitals][2] (phase_r, phase_i) of each band, may be NULL
+ * The HDF5 reading itself stays with the caller (no HDF5 library here). */
+int qmcg_spline_from_planewaves(int precision, int num_orbitals, int num_g, const int* gvecs, const double* coefs_g,
+                                const int mesh[3], int num_orbitals_padded, void* spline_coefs, double* phases);
+
 /* Measurement helper (no reference counterpart): average device time in ms of
  * the proposed-position evaluation kernel (distance rows, J1/J2, spline VGL and
  * determinant ratio) over num_electrons consecutive electrons, timed with CUDA

@@ -1,6 +1,7 @@
 #!/bin/sh
 # Builds oracle/_ref/libref.so: the reference's header-only tricubic spline evaluator
-# compiled in place from the reference's source tree (first argument, else
+# compiled in place from the reference's source tree (and libref_delayed.so, libref_bspline.so
+# for its delayed-update engine and its spline coefficient solve) (first argument, else
 # $QMCPACK_REFERENCE_DIR, else /root/reference), with a minimal config.h shim.
 # Test infrastructure only; skipped when the reference sources are absent.
 set -e
@@ -20,4 +21,9 @@ if [ -n "$BLAS" ]; then
     -I "$REF/src/Utilities" -I "$REF/src/Concurrency" \
     "$HERE/ref_delayed.cpp" -o "$HERE/_ref/libref_delayed.so" "$BLAS" -Wl,-rpath,"$BLASDIR" -Wl,--no-undefined
 fi
+# the reference's einspline coefficient solve (periodic cubic B-spline interpolation)
+${CC:-gcc} -O2 -std=gnu99 -fPIC -shared -Drestrict=__restrict__ -w \
+  -I "$HERE/ref_shim" -I "$REF/src/einspline" -I "$REF/src" \
+  "$HERE/ref_bspline.c" "$REF/src/einspline/bspline_create.c" "$REF/src/einspline/multi_bspline_create.c" \
+  -o "$HERE/_ref/libref_bspline.so"
 echo "built $HERE/_ref"

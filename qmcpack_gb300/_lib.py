@@ -25,7 +25,7 @@ EXPORTS = [
     "qmcg_group_create", "qmcg_group_destroy", "qmcg_group_sweeps", "qmcg_group_info", "qmcg_crowd_set_threads",
     "qmcg_mw_evaluate_gl", "qmcg_vmc_sweeps_trace", "qmcg_profile_recompute",
     "qmcg_dmc_init", "qmcg_dmc_step", "qmcg_dmc_copy_walkers", "qmcg_dmc_comb", "qmcg_dmc_reconfigure",
-    "qmcg_mw_evaluate_ratios", "qmcg_profile_ratios",
+    "qmcg_mw_evaluate_ratios", "qmcg_profile_ratios", "qmcg_spline_from_planewaves",
 ]
 TRACE_FIELDS = 12
 PROPOSAL_NUM_PARAMS = 43408
@@ -131,6 +131,7 @@ def load(path: str = LIB_PATH):
         "qmcg_dmc_reconfigure": [vp, C.c_double, _ip],
         "qmcg_mw_evaluate_ratios": [vp, C.c_int, _ip, _ip, _dp, _dp],
         "qmcg_profile_ratios": [vp, C.c_int, _ip, _ip, _dp, C.c_int, _dp],
+        "qmcg_spline_from_planewaves": [C.c_int, C.c_int, C.c_int, _ip, _dp, _ip, C.c_int, vp, _dp],
         "qmcg_mw_update_inv_mat": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp],
         "qmcg_mw_update_inv_mat_ex": [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                       C.c_int, vp],

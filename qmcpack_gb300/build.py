@@ -16,7 +16,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libqmcg.so")
 
 SOURCES = ["capi.cu", "move_kernels.cu", "recompute_kernels.cu", "sweep_kernel.cu", "flush_kernels.cu", "flush_tc.cu", "energy.cu", "learned.cu",
-           "noalloc.cu", "dmc.cu", "nlpp.cu", "block_update.cu"]
+           "noalloc.cu", "dmc.cu", "nlpp.cu", "block_update.cu",
+           "orbitals.cu"]
 HEADERS = ["common.cuh", "spline.cuh", "launch.h", "tc.cuh", "learned.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
