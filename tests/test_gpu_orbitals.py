@@ -50,3 +50,28 @@ def test_c1_sized_orbitals_timed():
     # spot check three bands against the oracle
     ref, _, _ = oo.spline_from_planewaves(gv, cg[:3], mesh, 16)
     assert np.abs(table[..., :3] - ref[..., :3]).max() <= 2e-6 * np.abs(ref).max()
+
+
+def test_system_from_planewave_orbitals():
+    """The table drives the move loop: a system whose orbitals come from plane waves gives
+    the FP64 oracle's log|psi| and inverse after mw_evaluateLog."""
+    import dataclasses
+
+    from oracle import oracle as orc
+    from qmcpack_gb300.crowd import Crowd, DeviceSystem
+    from qmcpack_gb300.system import make_system, make_walkers, scaled_spec
+    spec = scaled_spec("c0_32e", n_up=8, n_dn=8, grid=16, walkers=4, delay=1, precision=8)
+    s = make_system(spec, seed=3)
+    gv, cg = synthetic_planewaves(s.norb, (16, 16, 16), 5.0, seed=9)
+    table = spline_from_planewaves(gv, cg, (16, 16, 16), precision=8, num_orbitals_padded=s.npad)
+    s = dataclasses.replace(s, coefs=np.ascontiguousarray(table / np.abs(table).max()))
+    R = make_walkers(s, 4, seed=5)
+    g = Crowd(DeviceSystem(s), 4, 1)
+    g.load_walkers(R)
+    lg, _ = g.mw_evaluateLog()
+    o = orc.Crowd(s, 4, 1, 8)
+    o.load_walkers(R)
+    lo, _ = o.evaluate_log()
+    np.testing.assert_allclose(lg, lo, rtol=1e-10)
+    ai = o.ainv(0)
+    np.testing.assert_allclose(g.inverse(0), ai, rtol=0, atol=1e-10 * np.abs(ai).max())
