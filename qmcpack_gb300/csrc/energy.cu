@@ -360,30 +360,50 @@ cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, dou
 template<typename T>
 __global__ void __launch_bounds__(256) evaluate_gl_kernel(DevState<T> s, double* __restrict__ gl)
 {
+  // a warp per 32 consecutive electrons: the row sums of one electron at a time over the
+  // lanes, then the FP64 combination for all 32 at once, lane q holding electron i0 + q (the
+  // FP64 pipe's time goes by warp instruction, whatever the active lanes)
   const int iw = blockIdx.y, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (i >= s.ne)
+  const int i0 = (blockIdx.x * 8 + (threadIdx.x >> 5)) * 32;
+  if (i0 >= s.ne)
     return;
   const int N = s.norb, lda = s.lda;
-  const int sp    = i < s.nup ? 0 : 1;
-  const size_t rb = ((size_t)sp * s.nw + iw) * N + (i - sp * s.nup);
-  const T* a      = s.Ainv + rb * lda;
-  const T* g      = s.dgrad + rb * 3 * lda;
-  const T* l      = s.dlap + rb * lda;
-  T gx = 0, gy = 0, gz = 0, lp = 0;
-  for (int o = lane; o < N; o += 32)
+  const int cnt = min(32, s.ne - i0);
+  T kg[4] = {T(0), T(0), T(0), T(0)};
+  for (int q = 0; q < cnt; q++)
   {
-    const T av = a[o];
-    gx += av * g[o];
-    gy += av * g[lda + o];
-    gz += av * g[2 * lda + o];
-    lp += av * l[o];
+    const int i     = i0 + q;
+    const int sp    = i < s.nup ? 0 : 1;
+    const size_t rb = ((size_t)sp * s.nw + iw) * N + (i - sp * s.nup);
+    const T* a      = s.Ainv + rb * lda;
+    const T* g      = s.dgrad + rb * 3 * lda;
+    const T* l      = s.dlap + rb * lda;
+    T gx = 0, gy = 0, gz = 0, lp = 0;
+    for (int o = lane; o < N; o += 32)
+    {
+      const T av = a[o];
+      gx += av * g[o];
+      gy += av * g[lda + o];
+      gz += av * g[2 * lda + o];
+      lp += av * l[o];
+    }
+    gx = warp_sum(gx);
+    gy = warp_sum(gy);
+    gz = warp_sum(gz);
+    lp = warp_sum(lp);
+    if (lane == q)
+    {
+      kg[0] = gx;
+      kg[1] = gy;
+      kg[2] = gz;
+      kg[3] = lp;
+    }
   }
-  double G[3] = {static_cast<double>(warp_sum(gx)), static_cast<double>(warp_sum(gy)),
-                 static_cast<double>(warp_sum(gz))};
-  double L    = static_cast<double>(warp_sum(lp)) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
-  if (lane != 0)
+  if (lane >= cnt)
     return;
+  const int i = i0 + lane;
+  double G[3] = {static_cast<double>(kg[0]), static_cast<double>(kg[1]), static_cast<double>(kg[2])};
+  double L    = static_cast<double>(kg[3]) - (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
   if (s.has_j2)
   {
     const T* j2 = s.J2 + (size_t)iw * 5 * s.ne_pad + i;
@@ -410,7 +430,7 @@ __global__ void __launch_bounds__(256) evaluate_gl_kernel(DevState<T> s, double*
 template<typename T>
 cudaError_t launch_evaluate_gl(const DevState<T>& s, double* gl, cudaStream_t st)
 {
-  const dim3 grid((s.ne + 7) / 8, s.nw);
+  const dim3 grid((s.ne + 255) / 256, s.nw);
   evaluate_gl_kernel<T><<<grid, 256, 0, st>>>(s, gl);
   return cudaGetLastError();
 }
