@@ -452,7 +452,9 @@ int qmcg_mw_update_inv_mat_noalloc(int precision, int num_walkers, int n, int ld
  *   spline_coefs host output [mesh0+3][mesh1+3][mesh2+3][num_orbitals_padded], float
  *                (precision 4) or double (precision 8), zero beyond num_orbitals
  *   phases       [num_orbitals][2] (phase_r, phase_i) of each band, may be NULL
- * The HDF5 reading itself stays with the caller (no HDF5 library here). */
+ * The HDF5 reading itself stays with the caller (no HDF5 library here).  Synchronous: it
+ * allocates its device scratch (about 40 bytes per band and mesh point), works on the default
+ * stream and returns with the table in spline_coefs. */
 int qmcg_spline_from_planewaves(int precision, int num_orbitals, int num_g, const int* gvecs, const double* coefs_g,
                                 const int mesh[3], int num_orbitals_padded, void* spline_coefs, double* phases);
 
