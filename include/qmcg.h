@@ -246,7 +246,10 @@ int qmcg_mw_evaluate_gl(qmcg_crowd crowd, double* log_psi, double* grads, double
  * J1OrbitalSoA::evaluateRatios, J1OrbitalSoA.h:295-299).  The virtual moves of every walker
  * form one flat list of num_moves entries: walker [num_moves], electron [num_moves],
  * pos [num_moves][3] (bohr, FP64 host arrays); ratios [num_moves] FP64.  Nothing of the
- * walkers changes.  Returns QMCG_ERR_STATE while delayed updates are pending. */
+ * walkers changes.  Returns QMCG_ERR_STATE while delayed updates are pending, and
+ * QMCG_ERR_ARG naming the first move whose walker or electron is out of range or whose
+ * position is not finite (checked on the GPU; that move's ratio is NaN, the others are
+ * computed). */
 int qmcg_mw_evaluate_ratios(qmcg_crowd crowd, int num_moves, const int* walker, const int* electron, const double* pos,
                             double* ratios);
 

@@ -627,13 +627,18 @@ struct Crowd final : qmcg_crowd_s
     int* elec      = nullptr;
     double* pos    = nullptr;
     double* ratios = nullptr;
+    int* bad       = nullptr; // the first invalid move (INT_MAX: none)
+    int* bad_h     = nullptr; // pinned copy
     void release()
     {
       cudaFree(walker);
       cudaFree(elec);
       cudaFree(pos);
       cudaFree(ratios);
-      walker = elec = nullptr;
+      cudaFree(bad);
+      if (bad_h)
+        cudaFreeHost(bad_h);
+      walker = elec = bad = bad_h = nullptr;
       pos = ratios = nullptr;
       cap          = 0;
     }
@@ -1497,13 +1502,6 @@ struct Crowd final : qmcg_crowd_s
       return fail(QMCG_ERR_ARG, "bad virtual-move arguments");
     if (dc[0] || dc[1])
       return fail(QMCG_ERR_STATE, "virtual-move ratios need mw_completeUpdates first");
-    for (int v = 0; v < nvp; v++)
-    {
-      if (walker[v] < 0 || walker[v] >= nw || elec[v] < 0 || elec[v] >= sys->ne)
-        return fail(QMCG_ERR_ARG, "virtual move " + std::to_string(v) + ": walker or electron out of range");
-      if (!std::isfinite(pos[3 * v]) || !std::isfinite(pos[3 * v + 1]) || !std::isfinite(pos[3 * v + 2]))
-        return fail(QMCG_ERR_ARG, "virtual move " + std::to_string(v) + ": non-finite position");
-    }
     if (nvp == 0)
       return QMCG_OK;
     if ((size_t)nvp > vp.cap)
@@ -1514,14 +1512,22 @@ struct Crowd final : qmcg_crowd_s
       CUDA_TRY(cudaMalloc(&vp.elec, nvp * sizeof(int)));
       CUDA_TRY(cudaMalloc(&vp.pos, 3 * (size_t)nvp * sizeof(double)));
       CUDA_TRY(cudaMalloc(&vp.ratios, nvp * sizeof(double)));
+      CUDA_TRY(cudaMalloc(&vp.bad, sizeof(int)));
+      CUDA_TRY(cudaMallocHost(&vp.bad_h, sizeof(int)));
       vp.cap = nvp;
     }
+    // the moves' walker and electron indices and positions are checked by the kernel
+    CUDA_TRY(cudaMemsetAsync(vp.bad, 0x7f, sizeof(int), stream));
     CUDA_TRY(cudaMemcpyAsync(vp.walker, walker, nvp * sizeof(int), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(vp.elec, elec, nvp * sizeof(int), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(vp.pos, pos, 3 * (size_t)nvp * sizeof(double), cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, stream));
+    CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, vp.bad, stream));
     CUDA_TRY(cudaMemcpyAsync(ratios, vp.ratios, nvp * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(vp.bad_h, vp.bad, sizeof(int), cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
+    if (*vp.bad_h != 0x7f7f7f7f)
+      return fail(QMCG_ERR_ARG, "virtual move " + std::to_string(*vp.bad_h) +
+                                    ": walker or electron out of range, or non-finite position");
     return QMCG_OK;
   }
 
@@ -1540,7 +1546,7 @@ struct Crowd final : qmcg_crowd_s
     CUDA_TRY(cudaEventCreate(&b));
     CUDA_TRY(cudaEventRecord(a, stream));
     for (int i = 0; i < reps; i++)
-      CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, stream));
+      CUDA_TRY(launch_vp_ratios<T>(s, nvp, vp.walker, vp.elec, vp.pos, vp.ratios, vp.bad, stream));
     CUDA_TRY(cudaEventRecord(b, stream));
     CUDA_TRY(cudaEventSynchronize(b));
     float t = 0;

@@ -125,10 +125,12 @@ cudaError_t setup_local_energy();
 // out: [3][nw] doubles = local energy, kinetic, potential
 template<typename T>
 cudaError_t launch_local_energy(const DevState<T>& s, const EwaldDev<T>& ew, double* out, cudaStream_t st);
-// ratios of virtual moves (nlpp.cu): out[v] = psi(R, electron elec[v] at pos[v]) / psi(R) of walker walker[v]
+// ratios of virtual moves (nlpp.cu): out[v] = psi(R, electron elec[v] at pos[v]) / psi(R) of walker walker[v];
+// a move whose walker or electron is out of range or whose position is not finite gets a NaN ratio
+// and its index lowers *bad (atomicMin; the caller sets it to INT_MAX)
 template<typename T>
 cudaError_t launch_vp_ratios(const DevState<T>& s, int nvp, const int* walker, const int* elec, const double* pos,
-                             double* out, cudaStream_t st);
+                             double* out, int* bad, cudaStream_t st);
 // diffusion Monte Carlo (dmc.cu)
 cudaError_t launch_dmc_branch(int nw, const double* e_new, double* e_old, double* weight, int* age, double* rr,
                               const double* par, double* sums, double* w_out, cudaStream_t st);

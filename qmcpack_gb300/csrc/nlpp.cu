@@ -66,7 +66,7 @@ template<typename T>
 __global__ void __launch_bounds__(VP_NT) vp_ratio_kernel(DevState<T> s, int nvp, const int* __restrict__ vp_walker,
                                                          const int* __restrict__ vp_elec,
                                                          const double* __restrict__ vp_pos,
-                                                         double* __restrict__ out)
+                                                         double* __restrict__ out, int* __restrict__ bad)
 {
   constexpr int W = VpVec<T>::W;
   const int lane = threadIdx.x & 31;
@@ -74,8 +74,18 @@ __global__ void __launch_bounds__(VP_NT) vp_ratio_kernel(DevState<T> s, int nvp,
   if (v >= nvp)
     return;
   const int w = vp_walker[v], e = vp_elec[v];
-  const int spin = e >= s.nup ? 1 : 0, row = e - spin * s.nup;
   const double pos[3] = {vp_pos[3 * v], vp_pos[3 * v + 1], vp_pos[3 * v + 2]};
+  // the arguments are checked here, not on the host: an invalid move reads nothing
+  if (w < 0 || w >= s.nw || e < 0 || e >= s.ne || !isfinite(pos[0]) || !isfinite(pos[1]) || !isfinite(pos[2]))
+  {
+    if (lane == 0)
+    {
+      out[v] = nan("");
+      atomicMin(bad, v);
+    }
+    return;
+  }
+  const int spin = e >= s.nup ? 1 : 0, row = e - spin * s.nup;
   // ---------------- determinant: orbital values at r' against the inverse row
   T ru[3];
   spline_frac(s, pos, ru);
@@ -179,18 +189,18 @@ __global__ void __launch_bounds__(VP_NT) vp_ratio_kernel(DevState<T> s, int nvp,
 
 template<typename T>
 cudaError_t launch_vp_ratios(const DevState<T>& s, int nvp, const int* walker, const int* elec, const double* pos,
-                             double* out, cudaStream_t st)
+                             double* out, int* bad, cudaStream_t st)
 {
   if (nvp <= 0)
     return cudaSuccess;
   const int grid = (nvp + VP_NT / 32 - 1) / (VP_NT / 32);
-  vp_ratio_kernel<T><<<grid, VP_NT, 0, st>>>(s, nvp, walker, elec, pos, out);
+  vp_ratio_kernel<T><<<grid, VP_NT, 0, st>>>(s, nvp, walker, elec, pos, out, bad);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_vp_ratios<float>(const DevState<float>&, int, const int*, const int*, const double*,
-                                             double*, cudaStream_t);
+                                             double*, int*, cudaStream_t);
 template cudaError_t launch_vp_ratios<double>(const DevState<double>&, int, const int*, const int*, const double*,
-                                              double*, cudaStream_t);
+                                              double*, int*, cudaStream_t);
 
 } // namespace qmcg

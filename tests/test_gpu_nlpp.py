@@ -102,3 +102,34 @@ def test_virtual_move_ratios_fp32_c1():
             f.write(json.dumps({"workload": "c1_384e_virtual_moves", **table}) + "\n")
     assert table["ratio_rel"]["median"] < 1e-4
     assert table["ratio_rel_away_from_nodes"]["p99"] < 1e-2
+
+
+def test_invalid_virtual_moves_are_rejected_on_the_device():
+    """Walker or electron indices out of range and non-finite positions are caught by the
+    kernel before it reads anything: the call returns QMCG_ERR_ARG naming the first such move,
+    and the crowd stays usable."""
+    from qmcpack_gb300._lib import QmcgError
+    Crowd, DeviceSystem = _gpu()
+    nw = 4
+    spec = scaled_spec("c0_32e", n_up=8, n_dn=8, grid=12, walkers=nw, delay=1, precision=8)
+    s = make_system(spec, seed=81)
+    g = Crowd(DeviceSystem(s), nw, 1)
+    R = make_walkers(s, nw, seed=82)
+    g.load_walkers(R)
+    g.mw_evaluateLog()
+    w = np.array([0, 1, 2, 3, 1])
+    e = np.array([0, 3, 5, 7, 2])
+    pos = R[w, e] + 0.1
+    good = g.mw_evaluateRatios(w, e, pos)
+    assert np.all(np.isfinite(good))
+    for bad_w, bad_e, bad_p, first in ((nw, 3, None, 1), (1, s.n_elec, None, 1), (1, -1, None, 1),
+                                       (1, 3, np.nan, 1), (-1, 3, np.inf, 1)):
+        ww, ee, pp = w.copy(), e.copy(), pos.copy()
+        ww[first], ee[first] = bad_w, bad_e
+        if bad_p is not None:
+            pp[first, 2] = bad_p
+        ww[4] = nw + 5  # a later invalid move: the first one is reported
+        with pytest.raises(QmcgError) as ex:
+            g.mw_evaluateRatios(ww, ee, pp)
+        assert f"virtual move {first}:" in str(ex.value)
+    np.testing.assert_array_equal(g.mw_evaluateRatios(w, e, pos), good)
