@@ -643,7 +643,7 @@ struct Crowd final : qmcg_crowd_s
       cap          = 0;
     }
   } vp;
-  double* gl_d    = nullptr; // [nw][ne][4] per-electron gradient and Laplacian of log psi
+  double* gl_d    = nullptr; // per-electron gradient [nw][ne][3], then Laplacian [nw][ne], of log psi
   double* e_out  = nullptr; // [3][nw] local energy, kinetic, potential
   double* e_hist = nullptr; // [e_hist_cap][2][nw] per-sweep local and kinetic energies
   size_t e_hist_cap = 0;
@@ -1590,19 +1590,15 @@ struct Crowd final : qmcg_crowd_s
     if (!gl_d)
       CUDA_TRY(mem.alloc(&gl_d, n * 4));
     CUDA_TRY(launch_evaluate_gl<T>(s, gl_d, stream));
-    std::vector<double> h;
-    int rc = d2h(h, static_cast<const double*>(gl_d), n * 4);
-    if (rc)
-      return rc;
-    for (size_t e = 0; e < n; e++)
-    {
-      if (grads)
-        for (int d = 0; d < 3; d++)
-          grads[e * 3 + d] = h[e * 4 + d];
-      if (laps)
-        laps[e] = h[e * 4 + 3];
-    }
-    return lp ? get_log(lp, nullptr, nullptr) : QMCG_OK;
+    // the kernel writes the caller's layouts: straight copies, no host pass
+    if (grads)
+      CUDA_TRY(cudaMemcpyAsync(grads, gl_d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (laps)
+      CUDA_TRY(cudaMemcpyAsync(laps, gl_d + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (lp)
+      return get_log(lp, nullptr, nullptr);
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    return QMCG_OK;
   }
 
   // QMCHamiltonian::mw_evaluate for kinetic + Coulomb after all delayed updates

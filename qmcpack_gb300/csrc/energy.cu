@@ -420,11 +420,12 @@ __global__ void __launch_bounds__(256) evaluate_gl_kernel(DevState<T> s, double*
       G[d] += static_cast<double>(j1[(1 + d) * s.ne_pad]);
     L -= static_cast<double>(j1[4 * s.ne_pad]);
   }
-  double* o = gl + ((size_t)iw * s.ne + i) * 4;
-  o[0]      = G[0];
-  o[1]      = G[1];
-  o[2]      = G[2];
-  o[3]      = L;
+  // G [nw][ne][3] then L [nw][ne], the caller's layouts
+  const size_t e = (size_t)iw * s.ne + i;
+  gl[3 * e]     = G[0];
+  gl[3 * e + 1] = G[1];
+  gl[3 * e + 2] = G[2];
+  gl[3 * (size_t)s.nw * s.ne + e] = L;
 }
 
 template<typename T>
